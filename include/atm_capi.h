@@ -1,0 +1,208 @@
+/*
+ * atm_capi.h - C ABI of the GB300 atmosphere path (LUT builds + per-pixel
+ * composite).  Plain pointers, sizes and a cudaStream_t passed as void*; no
+ * C++ or torch types.  Every entry point returns 0 on success or a negative
+ * ATM_E* code; atm_last_error() gives the message of the calling thread's
+ * last failure.  Every launch is stream-ordered on the caller's stream and
+ * never synchronises the host, except where a function says so.
+ *
+ * Reference interface replaced: the Taichi class AtmosphereRenderer in
+ * src/planet_renderer/atmosphere/renderer.py (constructor :51-116, update
+ * :2072-2137, prepare_frame :2139-2187, composite :2189-2238,
+ * set_luts_frozen :2057-2070) and its kernels _build_transmittance :1034,
+ * _build_multi_scattering :1065, _build_sky_view :1208,
+ * _build_aerial_perspective :1304, _prepare_surface_lighting :1422,
+ * _composite :1827.  The Python layer (planet_renderer_gb300.atmosphere)
+ * keeps that class's method names and argument meaning on top of this ABI.
+ *
+ * Conventions (reference renderer.py:44-49, renderer.py(top):1150):
+ *  - vectors are in the camera's local East-Up-North frame; the camera is at
+ *    the origin and the planet centre at (0, -camera_radius, 0);
+ *  - position_view is the view-space (right, up, forward) hit position;
+ *  - surface_id < 0 marks a sky pixel;
+ *  - pixel (x, y) has screen_v = (y + 0.5) / height, increasing upward;
+ *  - per-pixel images are addressed as base + (x*stride_x + y*stride_y)
+ *    elements, each element `channels` floats (3 or 4).  The Taichi
+ *    to_numpy() layout (W, H, 3) is stride_x = H, stride_y = 1, channels 3;
+ *  - LUT read-back (atm_get_lut) is in the Taichi field layout (W, H[, D], 3).
+ */
+#ifndef ATM_CAPI_H
+#define ATM_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes. */
+#define ATM_OK 0
+#define ATM_E_INVALID (-1)     /* bad argument: null pointer, size, range  */
+#define ATM_E_CUDA (-2)        /* a CUDA call failed                        */
+#define ATM_E_NOMEM (-3)       /* device allocation failed                  */
+#define ATM_E_STATE (-4)       /* call order: e.g. composite before update  */
+#define ATM_E_TIMEOUT (-5)     /* a bounded device wait gave up             */
+
+/* Diagnostic views of the composite (reference diagnostics.py:15-25). */
+#define ATM_VIEW_COMPOSITE 0
+#define ATM_VIEW_SKY_VIEW 1
+#define ATM_VIEW_CAMERA_TRANSMITTANCE 2
+#define ATM_VIEW_TRANSMITTANCE_LUT 3
+#define ATM_VIEW_MULTI_SCATTERING_LUT 4
+#define ATM_VIEW_AERIAL_SCATTERING 5
+#define ATM_VIEW_AERIAL_TRANSMITTANCE 6
+#define ATM_VIEW_SURFACE_MASK 7
+#define ATM_VIEW_AERIAL_FROXEL_ONLY 8
+#define ATM_VIEW_AERIAL_DIRECT_ONLY 9
+#define ATM_VIEW_AERIAL_BLEND_WEIGHT 10
+
+/* LUT kinds for atm_get_lut. */
+#define ATM_LUT_TRANSMITTANCE 0
+#define ATM_LUT_MULTI_SCATTERING 1
+#define ATM_LUT_SKY_VIEW 2
+#define ATM_LUT_AERIAL 3
+
+/*
+ * Optical parameters and LUT quality of one spherical atmosphere.  Field for
+ * field the reference's AtmosphereConfig (atmosphere/config.py:29-59); the
+ * planet radius is passed per call, as in the reference.  Lengths in metres,
+ * coefficients in 1/m.  Values are double, as Python floats are; kernels
+ * round them to float exactly where the Taichi trace would.
+ */
+typedef struct AtmParams {
+  double top_altitude_m;
+  double rayleigh_scattering_per_m[3];
+  double rayleigh_scale_height_m;
+  double mie_scattering_per_m[3];
+  double mie_extinction_per_m[3];
+  double mie_scale_height_m;
+  double mie_phase_g;
+  double absorption_extinction_per_m[3];
+  double absorption_peak_altitude_m;
+  double absorption_half_width_m;
+  double ground_albedo[3];
+  int32_t transmittance_lut_width;
+  int32_t transmittance_lut_height;
+  int32_t multi_scattering_lut_width;
+  int32_t multi_scattering_lut_height;
+  int32_t sky_view_lut_width;
+  int32_t sky_view_lut_height;
+  int32_t aerial_lut_width;
+  int32_t aerial_lut_height;
+  int32_t aerial_lut_depth;
+  int32_t transmittance_steps;
+  int32_t multi_scattering_directions;
+  int32_t multi_scattering_steps;
+  int32_t sky_view_steps;
+  int32_t aerial_steps_per_slice;
+  int32_t aerial_horizon_raymarch_steps;
+  int32_t aerial_terminator_substeps;
+} AtmParams;
+
+/* Addressing of the caller's per-pixel images (G-buffer, scene, space, hdr,
+ * surface-lighting outputs).  All images of one call share it; surface_id
+ * uses the same element strides with one int32 per element. */
+typedef struct AtmImage {
+  int32_t width;
+  int32_t height;
+  int64_t stride_x; /* elements between (x, y) and (x+1, y) */
+  int64_t stride_y; /* elements between (x, y) and (x, y+1) */
+  int32_t channels; /* floats per element of the float images: 3 or 4 */
+} AtmImage;
+
+/* Host-visible state of a renderer: the reference's public attributes
+ * (atmosphere/renderer.py:97-116). has_* = 0 stands for Python None. */
+typedef struct AtmState {
+  int32_t luts_frozen;
+  int32_t has_sky_snapshot;
+  double sky_snapshot_altitude_m;
+  double sky_snapshot_sun_cosine;
+  int32_t has_aerial_snapshot;
+  double aerial_snapshot_altitude_m;
+  int64_t transmittance_rebuilds;
+  int64_t multi_scattering_rebuilds;
+  int64_t sky_view_rebuilds;
+  int64_t aerial_rebuilds;
+} AtmState;
+
+/* Explicit inputs of one LUT build (atm_build_lut), bypassing the cache
+ * keys of atm_update / atm_prepare_frame.  Angles in radians here. */
+typedef struct AtmBuildArgs {
+  double planet_radius_m;
+  double camera_altitude_m;
+  double sun_zenith_cosine;       /* sky-view                       */
+  double sun_local[3];            /* aerial perspective             */
+  double solar_irradiance[3];
+  double sun_angular_radius_rad;
+  double view_basis[9];           /* right, up, forward (aerial)    */
+  double tangent_half_fov;        /* aerial                         */
+  int32_t frame_width;            /* aerial: aspect = width/height  */
+  int32_t frame_height;
+} AtmBuildArgs;
+
+typedef struct AtmHandle AtmHandle;
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char* atm_last_error(void);
+
+/* Allocate a renderer for width x height frames on the current CUDA device:
+ * the four LUTs (zero-filled, as Taichi fields are) and a radiance-sample
+ * counter.  Validates params with the reference's ranges
+ * (atmosphere/config.py:61-128).  Replaces AtmosphereRenderer.__init__
+ * (atmosphere/renderer.py:51-116). */
+int atm_create(const AtmParams* params, int32_t width, int32_t height, AtmHandle** out);
+int atm_destroy(AtmHandle* handle);
+
+/* AtmosphereRenderer.set_luts_frozen (renderer.py:2057-2070). */
+int atm_set_luts_frozen(AtmHandle* handle, int32_t frozen);
+int atm_get_state(const AtmHandle* handle, AtmState* out);
+
+/* AtmosphereRenderer.update (renderer.py:2072-2137): rebuild the
+ * transmittance, multi-scattering and sky-view LUTs whose cache keys
+ * changed; keys, float rounding points and counters as in the reference. */
+int atm_update(AtmHandle* handle, double planet_radius_m, double camera_radius_m, const double sun_local[3],
+               const double solar_irradiance[3], double sun_angular_radius_degrees, void* stream);
+
+/* AtmosphereRenderer.prepare_frame (renderer.py:2139-2187): per surface
+ * pixel sun transmittance and sky radiance into the caller's two images,
+ * then the aerial-perspective volume unless frozen. view_basis = right, up,
+ * forward (9 doubles). */
+int atm_prepare_frame(AtmHandle* handle, const float* position_view, const int32_t* surface_id,
+                      const AtmImage* image, double planet_radius_m, double camera_radius_m,
+                      const double sun_local[3], const double solar_irradiance[3],
+                      double sun_angular_radius_degrees, const double view_basis[9], double tangent_half_fov,
+                      float* surface_sun_transmittance, float* surface_sky_radiance, void* stream);
+
+/* AtmosphereRenderer.composite (renderer.py:2189-2238) -> hdr. */
+int atm_composite(AtmHandle* handle, const float* scene_hdr, const float* space_hdr, const int32_t* surface_id,
+                  const float* position_view, float* hdr, const AtmImage* image, double planet_radius_m,
+                  double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
+                  const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                  const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                  double star_contrast_end, int32_t diagnostic_view, void* stream);
+
+/* Build one LUT from explicit inputs (no cache keys, counters untouched):
+ * the kernels _build_transmittance :1034, _build_multi_scattering :1065,
+ * _build_sky_view :1208, _build_aerial_perspective :1304. */
+int atm_build_lut(AtmHandle* handle, int32_t kind, const AtmBuildArgs* args, void* stream);
+
+/* Dimensions (w, h, d; d = 1 for 2-D) and device storage of a LUT: float4
+ * texels, row-major [z][y][x]. */
+int atm_lut_info(const AtmHandle* handle, int32_t kind, int32_t dims[3], void** device_ptr);
+
+/* Copy a LUT to / from a device buffer in the Taichi field layout
+ * (W, H[, D], 3) float32 - what the reference's field.to_numpy() holds. */
+int atm_read_lut(const AtmHandle* handle, int32_t kind, float* dst_device, void* stream);
+int atm_load_lut(AtmHandle* handle, int32_t kind, const float* src_device, void* stream);
+
+/* Radiance samples (one constant-source segment each, reference
+ * _scattering_segment :858-899) evaluated by composites since the last
+ * reset.  Synchronises `stream`. */
+int atm_read_sample_counter(AtmHandle* handle, int32_t reset, uint64_t* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ATM_CAPI_H */

@@ -1,0 +1,498 @@
+// atm_capi.cu - C ABI of libplanet_atm (declared in include/atm_capi.h).
+//
+// Host side of the reference's AtmosphereRenderer (atmosphere/renderer.py
+// :51-116, :2057-2238): the renderer state, the LUT cache keys and the
+// float rounding points of update / prepare_frame / composite live here, in
+// native code, so a non-Python host gets the same behaviour as the Python
+// layer (which is a thin ctypes wrapper over these functions).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "atm_capi.h"
+#include "atm_kernels.h"
+
+#define ATM_API extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(ATM_E_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define ATM_CUDA(call, what)                  \
+  do {                                        \
+    cudaError_t e_ = (call);                  \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+constexpr double kPi = 3.141592653589793;
+
+bool finite_nonneg3(const double* v) {
+  for (int i = 0; i < 3; ++i)
+    if (!std::isfinite(v[i]) || v[i] < 0.0) return false;
+  return true;
+}
+
+// Validation ranges of the reference AtmosphereConfig (config.py:61-128).
+int validate(const AtmParams& p) {
+  if (!finite_nonneg3(p.rayleigh_scattering_per_m) || !finite_nonneg3(p.mie_scattering_per_m) ||
+      !finite_nonneg3(p.mie_extinction_per_m) || !finite_nonneg3(p.absorption_extinction_per_m) ||
+      !finite_nonneg3(p.ground_albedo))
+    return fail(ATM_E_INVALID, "atmosphere coefficients must contain three non-negative values");
+  for (double a : p.ground_albedo)
+    if (a > 1.0) return fail(ATM_E_INVALID, "atmosphere.ground_albedo must remain in [0, 1]");
+  const double positive[] = {p.top_altitude_m, p.rayleigh_scale_height_m, p.mie_scale_height_m,
+                             p.absorption_half_width_m};
+  for (double v : positive)
+    if (!std::isfinite(v) || v <= 0.0) return fail(ATM_E_INVALID, "atmosphere lengths must be positive and finite");
+  if (!(0.0 <= p.absorption_peak_altitude_m && p.absorption_peak_altitude_m <= p.top_altitude_m))
+    return fail(ATM_E_INVALID, "atmosphere absorption peak must lie inside the shell");
+  if (!(-0.99 < p.mie_phase_g && p.mie_phase_g < 0.99))
+    return fail(ATM_E_INVALID, "atmosphere.mie_phase_g must be in (-0.99, 0.99)");
+  for (int i = 0; i < 3; ++i)
+    if (p.mie_scattering_per_m[i] > p.mie_extinction_per_m[i])
+      return fail(ATM_E_INVALID, "Mie scattering cannot exceed Mie extinction");
+  struct Range {
+    int32_t v, lo, hi;
+    const char* name;
+  } ranges[] = {
+      {p.transmittance_lut_width, 16, 2048, "transmittance_lut_width"},
+      {p.transmittance_lut_height, 16, 1024, "transmittance_lut_height"},
+      {p.sky_view_lut_width, 16, 2048, "sky_view_lut_width"},
+      {p.sky_view_lut_height, 16, 2048, "sky_view_lut_height"},
+      {p.multi_scattering_lut_width, 8, 256, "multi_scattering_lut_width"},
+      {p.multi_scattering_lut_height, 8, 256, "multi_scattering_lut_height"},
+      {p.aerial_lut_width, 4, 256, "aerial_lut_width"},
+      {p.aerial_lut_height, 4, 256, "aerial_lut_height"},
+      {p.aerial_lut_depth, 8, 256, "aerial_lut_depth"},
+      {p.transmittance_steps, 4, 256, "transmittance_steps"},
+      {p.multi_scattering_directions, 4, 128, "multi_scattering_directions"},
+      {p.multi_scattering_steps, 4, 128, "multi_scattering_steps"},
+      {p.sky_view_steps, 4, 256, "sky_view_steps"},
+      {p.aerial_steps_per_slice, 1, 16, "aerial_steps_per_slice"},
+      {p.aerial_horizon_raymarch_steps, 4, 64, "aerial_horizon_raymarch_steps"},
+      {p.aerial_terminator_substeps, 2, 16, "aerial_terminator_substeps"},
+  };
+  for (const Range& r : ranges)
+    if (r.v < r.lo || r.v > r.hi) return fail(ATM_E_INVALID, "%s must be in %d..%d", r.name, r.lo, r.hi);
+  return ATM_OK;
+}
+
+// math.radians: x * (pi / 180) in double, then the kernel argument's f32 rounding
+float radians_f32(double degrees) { return float(degrees * (kPi / 180.0)); }
+
+}  // namespace
+
+namespace atm {
+
+DevParams make_dev_params(const AtmParams& p) {
+  DevParams d{};
+  d.top = float(p.top_altitude_m);
+  for (int i = 0; i < 3; ++i) {
+    d.beta_r[i] = float(p.rayleigh_scattering_per_m[i]);
+    d.beta_ms[i] = float(p.mie_scattering_per_m[i]);
+    d.beta_me[i] = float(p.mie_extinction_per_m[i]);
+    d.beta_o[i] = float(p.absorption_extinction_per_m[i]);
+    d.albedo[i] = float(p.ground_albedo[i]);
+  }
+  d.h_r = float(p.rayleigh_scale_height_m);
+  d.h_m = float(p.mie_scale_height_m);
+  d.oz_peak = float(p.absorption_peak_altitude_m);
+  d.oz_half = float(p.absorption_half_width_m);
+  const double g = p.mie_phase_g;  // Python-constant folding in double (renderer.py:795-804)
+  d.mie_c1 = float(1.0 + g * g);
+  d.mie_c2 = float(2.0 * g);
+  d.mie_k1 = float(3.0 * (1.0 - g * g));
+  d.mie_k2 = float(8.0 * kPi * (2.0 + g * g));
+  d.ray_k = float(16.0 * kPi);
+  d.t_w = p.transmittance_lut_width;
+  d.t_h = p.transmittance_lut_height;
+  d.ms_w = p.multi_scattering_lut_width;
+  d.ms_h = p.multi_scattering_lut_height;
+  d.sv_w = p.sky_view_lut_width;
+  d.sv_h = p.sky_view_lut_height;
+  d.ap_w = p.aerial_lut_width;
+  d.ap_h = p.aerial_lut_height;
+  d.ap_d = p.aerial_lut_depth;
+  d.t_steps = p.transmittance_steps;
+  d.ms_dirs = p.multi_scattering_directions;
+  d.ms_steps = p.multi_scattering_steps;
+  d.sv_steps = p.sky_view_steps;
+  d.ap_steps = p.aerial_steps_per_slice;
+  d.limb_steps = p.aerial_horizon_raymarch_steps;
+  d.substeps = p.aerial_terminator_substeps;
+  return d;
+}
+
+}  // namespace atm
+
+struct AtmHandle {
+  AtmParams params;
+  atm::DevParams dev;
+  int32_t width = 0, height = 0;
+  float4* lut[4] = {nullptr, nullptr, nullptr, nullptr};
+  int32_t dims[4][3] = {};
+  unsigned long long* samples = nullptr;
+  // cache keys (reference renderer.py:97-107); valid flags stand for "not None"
+  bool t_valid = false;
+  double t_key = 0.0;
+  bool ms_valid = false;
+  double ms_key[5] = {};  // R, E[3], angular radius (f32-rounded)
+  bool sky_valid = false;
+  double sky_key[6] = {};  // altitude, sun cosine, E[3], angular radius
+  bool aerial_available = false;
+  AtmState state{};
+};
+
+namespace {
+
+size_t lut_texels(const AtmHandle* h, int kind) {
+  return size_t(h->dims[kind][0]) * h->dims[kind][1] * h->dims[kind][2];
+}
+
+int check_handle(const AtmHandle* h) {
+  if (h == nullptr) return fail(ATM_E_INVALID, "null AtmHandle");
+  return ATM_OK;
+}
+
+int check_image(const AtmHandle* h, const AtmImage* img) {
+  if (img == nullptr) return fail(ATM_E_INVALID, "null AtmImage");
+  if (img->width != h->width || img->height != h->height)
+    return fail(ATM_E_INVALID, "image is %dx%d but the renderer was created for %dx%d", img->width, img->height,
+                h->width, h->height);
+  if (img->channels != 3 && img->channels != 4) return fail(ATM_E_INVALID, "channels must be 3 or 4");
+  if (img->stride_x <= 0 || img->stride_y <= 0) return fail(ATM_E_INVALID, "image strides must be positive");
+  return ATM_OK;
+}
+
+atm::ImageLayout layout_of(const AtmImage* img) {
+  return {img->width, img->height, img->stride_x, img->stride_y, img->channels};
+}
+
+void to_f32(const double* in, float* out, int n) {
+  for (int i = 0; i < n; ++i) out[i] = float(in[i]);
+}
+
+int build_transmittance(AtmHandle* h, double R, cudaStream_t s) {
+  ATM_CUDA(atm::launch_transmittance(h->dev, float(R), h->lut[ATM_LUT_TRANSMITTANCE], s), "transmittance build");
+  return ATM_OK;
+}
+
+int build_multi_scattering(AtmHandle* h, double R, const double E[3], double ar, cudaStream_t s) {
+  float e[3];
+  to_f32(E, e, 3);
+  ATM_CUDA(atm::launch_multi_scattering(h->dev, float(R), e, float(ar), h->lut[ATM_LUT_TRANSMITTANCE],
+                                        h->lut[ATM_LUT_MULTI_SCATTERING], s),
+           "multi-scattering build");
+  return ATM_OK;
+}
+
+int build_sky_view(AtmHandle* h, double R, double alt, double sun_cos, const double E[3], double ar,
+                   cudaStream_t s) {
+  float e[3];
+  to_f32(E, e, 3);
+  ATM_CUDA(atm::launch_sky_view(h->dev, float(R), float(alt), float(sun_cos), e, float(ar),
+                                h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
+                                h->lut[ATM_LUT_SKY_VIEW], s),
+           "sky-view build");
+  return ATM_OK;
+}
+
+int build_aerial(AtmHandle* h, int width, int height, double R, double alt, const double sun[3], const double E[3],
+                 double ar, const double basis[9], double tanfov, cudaStream_t s) {
+  float sn[3], e[3], b[9];
+  to_f32(sun, sn, 3);
+  to_f32(E, e, 3);
+  to_f32(basis, b, 9);
+  ATM_CUDA(atm::launch_aerial(h->dev, width, height, float(R), float(alt), sn, e, float(ar), b, b + 3, b + 6,
+                              float(tanfov), h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
+                              h->lut[ATM_LUT_AERIAL], s),
+           "aerial-perspective build");
+  return ATM_OK;
+}
+
+bool finite_n(const double* v, int n) {
+  for (int i = 0; i < n; ++i)
+    if (!std::isfinite(v[i])) return false;
+  return true;
+}
+
+}  // namespace
+
+ATM_API const char* atm_last_error(void) { return g_error.c_str(); }
+
+ATM_API int atm_create(const AtmParams* params, int32_t width, int32_t height, AtmHandle** out) {
+  if (params == nullptr || out == nullptr) return fail(ATM_E_INVALID, "null argument to atm_create");
+  *out = nullptr;
+  if (width < 1 || height < 1 || width > 16384 || height > 16384)
+    return fail(ATM_E_INVALID, "frame size %dx%d outside 1..16384", width, height);
+  int rc = validate(*params);
+  if (rc != ATM_OK) return rc;
+  AtmHandle* h = new (std::nothrow) AtmHandle();
+  if (h == nullptr) return fail(ATM_E_NOMEM, "host allocation failed");
+  h->params = *params;
+  h->dev = atm::make_dev_params(*params);
+  h->width = width;
+  h->height = height;
+  const int32_t dims[4][3] = {
+      {params->transmittance_lut_width, params->transmittance_lut_height, 1},
+      {params->multi_scattering_lut_width, params->multi_scattering_lut_height, 1},
+      {params->sky_view_lut_width, params->sky_view_lut_height, 1},
+      {params->aerial_lut_width, params->aerial_lut_height, params->aerial_lut_depth},
+  };
+  std::memcpy(h->dims, dims, sizeof(dims));
+  for (int k = 0; k < 4; ++k) {
+    const size_t bytes = lut_texels(h, k) * sizeof(float4);
+    cudaError_t e = cudaMalloc(&h->lut[k], bytes);
+    if (e == cudaSuccess) e = cudaMemset(h->lut[k], 0, bytes);
+    if (e != cudaSuccess) {
+      atm_destroy(h);
+      return e == cudaErrorMemoryAllocation ? fail(ATM_E_NOMEM, "LUT allocation failed") : cuda_fail(e, "LUT init");
+    }
+  }
+  cudaError_t e = cudaMalloc(&h->samples, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(h->samples, 0, sizeof(unsigned long long));
+  if (e != cudaSuccess) {
+    atm_destroy(h);
+    return cuda_fail(e, "sample counter");
+  }
+  *out = h;
+  return ATM_OK;
+}
+
+ATM_API int atm_destroy(AtmHandle* h) {
+  if (h == nullptr) return ATM_OK;
+  for (float4*& p : h->lut) {
+    if (p) cudaFree(p);
+    p = nullptr;
+  }
+  if (h->samples) cudaFree(h->samples);
+  delete h;
+  return ATM_OK;
+}
+
+ATM_API int atm_set_luts_frozen(AtmHandle* h, int32_t frozen) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  const bool f = frozen != 0;
+  if (h->state.luts_frozen && !f) h->sky_valid = false;  // renderer.py:2068-2069
+  h->state.luts_frozen = f ? 1 : 0;
+  return ATM_OK;
+}
+
+ATM_API int atm_get_state(const AtmHandle* h, AtmState* out) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (out == nullptr) return fail(ATM_E_INVALID, "null AtmState");
+  *out = h->state;
+  return ATM_OK;
+}
+
+ATM_API int atm_update(AtmHandle* h, double planet_radius_m, double camera_radius_m, const double sun_local[3],
+                       const double solar_irradiance[3], double sun_angular_radius_degrees, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (sun_local == nullptr || solar_irradiance == nullptr) return fail(ATM_E_INVALID, "null vector argument");
+  if (!std::isfinite(planet_radius_m) || planet_radius_m <= 1.0 || !std::isfinite(camera_radius_m) ||
+      !finite_n(sun_local, 3) || !finite_n(solar_irradiance, 3) || !std::isfinite(sun_angular_radius_degrees))
+    return fail(ATM_E_INVALID, "non-finite update argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const double R = planet_radius_m;
+  double n = std::sqrt(sun_local[0] * sun_local[0] + sun_local[1] * sun_local[1] + sun_local[2] * sun_local[2]);
+  n = n > 1.0e-12 ? n : 1.0e-12;
+  const double sun_y = sun_local[1] / n;
+  const double ar = double(radians_f32(sun_angular_radius_degrees));  // renderer.py:2086-2088
+  if (!h->t_valid || h->t_key != R) {
+    if ((rc = build_transmittance(h, R, s))) return rc;
+    h->t_valid = true;
+    h->t_key = R;
+    h->ms_valid = false;
+    h->sky_valid = false;
+    h->state.transmittance_rebuilds++;
+  }
+  const double ms_key[5] = {R, solar_irradiance[0], solar_irradiance[1], solar_irradiance[2], ar};
+  if (!h->ms_valid || std::memcmp(ms_key, h->ms_key, sizeof(ms_key)) != 0) {
+    if ((rc = build_multi_scattering(h, R, solar_irradiance, ar, s))) return rc;
+    std::memcpy(h->ms_key, ms_key, sizeof(ms_key));
+    h->ms_valid = true;
+    h->sky_valid = false;
+    h->state.multi_scattering_rebuilds++;
+  }
+  // altitude kept apart from the Earth-scale radius before it meets f32 (:2112-2118)
+  const double alt_key = double(float(std::fmax(camera_radius_m - R, 0.0)));
+  const double zen_key = double(float(std::fmin(std::fmax(sun_y, -1.0), 1.0)));
+  const double sky_key[6] = {alt_key, zen_key, solar_irradiance[0], solar_irradiance[1], solar_irradiance[2], ar};
+  const bool changed = !h->sky_valid || std::memcmp(sky_key, h->sky_key, sizeof(sky_key)) != 0;
+  if (changed && (!h->state.luts_frozen || !h->sky_valid)) {
+    if ((rc = build_sky_view(h, R, alt_key, zen_key, solar_irradiance, ar, s))) return rc;
+    std::memcpy(h->sky_key, sky_key, sizeof(sky_key));
+    h->sky_valid = true;
+    h->state.has_sky_snapshot = 1;
+    h->state.sky_snapshot_altitude_m = alt_key;
+    h->state.sky_snapshot_sun_cosine = zen_key;
+    h->state.sky_view_rebuilds++;
+  }
+  return ATM_OK;
+}
+
+ATM_API int atm_prepare_frame(AtmHandle* h, const float* position_view, const int32_t* surface_id,
+                              const AtmImage* image, double planet_radius_m, double camera_radius_m,
+                              const double sun_local[3], const double solar_irradiance[3],
+                              double sun_angular_radius_degrees, const double view_basis[9],
+                              double tangent_half_fov, float* surface_sun_transmittance, float* surface_sky_radiance,
+                              void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!position_view || !surface_id || !surface_sun_transmittance || !surface_sky_radiance || !sun_local ||
+      !solar_irradiance || !view_basis)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_prepare_frame");
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const double R = planet_radius_m;
+  const double alt = std::fmax(camera_radius_m - R, 0.0);
+  const float ar = radians_f32(sun_angular_radius_degrees);
+  float sn[3], b[9];
+  to_f32(sun_local, sn, 3);
+  to_f32(view_basis, b, 9);
+  ATM_CUDA(atm::launch_prepare_surface(h->dev, layout_of(image), position_view, surface_id, float(R), float(alt), sn,
+                                       ar, b, b + 3, b + 6, h->lut[ATM_LUT_TRANSMITTANCE],
+                                       h->lut[ATM_LUT_MULTI_SCATTERING], surface_sun_transmittance,
+                                       surface_sky_radiance, s),
+           "surface lighting");
+  if (!h->state.luts_frozen || !h->aerial_available) {
+    if ((rc = build_aerial(h, h->width, h->height, R, alt, sun_local, solar_irradiance, double(ar), view_basis,
+                           tangent_half_fov, s)))
+      return rc;
+    h->state.has_aerial_snapshot = 1;
+    h->state.aerial_snapshot_altitude_m = camera_radius_m - planet_radius_m;
+    h->aerial_available = true;
+    h->state.aerial_rebuilds++;
+  }
+  return ATM_OK;
+}
+
+ATM_API int atm_composite(AtmHandle* h, const float* scene_hdr, const float* space_hdr, const int32_t* surface_id,
+                          const float* position_view, float* hdr, const AtmImage* image, double planet_radius_m,
+                          double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
+                          const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                          const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                          double star_contrast_end, int32_t diagnostic_view, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!scene_hdr || !space_hdr || !surface_id || !position_view || !hdr || !sun_local || !solar_irradiance ||
+      !sun_disk_radiance || !view_basis)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_composite");
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  const double alt = std::fmax(camera_radius_m - planet_radius_m, 0.0);
+  const double sky_alt = h->state.has_sky_snapshot ? h->state.sky_snapshot_altitude_m : alt;  // :2215-2217
+  atm::CompositeScalars A{};
+  A.bottom = float(planet_radius_m);
+  A.cam_alt = float(alt);
+  A.sky_alt = float(sky_alt);
+  A.ar = radians_f32(sun_angular_radius_degrees);
+  A.tanfov = float(tangent_half_fov);
+  A.star_start = float(star_contrast_start);
+  A.star_end = float(star_contrast_end);
+  to_f32(sun_local, A.sun, 3);
+  to_f32(solar_irradiance, A.E, 3);
+  to_f32(sun_disk_radiance, A.disk, 3);
+  to_f32(view_basis, A.right, 3);
+  to_f32(view_basis + 3, A.up, 3);
+  to_f32(view_basis + 6, A.fwd, 3);
+  A.view = diagnostic_view;
+  ATM_CUDA(atm::launch_composite(h->dev, layout_of(image), A, scene_hdr, space_hdr, surface_id, position_view,
+                                 h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
+                                 h->lut[ATM_LUT_SKY_VIEW], h->lut[ATM_LUT_AERIAL], hdr, h->samples,
+                                 static_cast<cudaStream_t>(stream)),
+           "composite");
+  return ATM_OK;
+}
+
+ATM_API int atm_build_lut(AtmHandle* h, int32_t kind, const AtmBuildArgs* a, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (a == nullptr) return fail(ATM_E_INVALID, "null AtmBuildArgs");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  switch (kind) {
+    case ATM_LUT_TRANSMITTANCE:
+      return build_transmittance(h, a->planet_radius_m, s);
+    case ATM_LUT_MULTI_SCATTERING:
+      return build_multi_scattering(h, a->planet_radius_m, a->solar_irradiance, a->sun_angular_radius_rad, s);
+    case ATM_LUT_SKY_VIEW:
+      return build_sky_view(h, a->planet_radius_m, a->camera_altitude_m, a->sun_zenith_cosine, a->solar_irradiance,
+                            a->sun_angular_radius_rad, s);
+    case ATM_LUT_AERIAL:
+      if (a->frame_width < 1 || a->frame_height < 1) return fail(ATM_E_INVALID, "aerial build needs the frame size");
+      return build_aerial(h, a->frame_width, a->frame_height, a->planet_radius_m, a->camera_altitude_m, a->sun_local,
+                          a->solar_irradiance, a->sun_angular_radius_rad, a->view_basis, a->tangent_half_fov, s);
+    default:
+      return fail(ATM_E_INVALID, "unknown LUT kind %d", kind);
+  }
+}
+
+ATM_API int atm_lut_info(const AtmHandle* h, int32_t kind, int32_t dims[3], void** device_ptr) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (kind < 0 || kind > 3) return fail(ATM_E_INVALID, "unknown LUT kind %d", kind);
+  if (dims) std::memcpy(dims, h->dims[kind], sizeof(int32_t) * 3);
+  if (device_ptr) *device_ptr = h->lut[kind];
+  return ATM_OK;
+}
+
+ATM_API int atm_read_lut(const AtmHandle* h, int32_t kind, float* dst_device, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (kind < 0 || kind > 3) return fail(ATM_E_INVALID, "unknown LUT kind %d", kind);
+  if (dst_device == nullptr) return fail(ATM_E_INVALID, "null destination");
+  ATM_CUDA(atm::launch_lut_to_fields(h->lut[kind], h->dims[kind][0], h->dims[kind][1], h->dims[kind][2], dst_device,
+                                     static_cast<cudaStream_t>(stream)),
+           "LUT read");
+  return ATM_OK;
+}
+
+ATM_API int atm_load_lut(AtmHandle* h, int32_t kind, const float* src_device, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if (kind < 0 || kind > 3) return fail(ATM_E_INVALID, "unknown LUT kind %d", kind);
+  if (src_device == nullptr) return fail(ATM_E_INVALID, "null source");
+  ATM_CUDA(atm::launch_fields_to_lut(src_device, h->dims[kind][0], h->dims[kind][1], h->dims[kind][2], h->lut[kind],
+                                     static_cast<cudaStream_t>(stream)),
+           "LUT load");
+  return ATM_OK;
+}
+
+ATM_API int atm_read_sample_counter(AtmHandle* h, int32_t reset, uint64_t* out, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned long long v = 0;
+  ATM_CUDA(cudaMemcpyAsync(&v, h->samples, sizeof(v), cudaMemcpyDeviceToHost, s), "sample counter read");
+  if (reset) ATM_CUDA(cudaMemsetAsync(h->samples, 0, sizeof(v), s), "sample counter reset");
+  ATM_CUDA(cudaStreamSynchronize(s), "sample counter sync");
+  if (out) *out = v;
+  return ATM_OK;
+}

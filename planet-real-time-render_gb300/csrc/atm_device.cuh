@@ -1,0 +1,410 @@
+// atm_device.cuh - device math of the spherical-atmosphere model (sm_103a).
+//
+// FP32 formulation of the reference's Taichi functions in
+// src/planet_renderer/atmosphere/renderer.py (line numbers below).  The
+// arithmetic follows the reference expression by expression so results agree
+// with it to float rounding; where the reference evaluates the same quantity
+// twice with identical inputs (density in extinction and source; horizon and
+// sun zenith in disk visibility and representative zenith; a base
+// interval's upper boundary and the next one's lower boundary; the
+// terminator weight's midpoint visibility and the coarse sample's) it is
+// evaluated once here - same inputs, same operations, same value.
+//
+// LUT storage: float4 texels (rgb + pad), row-major, index y * width + x;
+// the aerial volume is [z][y][x].  Reads go through the read-only path.
+#pragma once
+
+#include <cstdint>
+
+namespace atm {
+
+constexpr float kPiF = 3.14159265358979323846f;  // f32(math.pi), renderer.py:12
+constexpr float kLargeF = 1.0e30f;               // _LARGE_DISTANCE, :13
+
+// Parameters rounded to float exactly where the Taichi trace rounds them
+// (Python constants fold in double, then meet f32 values).
+struct DevParams {
+  float top;                   // top_altitude_m
+  float beta_r[3];             // Rayleigh scattering
+  float beta_ms[3];            // Mie scattering
+  float beta_me[3];            // Mie extinction
+  float beta_o[3];             // ozone absorption
+  float albedo[3];             // ground albedo
+  float h_r, h_m;              // scale heights
+  float oz_peak, oz_half;      // ozone tent
+  float mie_c1, mie_c2;        // f32(1+g^2), f32(2g)
+  float mie_k1, mie_k2;        // f32(3(1-g^2)), f32(8 pi (2+g^2))
+  float ray_k;                 // f32(16 pi)
+  int t_w, t_h, ms_w, ms_h, sv_w, sv_h, ap_w, ap_h, ap_d;
+  int t_steps, ms_dirs, ms_steps, sv_steps, ap_steps, limb_steps, substeps;
+};
+
+struct f3 {
+  float x, y, z;
+};
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ f3 splat(float s) { return {s, s, s}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a, f3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, float s) { return {a.x * s, a.y * s, a.z * s}; }
+__device__ __forceinline__ f3 operator/(f3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+__device__ __forceinline__ f3 operator/(f3 a, f3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+__device__ __forceinline__ float dot(f3 a, f3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ float norm(f3 a) { return sqrtf(dot(a, a)); }
+__device__ __forceinline__ float mx(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float mn(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ float clampf(float x, float lo, float hi) { return mn(mx(x, lo), hi); }
+__device__ __forceinline__ f3 vmax(f3 a, float s) { return {mx(a.x, s), mx(a.y, s), mx(a.z, s)}; }
+__device__ __forceinline__ f3 vmin(f3 a, float s) { return {mn(a.x, s), mn(a.y, s), mn(a.z, s)}; }
+__device__ __forceinline__ f3 vclamp(f3 a, float lo, float hi) { return vmin(vmax(a, lo), hi); }
+__device__ __forceinline__ f3 vexp(f3 a) { return {expf(a.x), expf(a.y), expf(a.z)}; }
+__device__ __forceinline__ f3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ f3 from4(float4 v) { return {v.x, v.y, v.z}; }
+__device__ __forceinline__ float4 to4(f3 v) { return make_float4(v.x, v.y, v.z, 0.0f); }
+__device__ __forceinline__ f3 arr3(const float (&a)[3]) { return {a[0], a[1], a[2]}; }
+
+// Composition of two consecutive ray segments: (L1,T1) then (L2,T2).
+struct Seg {
+  f3 L, T;
+};
+__device__ __forceinline__ Seg seg_then(Seg a, Seg b) { return {a.L + a.T * b.L, a.T * b.T}; }
+
+// ---- density and coefficients (:168-209) ----------------------------------
+struct Density {
+  float r, m, o;
+};
+__device__ __forceinline__ Density density(const DevParams& P, float h) {
+  Density d{0.0f, 0.0f, 0.0f};
+  if (0.0f <= h && h <= P.top) {
+    d.r = expf(-h / P.h_r);
+    d.m = expf(-h / P.h_m);
+    d.o = mx(1.0f - fabsf(h - P.oz_peak) / P.oz_half, 0.0f);
+  }
+  return d;
+}
+__device__ __forceinline__ f3 extinction_of(const DevParams& P, Density d) {
+  return (arr3(P.beta_r) * d.r + arr3(P.beta_me) * d.m) + arr3(P.beta_o) * d.o;
+}
+__device__ __forceinline__ f3 scattering_of(const DevParams& P, Density d) {
+  return arr3(P.beta_r) * d.r + arr3(P.beta_ms) * d.m;
+}
+
+// ---- shells and intervals (:211-408) ---------------------------------------
+__device__ __forceinline__ void sphere_roots(f3 o, f3 d, float radius, float& nearv, float& farv, bool& hit) {
+  float projected = dot(o, d);
+  float perpendicular = norm(o - d * projected);
+  float clearance = radius - perpendicular;
+  hit = clearance >= 0.0f;
+  nearv = kLargeF;
+  farv = -kLargeF;
+  if (hit) {
+    float root = sqrtf(mx(mx(clearance, 0.0f) * (radius + perpendicular), 0.0f));
+    nearv = -projected - root;
+    farv = -projected + root;
+  }
+}
+__device__ __forceinline__ float shell_rho(float h, float bottom) {
+  float a = mx(h, 0.0f);
+  return sqrtf(a * (2.0f * bottom + a));
+}
+__device__ __forceinline__ float altitude_on_ray(float h0, float cosv, float t, float bottom) {
+  float a = mx(h0, 0.0f);
+  float orad = bottom + a;
+  float delta = (a * (2.0f * bottom + a) + 2.0f * orad * cosv * t) + t * t;
+  float len = sqrtf(mx(bottom * bottom + delta, 0.0f));
+  return delta / mx(len + bottom, 1.0f);
+}
+__device__ __forceinline__ void shell_roots(float h0, float cosv, float shell, float bottom, float& nearv,
+                                            float& farv, bool& hit) {
+  float orad = bottom + h0;
+  float hl = orad * cosv;
+  float c = (h0 - shell) * ((2.0f * bottom + h0) + shell);
+  float disc = hl * hl - c;
+  hit = disc >= 0.0f;
+  nearv = kLargeF;
+  farv = -kLargeF;
+  if (hit) {
+    float root = sqrtf(mx(disc, 0.0f));
+    float sign = hl < 0.0f ? -1.0f : 1.0f;
+    float q = -hl - sign * root;
+    float r0 = -hl - root;
+    float r1 = -hl + root;
+    if (fabsf(q) > 1.0e-12f) {
+      r0 = q;
+      r1 = c / q;
+    }
+    nearv = mn(r0, r1);
+    farv = mx(r0, r1);
+  }
+}
+__device__ __forceinline__ void segment_from_altitude(const DevParams& P, float h, float cosv, float bottom,
+                                                      float& start, float& end, bool& valid, bool& ground) {
+  float on, of;
+  bool oh;
+  shell_roots(h, cosv, P.top, bottom, on, of, oh);
+  start = mx(on, 0.0f);
+  end = of;
+  valid = oh && end > start;
+  ground = false;
+  float gn, gf;
+  bool gh;
+  shell_roots(h, cosv, 0.0f, bottom, gn, gf, gh);
+  if (valid && gh) {
+    float gd = kLargeF;
+    if (gn > start + 1.0e-3f)
+      gd = gn;
+    else if (gf > start + 1.0e-3f)
+      gd = gf;
+    if (gd < end) {
+      end = gd;
+      ground = true;
+    }
+  }
+}
+__device__ __forceinline__ void segment_vec(const DevParams& P, f3 o, f3 d, float bottom, float& start, float& end,
+                                            bool& valid, bool& ground) {
+  float on, of;
+  bool oh;
+  sphere_roots(o, d, bottom + P.top, on, of, oh);
+  start = mx(on, 0.0f);
+  end = of;
+  valid = oh && end > start;
+  ground = false;
+  float gn, gf;
+  bool gh;
+  sphere_roots(o, d, bottom, gn, gf, gh);
+  if (valid && gh) {
+    float gd = kLargeF;
+    float eps = mx(0.001f, bottom * 1.0e-8f);
+    if (gn > start + eps)
+      gd = gn;
+    else if (gf > start + eps)
+      gd = gf;
+    if (gd < end) {
+      end = gd;
+      ground = true;
+    }
+  }
+}
+__device__ __forceinline__ void aerial_prefix(const DevParams& P, float h, float cosv, float bottom, float& start,
+                                              float& end, bool& valid) {
+  bool v, g;
+  segment_from_altitude(P, h, cosv, bottom, start, end, v, g);
+  if (v && !g) {
+    float closest = -(bottom + h) * cosv;
+    if (closest > start && closest < end) end = closest;
+  }
+  valid = v && end > start;
+}
+__device__ __forceinline__ float distance_to_top(const DevParams& P, float h, float cosv, float bottom) {
+  float radius = bottom + mx(h, 0.0f);
+  float delta = (P.top - h) * ((2.0f * bottom + P.top) + h);
+  float disc = radius * radius * cosv * cosv + delta;
+  return mx(-radius * cosv + sqrtf(mx(disc, 0.0f)), 0.0f);
+}
+
+// ---- LUT parameterisations (:410-568) ---------------------------------------
+__device__ __forceinline__ void t_uv_to_ray(const DevParams& P, float u, float v, float bottom, float& h,
+                                            float& cosv, float& dist) {
+  float sh = shell_rho(P.top, bottom);
+  float rho = sh * clampf(v, 0.0f, 1.0f);
+  float rl = sqrtf(rho * rho + bottom * bottom);
+  h = rho * rho / mx(rl + bottom, 1.0f);
+  float radius = bottom + h;
+  float dmin = P.top - h;
+  float dmax = rho + sh;
+  dist = dmin + clampf(u, 0.0f, 1.0f) * (dmax - dmin);
+  float c = 1.0f;
+  if (dist > 1.0e-6f) c = ((P.top - h) * ((2.0f * bottom + P.top) + h) - dist * dist) / (2.0f * radius * dist);
+  cosv = clampf(c, -1.0f, 1.0f);
+}
+__device__ __forceinline__ void t_ray_to_uv(const DevParams& P, float h, float cosv, float bottom, float sh,
+                                            float& u, float& v) {
+  h = clampf(h, 0.0f, P.top);
+  float rho = shell_rho(h, bottom);
+  float d = distance_to_top(P, h, cosv, bottom);
+  float dmin = P.top - h;
+  float dmax = rho + sh;
+  u = clampf((d - dmin) / mx(dmax - dmin, 1.0e-6f), 0.0f, 1.0f);
+  v = clampf(rho / mx(sh, 1.0e-6f), 0.0f, 1.0f);
+}
+__device__ __forceinline__ float warp_boundary(float closest_raw, float start, float end, float f) {
+  float closest = clampf(closest_raw, start, end);
+  float eps = mx((end - start) * 1.0e-6f, 1.0e-5f);
+  if (closest <= start + eps) return start + (end - start) * f * f;
+  if (closest >= end - eps) {
+    float inv = 1.0f - f;
+    return end - (end - start) * inv * inv;
+  }
+  if (f < 0.5f) {
+    float inv = 1.0f - f * 2.0f;
+    return closest - (closest - start) * inv * inv;
+  }
+  float local = f * 2.0f - 1.0f;
+  return closest + (end - closest) * local * local;
+}
+__device__ __forceinline__ float horizon_cosine(float h, float bottom) {
+  float radius = bottom + mx(h, 0.0f);
+  return -shell_rho(h, bottom) / mx(radius, 1.0f);
+}
+__device__ __forceinline__ float sky_horizon_zenith(float h, float bottom) {
+  float a = mx(h, 0.0f);
+  float radius = bottom + a;
+  float tc = shell_rho(a, bottom) / mx(radius, 1.0f);
+  return kPiF - acosf(clampf(tc, 0.0f, 1.0f));
+}
+__device__ __forceinline__ float sky_v_to_zenith(float v, float hz) {
+  if (v < 0.5f) {
+    float inv = 1.0f - 2.0f * v;
+    return hz * (1.0f - inv * inv);
+  }
+  float local = 2.0f * v - 1.0f;
+  return hz + (kPiF - hz) * local * local;
+}
+__device__ __forceinline__ float sky_zenith_to_v(float z, float hz) {
+  if (z < hz) {
+    float n = clampf(z / mx(hz, 1.0e-6f), 0.0f, 1.0f);
+    return 0.5f * (1.0f - sqrtf(mx(1.0f - n, 0.0f)));
+  }
+  float n = clampf((z - hz) / mx(kPiF - hz, 1.0e-6f), 0.0f, 1.0f);
+  return 0.5f + 0.5f * sqrtf(n);
+}
+__device__ __forceinline__ float sun_u_to_cosine(float u, float h, float bottom) {
+  float hc = horizon_cosine(h, bottom);
+  float c;
+  if (u < 0.5f) {
+    float inv = 1.0f - 2.0f * u;
+    c = hc - (hc + 1.0f) * inv * inv;
+  } else {
+    float local = 2.0f * u - 1.0f;
+    c = hc + (1.0f - hc) * local * local;
+  }
+  return clampf(c, -1.0f, 1.0f);
+}
+__device__ __forceinline__ float sun_cosine_to_u(float c, float hc) {
+  if (c < hc) {
+    float n = clampf((hc - c) / mx(hc + 1.0f, 1.0e-6f), 0.0f, 1.0f);
+    return 0.5f * (1.0f - sqrtf(n));
+  }
+  float n = clampf((c - hc) / mx(1.0f - hc, 1.0e-6f), 0.0f, 1.0f);
+  return 0.5f + 0.5f * sqrtf(n);
+}
+
+// ---- LUT sampling -----------------------------------------------------------
+// Bilinear tap with the reference's half-texel rule and edge clamp
+// (:618-640, :655-683, :1503-1525).
+__device__ __forceinline__ f3 bilinear(const float4* __restrict__ lut, int w, int h, float u, float v) {
+  float x = clampf(u * float(w) - 0.5f, 0.0f, float(w - 1));
+  float y = clampf(v * float(h) - 0.5f, 0.0f, float(h - 1));
+  int x0 = int(floorf(x));
+  int y0 = int(floorf(y));
+  int x1 = min(x0 + 1, w - 1);
+  int y1 = min(y0 + 1, h - 1);
+  float fx = x - float(x0);
+  float fy = y - float(y0);
+  f3 a = from4(__ldg(lut + y0 * w + x0));
+  f3 b = from4(__ldg(lut + y0 * w + x1));
+  f3 c = from4(__ldg(lut + y1 * w + x0));
+  f3 d = from4(__ldg(lut + y1 * w + x1));
+  f3 lo = a * (1.0f - fx) + b * fx;
+  f3 hi = c * (1.0f - fx) + d * fx;
+  return lo * (1.0f - fy) + hi * fy;
+}
+
+// Per-launch geometry shared by every sample of a kernel.
+struct Frame {
+  const float4* __restrict__ tlut;
+  const float4* __restrict__ mslut;
+  float bottom;     // planet radius (f32)
+  float shell_top;  // shell_rho(top, bottom)
+  float ar;         // sun angular radius (rad)
+  f3 sun;
+  f3 E;             // solar irradiance
+};
+
+// _sample_transmittance_unoccluded :609-640
+__device__ __forceinline__ f3 sample_t(const DevParams& P, const Frame& F, float h, float cosv) {
+  float u, v;
+  t_ray_to_uv(P, mx(h, 0.0f), cosv, F.bottom, F.shell_top, u, v);
+  return bilinear(F.tlut, P.t_w, P.t_h, u, v);
+}
+// _sample_multi_scattering :642-683
+__device__ __forceinline__ f3 sample_ms(const DevParams& P, const Frame& F, float h, float sc, float hc) {
+  float af = clampf(h / P.top, 0.0f, 1.0f);
+  float u = sun_cosine_to_u(sc, hc);
+  float v = sqrtf(af);
+  return bilinear(F.mslut, P.ms_w, P.ms_h, u, v);
+}
+
+// Horizon quantities at one sample altitude.
+struct Horizon {
+  float hc;  // horizon cosine
+  float hz;  // horizon zenith
+};
+__device__ __forceinline__ Horizon horizon_at(float h, float bottom) {
+  Horizon H;
+  H.hc = horizon_cosine(h, bottom);
+  H.hz = acosf(clampf(H.hc, -1.0f, 1.0f));
+  return H;
+}
+// _solar_disk_visibility :728-754, given horizon and sun zenith
+__device__ __forceinline__ float disk_visibility(float hz, float sz, float ar) {
+  float n = clampf((hz - sz) / mx(ar, 1.0e-6f), -1.0f, 1.0f);
+  return (acosf(-n) + n * sqrtf(mx(1.0f - n * n, 0.0f))) / kPiF;
+}
+// _sample_solar_transmittance :756-789 (returns visibility too)
+__device__ __forceinline__ f3 sample_solar_t(const DevParams& P, const Frame& F, float h, float sc, Horizon H,
+                                             float& vis) {
+  float sz = acosf(clampf(sc, -1.0f, 1.0f));
+  vis = disk_visibility(H.hz, sz, F.ar);
+  float rz = mn(sz, H.hz - F.ar * 0.25f);
+  float rc = cosf(mx(rz, 0.0f));
+  return sample_t(P, F, h, rc) * vis;
+}
+// _rayleigh_phase / _mie_phase :791-804
+__device__ __forceinline__ float rayleigh_phase(const DevParams& P, float c) {
+  return 3.0f * (1.0f + c * c) / P.ray_k;
+}
+__device__ __forceinline__ float mie_phase(const DevParams& P, float c) {
+  float den = mx(P.mie_c1 - P.mie_c2 * c, 1.0e-8f);
+  return P.mie_k1 * (1.0f + c * c) / (P.mie_k2 * (den * sqrtf(den)));
+}
+// _segment_integral :806-816
+__device__ __forceinline__ void segment_integral(f3 ext, float step, f3& tr, f3& integ) {
+  tr = vexp(-vmin(ext * step, 80.0f));
+  integ.x = ext.x > 1.0e-12f ? (1.0f - tr.x) / ext.x : step;
+  integ.y = ext.y > 1.0e-12f ? (1.0f - tr.y) / ext.y : step;
+  integ.z = ext.z > 1.0e-12f ? (1.0f - tr.z) / ext.z : step;
+}
+
+// One constant-source sample at `dist` along `ray` from the local-axis origin
+// (0, bottom + h0, 0): _scattering_segment :858-899 with
+// _scattering_source :818-856.  `ray_cos_sun` = clamp(ray . sun).
+// Returns the segment (L, T) and the disk visibility at the sample.
+template <bool kMultiple>
+__device__ __forceinline__ Seg source_segment(const DevParams& P, const Frame& F, float o_y, float h0, f3 ray,
+                                              float ray_y, float start, float end, float phase_r, float phase_m,
+                                              float& vis) {
+  float step = mx(end - start, 0.0f);
+  float dist = (start + end) * 0.5f;
+  f3 point = mk(ray.x * dist, o_y + ray.y * dist, ray.z * dist);
+  float h = altitude_on_ray(h0, ray_y, dist, F.bottom);
+  Density d = density(P, h);
+  f3 ext = extinction_of(P, d);
+  Seg s;
+  f3 integ;
+  segment_integral(ext, step, s.T, integ);
+  float radius = norm(point);
+  f3 radial = point / mx(radius, 1.0f);
+  float sc = dot(radial, F.sun);
+  Horizon H = horizon_at(h, F.bottom);
+  f3 st = sample_solar_t(P, F, h, sc, H, vis);
+  f3 src = (F.E * st) * (arr3(P.beta_r) * d.r * phase_r + arr3(P.beta_ms) * d.m * phase_m);
+  if (kMultiple) src = src + scattering_of(P, d) * sample_ms(P, F, h, sc, H.hc);
+  s.L = src * integ;
+  return s;
+}
+
+}  // namespace atm

@@ -1,0 +1,50 @@
+// atm_kernels.h - host-side launch wrappers of the atmosphere kernels.
+// Internal to libplanet_atm; the public interface is include/atm_capi.h.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "atm_capi.h"
+#include "atm_device.cuh"
+
+namespace atm {
+
+DevParams make_dev_params(const AtmParams& p);
+
+// Per-pixel image addressing: element (x, y) at base + (x*sx + y*sy)*channels.
+struct ImageLayout {
+  int32_t width, height;
+  int64_t sx, sy;
+  int32_t channels;
+};
+
+struct CompositeScalars {
+  float bottom, cam_alt, sky_alt, ar, tanfov, star_start, star_end;
+  float sun[3], E[3], disk[3], right[3], up[3], fwd[3];
+  int32_t view;
+};
+
+cudaError_t launch_transmittance(const DevParams& P, float bottom, float4* out, cudaStream_t s);
+cudaError_t launch_multi_scattering(const DevParams& P, float bottom, const float E[3], float ar,
+                                    const float4* tlut, float4* out, cudaStream_t s);
+cudaError_t launch_sky_view(const DevParams& P, float bottom, float cam_alt, float sun_cos, const float E[3],
+                            float ar, const float4* tlut, const float4* mslut, float4* out, cudaStream_t s);
+cudaError_t launch_aerial(const DevParams& P, int width, int height, float bottom, float cam_alt, const float sun[3],
+                          const float E[3], float ar, const float right[3], const float up[3], const float fwd[3],
+                          float tanfov, const float4* tlut, const float4* mslut, float4* out, cudaStream_t s);
+cudaError_t launch_prepare_surface(const DevParams& P, const ImageLayout& L, const float* pos, const int32_t* sid,
+                                   float bottom, float cam_alt, const float sun[3], float ar, const float right[3],
+                                   const float up[3], const float fwd[3], const float4* tlut, const float4* mslut,
+                                   float* out_sun_t, float* out_sky, cudaStream_t s);
+cudaError_t launch_composite(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                             const float* scene, const float* space, const int32_t* sid, const float* pos,
+                             const float4* tlut, const float4* mslut, const float4* svlut, const float4* aplut,
+                             float* hdr, unsigned long long* sample_counter, cudaStream_t s);
+// LUT (float4 [z][y][x]) -> Taichi field layout (W, H[, D], 3) floats.
+cudaError_t launch_lut_to_fields(const float4* lut, int w, int h, int d, float* dst, cudaStream_t s);
+// Taichi field layout (W, H[, D], 3) floats -> LUT (float4 [z][y][x]).
+cudaError_t launch_fields_to_lut(const float* src, int w, int h, int d, float4* lut, cudaStream_t s);
+
+}  // namespace atm

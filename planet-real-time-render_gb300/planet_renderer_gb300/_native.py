@@ -1,0 +1,194 @@
+"""ctypes binding of libplanet_atm (the C ABI declared in include/atm_capi.h).
+
+The library is built in-tree by ``build_native.py`` (``__graft_entry__.build()``
+runs it).  There is no CPU fallback: if the library is missing or cannot be
+loaded, :func:`library` raises ``RuntimeError``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+LIBRARY_PATH = Path(__file__).resolve().parent / "lib" / "libplanet_atm.so"
+
+ATM_OK = 0
+ATM_E_INVALID = -1
+ATM_E_CUDA = -2
+ATM_E_NOMEM = -3
+ATM_E_STATE = -4
+ATM_E_TIMEOUT = -5
+
+LUT_TRANSMITTANCE = 0
+LUT_MULTI_SCATTERING = 1
+LUT_SKY_VIEW = 2
+LUT_AERIAL = 3
+
+c_double3 = ctypes.c_double * 3
+c_double9 = ctypes.c_double * 9
+
+
+class AtmParams(ctypes.Structure):
+    _fields_ = [
+        ("top_altitude_m", ctypes.c_double),
+        ("rayleigh_scattering_per_m", c_double3),
+        ("rayleigh_scale_height_m", ctypes.c_double),
+        ("mie_scattering_per_m", c_double3),
+        ("mie_extinction_per_m", c_double3),
+        ("mie_scale_height_m", ctypes.c_double),
+        ("mie_phase_g", ctypes.c_double),
+        ("absorption_extinction_per_m", c_double3),
+        ("absorption_peak_altitude_m", ctypes.c_double),
+        ("absorption_half_width_m", ctypes.c_double),
+        ("ground_albedo", c_double3),
+        ("transmittance_lut_width", ctypes.c_int32),
+        ("transmittance_lut_height", ctypes.c_int32),
+        ("multi_scattering_lut_width", ctypes.c_int32),
+        ("multi_scattering_lut_height", ctypes.c_int32),
+        ("sky_view_lut_width", ctypes.c_int32),
+        ("sky_view_lut_height", ctypes.c_int32),
+        ("aerial_lut_width", ctypes.c_int32),
+        ("aerial_lut_height", ctypes.c_int32),
+        ("aerial_lut_depth", ctypes.c_int32),
+        ("transmittance_steps", ctypes.c_int32),
+        ("multi_scattering_directions", ctypes.c_int32),
+        ("multi_scattering_steps", ctypes.c_int32),
+        ("sky_view_steps", ctypes.c_int32),
+        ("aerial_steps_per_slice", ctypes.c_int32),
+        ("aerial_horizon_raymarch_steps", ctypes.c_int32),
+        ("aerial_terminator_substeps", ctypes.c_int32),
+    ]
+
+    @classmethod
+    def from_config(cls, config) -> "AtmParams":
+        p = cls()
+        for name, ctype in cls._fields_:
+            value = getattr(config, name)
+            if isinstance(value, (tuple, list)):
+                getattr(p, name)[:] = [float(v) for v in value]
+            elif ctype is ctypes.c_int32:
+                setattr(p, name, int(value))
+            else:
+                setattr(p, name, float(value))
+        return p
+
+
+class AtmImage(ctypes.Structure):
+    _fields_ = [
+        ("width", ctypes.c_int32),
+        ("height", ctypes.c_int32),
+        ("stride_x", ctypes.c_int64),
+        ("stride_y", ctypes.c_int64),
+        ("channels", ctypes.c_int32),
+    ]
+
+
+class AtmState(ctypes.Structure):
+    _fields_ = [
+        ("luts_frozen", ctypes.c_int32),
+        ("has_sky_snapshot", ctypes.c_int32),
+        ("sky_snapshot_altitude_m", ctypes.c_double),
+        ("sky_snapshot_sun_cosine", ctypes.c_double),
+        ("has_aerial_snapshot", ctypes.c_int32),
+        ("aerial_snapshot_altitude_m", ctypes.c_double),
+        ("transmittance_rebuilds", ctypes.c_int64),
+        ("multi_scattering_rebuilds", ctypes.c_int64),
+        ("sky_view_rebuilds", ctypes.c_int64),
+        ("aerial_rebuilds", ctypes.c_int64),
+    ]
+
+
+class AtmBuildArgs(ctypes.Structure):
+    _fields_ = [
+        ("planet_radius_m", ctypes.c_double),
+        ("camera_altitude_m", ctypes.c_double),
+        ("sun_zenith_cosine", ctypes.c_double),
+        ("sun_local", c_double3),
+        ("solar_irradiance", c_double3),
+        ("sun_angular_radius_rad", ctypes.c_double),
+        ("view_basis", c_double9),
+        ("tangent_half_fov", ctypes.c_double),
+        ("frame_width", ctypes.c_int32),
+        ("frame_height", ctypes.c_int32),
+    ]
+
+
+_P = ctypes.c_void_p
+_I32 = ctypes.c_int32
+_D = ctypes.c_double
+
+# name -> (restype, argtypes); the exported entry points of atm_capi.h
+SIGNATURES = {
+    "atm_last_error": (ctypes.c_char_p, []),
+    "atm_create": (ctypes.c_int, [ctypes.POINTER(AtmParams), _I32, _I32, ctypes.POINTER(_P)]),
+    "atm_destroy": (ctypes.c_int, [_P]),
+    "atm_set_luts_frozen": (ctypes.c_int, [_P, _I32]),
+    "atm_get_state": (ctypes.c_int, [_P, ctypes.POINTER(AtmState)]),
+    "atm_update": (ctypes.c_int, [_P, _D, _D, c_double3, c_double3, _D, _P]),
+    "atm_prepare_frame": (
+        ctypes.c_int,
+        [_P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, _D, c_double9, _D, _P, _P, _P],
+    ),
+    "atm_composite": (
+        ctypes.c_int,
+        [_P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, c_double3, _D, c_double9,
+         _D, _D, _D, _I32, _P],
+    ),
+    "atm_build_lut": (ctypes.c_int, [_P, _I32, ctypes.POINTER(AtmBuildArgs), _P]),
+    "atm_lut_info": (ctypes.c_int, [_P, _I32, ctypes.POINTER(_I32), ctypes.POINTER(_P)]),
+    "atm_read_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
+    "atm_load_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
+    "atm_read_sample_counter": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
+}
+
+_LIB: ctypes.CDLL | None = None
+
+
+def library() -> ctypes.CDLL:
+    """Load libplanet_atm.so (raises RuntimeError if it is not built)."""
+
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = Path(os.environ.get("PLANET_ATM_LIBRARY", LIBRARY_PATH))
+    if not path.exists():
+        raise RuntimeError(
+            f"libplanet_atm.so not found at {path}; build it with "
+            "`python planet-real-time-render_gb300/build_native.py` (needs nvcc)"
+        )
+    lib = ctypes.CDLL(str(path))
+    for name, (restype, argtypes) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = restype
+        fn.argtypes = argtypes
+    _LIB = lib
+    return lib
+
+
+class AtmError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{message} (code {code})")
+        self.code = code
+
+
+def check(rc: int) -> None:
+    """Raise on a non-zero return code: ValueError for invalid arguments."""
+
+    if rc == ATM_OK:
+        return
+    message = (library().atm_last_error() or b"").decode(errors="replace")
+    if rc == ATM_E_INVALID:
+        raise ValueError(message)
+    raise AtmError(rc, message)
+
+
+def d3(values) -> ctypes.Array:
+    return c_double3(*[float(v) for v in values])
+
+
+def d9(basis) -> ctypes.Array:
+    flat = [float(v) for vec in basis for v in vec]
+    if len(flat) != 9:
+        raise ValueError("view_basis must be three 3-vectors (right, up, forward)")
+    return c_double9(*flat)

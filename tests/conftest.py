@@ -1,0 +1,87 @@
+"""Shared test setup.
+
+* ``gpu`` marks tests that need a CUDA device (run with ``-m gpu``).
+* Paths: the repo root (for the ``oracle`` test infrastructure) and the
+  source root ``planet-real-time-render_gb300`` (for ``planet_renderer_gb300``).
+* :func:`assert_parity` is the parity criterion used against the oracle and
+  the golden vectors of the reference.
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+GOLDEN = ROOT / "tests" / "golden"
+for p in (ROOT, ROOT / "planet-real-time-render_gb300"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+# Parity criterion, per RGB channel of an output array:
+#   |got - ref| <= RTOL * |ref| + ATOL_FRAC * max|ref[..., c]|
+# RTOL is the 1e-3 relative tolerance of the target.  ATOL_FRAC bounds
+# differences at values far below the channel's peak, where two float32
+# evaluations of the reference's own algorithm already disagree: running the
+# reference kernels and the oracle restatement (identical in float64 to
+# 3e-11) both in float32 gives differences up to 1.5e-8 absolute on a 1.7e-3
+# peak in the aerial volume of an orbital camera (1e-5 of the peak) and
+# night-side multi-scattering texels at 1e-9 of the peak.
+RTOL = 1.0e-3
+ATOL_FRAC = 1.0e-5
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (the sm_103a kernels)")
+
+
+def parity_report(got, ref, rtol=RTOL, atol_frac=ATOL_FRAC) -> dict:
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    assert got.shape == ref.shape, (got.shape, ref.shape)
+    g = got.reshape(-1, got.shape[-1])
+    r = ref.reshape(-1, ref.shape[-1])
+    peak = np.abs(r).max(axis=0)
+    diff = np.abs(g - r)
+    allowed = rtol * np.abs(r) + atol_frac * peak
+    with np.errstate(divide="ignore", invalid="ignore"):
+        pure_rel = np.where(np.abs(r) > 0, diff / np.abs(r), np.where(diff > 0, np.inf, 0.0))
+    return {
+        "max_excess": float(np.max(diff / np.maximum(allowed, 1e-300))) if diff.size else 0.0,
+        "max_rel_floor": float(np.max(diff / np.maximum(np.abs(r), 1e-4 * np.maximum(peak, 1e-300)))),
+        "frac_pure_rel_ok": float(np.mean(pure_rel <= rtol)),
+        "finite": bool(np.isfinite(g).all()),
+    }
+
+
+def assert_parity(got, ref, what: str = "", rtol=RTOL, atol_frac=ATOL_FRAC) -> dict:
+    rep = parity_report(got, ref, rtol, atol_frac)
+    assert rep["finite"], f"{what}: non-finite values"
+    assert rep["max_excess"] <= 1.0, f"{what}: parity {rep}"
+    return rep
+
+
+def load_golden(name: str):
+    path = GOLDEN / f"{name}.npz"
+    if not path.exists():
+        pytest.skip(f"golden fixture {name} not generated")
+    data = np.load(path)
+    return data, json.loads(str(data["meta"]))
+
+
+@pytest.fixture(scope="session")
+def oracle_f32():
+    from oracle.atm import Oracle
+
+    return Oracle("f32")
+
+
+@pytest.fixture(scope="session")
+def oracle_f64():
+    from oracle.atm import Oracle
+
+    return Oracle("f64")

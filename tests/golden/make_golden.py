@@ -1,0 +1,275 @@
+"""Generate golden vectors by running the reference's own atmosphere code.
+
+    python tests/golden/make_golden.py [--reference PATH] [--only NAME ...]
+
+Imports ``planet_renderer.atmosphere`` from the reference checkout with the
+float32 Taichi stand-in of ``taichi_f32_shim.py`` installed as ``taichi``, and
+drives the reference's public host methods ``AtmosphereRenderer.update``,
+``prepare_frame`` and ``composite`` (``atmosphere/renderer.py:2072-2238``),
+which launch its kernels unchanged.  Inputs (parameters, G-buffer, camera,
+sun) and outputs (every LUT, the surface-lighting fields and ``hdr`` for each
+diagnostic view) are written to ``tests/golden/<name>.npz``.
+
+``--precision f64`` runs the same reference source with every f32 replaced
+by float64; the oracle's FP64 instance must then agree to rounding level,
+which shows the restatement is the reference's algorithm (the f32 fixtures
+then bound the rounding noise between two f32 evaluations of it).
+
+Scenarios:
+  tiny_earth, tiny_small_planet, tiny_orbit
+      the LUT sizes of the reference's own integrated CPU test
+      (tests/test_m2_terrain.py:215-230), full 24x16 frames, all 11 views;
+  earth_config1
+      the Earth workload at full LUT sizes (T 256x64/40 steps, MS 32x32 with
+      64 directions x 20 steps, SV 192x108/30 steps, AP 32^3, 48 limb
+      intervals): full LUTs, and a 1920x1080 frame sampled at selected pixels;
+  earth_cameras
+      the same LUTs re-keyed for cameras at 50 km and 2000 km with low suns
+      (twilight / terminator), composite sampled at selected pixels.
+
+The script reads the reference only when it runs; the tests read the .npz.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ROOT = HERE.parents[1]
+sys.path.insert(0, str(HERE))
+sys.path.insert(0, str(ROOT / "planet-real-time-render_gb300"))
+
+import taichi_f32_shim as shim  # noqa: E402
+
+TINY_LUTS = dict(
+    transmittance_lut_width=16,
+    transmittance_lut_height=16,
+    multi_scattering_lut_width=8,
+    multi_scattering_lut_height=8,
+    sky_view_lut_width=16,
+    sky_view_lut_height=16,
+    aerial_lut_width=4,
+    aerial_lut_height=4,
+    aerial_lut_depth=8,
+    transmittance_steps=4,
+    multi_scattering_directions=4,
+    multi_scattering_steps=4,
+    sky_view_steps=4,
+    aerial_steps_per_slice=1,
+)
+
+
+def _import_reference(reference: Path):
+    shim.install()
+    sys.path.insert(0, str(reference / "src"))
+    from planet_renderer.atmosphere import (  # type: ignore
+        AtmosphereConfig,
+        AtmosphereDiagnosticView,
+        AtmosphereRenderer,
+    )
+
+    return AtmosphereConfig, AtmosphereDiagnosticView, AtmosphereRenderer
+
+
+def _fill_field(field, array):
+    field.from_numpy(np.asarray(array, dtype=field.data.dtype))
+
+
+def run_scenario(name, reference, config_kwargs, planet_radius, camera_altitude, sun_zenith_deg, sun_azimuth_deg,
+                 yaw_deg, pitch_deg, width, height, sample_pixels=None, seed=2027, reuse=None,
+                 views=None, solar_irradiance=(4.0, 3.9, 3.7), sun_angular_radius_degrees=0.266):
+    """Run one camera through update/prepare_frame/composite and collect IO."""
+
+    import torch
+
+    from planet_renderer_gb300 import camera as cam
+    from planet_renderer_gb300.atmosphere import scene
+    from planet_renderer_gb300.lighting import LightingState
+
+    AtmosphereConfig, View, Renderer = _import_reference(reference)
+    config = AtmosphereConfig(**config_kwargs)
+    renderer = reuse if reuse is not None else Renderer(width, height, config)
+    basis = cam.view_basis(yaw_deg, pitch_deg)
+    tanfov = cam.tangent_half_fov(60.0)
+    sun = cam.sun_from_zenith(sun_zenith_deg, sun_azimuth_deg)
+    lighting = LightingState(sun, sun_angular_radius_degrees, solar_irradiance)
+    camera_radius = planet_radius + camera_altitude
+
+    if sample_pixels is None:
+        pixels = None
+        gb = scene.synthesize_gbuffer(width, height, planet_radius, camera_altitude, basis, tanfov, sun,
+                                      solar_irradiance, seed=seed)
+    else:
+        pixels = np.asarray(sample_pixels, dtype=np.int64)
+        gb = scene.synthesize_gbuffer(width, height, planet_radius, camera_altitude, basis, tanfov, sun,
+                                      solar_irradiance, seed=seed, pixels=torch.as_tensor(pixels))
+    gb = {k: v.numpy() for k, v in gb.items()}
+
+    position = shim.Vector.field(3, dtype=shim.f32, shape=(width, height))
+    surface = shim.field(dtype=shim.i32, shape=(width, height))
+    surface.fill(-1)
+    scene_hdr = shim.Vector.field(3, dtype=shim.f32, shape=(width, height))
+    space_hdr = shim.Vector.field(3, dtype=shim.f32, shape=(width, height))
+    hdr = shim.Vector.field(3, dtype=shim.f32, shape=(width, height))
+    if pixels is None:
+        _fill_field(position, gb["position_view"])
+        _fill_field(surface, gb["surface_id"])
+        _fill_field(scene_hdr, gb["scene_hdr"])
+        _fill_field(space_hdr, gb["space_hdr"])
+    else:
+        for k, (x, y) in enumerate(pixels):
+            position[x, y] = gb["position_view"][k]
+            surface[x, y] = gb["surface_id"][k]
+            scene_hdr[x, y] = gb["scene_hdr"][k]
+            space_hdr[x, y] = gb["space_hdr"][k]
+        shim.restrict_iteration(surface, [tuple(p) for p in pixels])
+        shim.restrict_iteration(hdr, [tuple(p) for p in pixels])
+        # the reference's per-pixel surface fields are frame sized
+        shim.restrict_iteration(renderer.surface_sun_transmittance, [tuple(p) for p in pixels])
+
+    t0 = time.time()
+    renderer.update(planet_radius, camera_radius, sun.copy(), solar_irradiance, sun_angular_radius_degrees)
+    t_update = time.time() - t0
+    t0 = time.time()
+    renderer.prepare_frame(position, surface, planet_radius, camera_radius, sun.copy(), solar_irradiance,
+                           sun_angular_radius_degrees, basis, tanfov)
+    t_prepare = time.time() - t0
+
+    out = {}
+    out["transmittance_lut"] = renderer.transmittance_lut.to_numpy()
+    out["multi_scattering_lut"] = renderer.multi_scattering_lut.to_numpy()
+    out["sky_view_lut"] = renderer.sky_view_lut.to_numpy()
+    out["aerial_scattering_lut"] = renderer.aerial_scattering_lut.to_numpy()
+    sun_t = renderer.surface_sun_transmittance.to_numpy()
+    sky_l = renderer.surface_sky_radiance.to_numpy()
+    views = list(View) if views is None else views
+    t0 = time.time()
+    for view in views:
+        hdr.fill(0.0)
+        renderer.composite(scene_hdr, space_hdr, surface, position, hdr, planet_radius, camera_radius, sun.copy(),
+                           solar_irradiance, lighting.sun_disk_radiance, sun_angular_radius_degrees, basis, tanfov,
+                           4.0, 12.0, view)
+        result = hdr.to_numpy()
+        out[f"hdr_view{int(view)}"] = result if pixels is None else result[pixels[:, 0], pixels[:, 1]]
+    t_composite = time.time() - t0
+    shim.clear_restrictions()
+
+    if pixels is None:
+        out.update({k: v for k, v in gb.items()})
+        out["surface_sun_transmittance"] = sun_t
+        out["surface_sky_radiance"] = sky_l
+    else:
+        out.update({k: v for k, v in gb.items()})
+        out["pixels"] = pixels.astype(np.int32)
+        out["surface_sun_transmittance"] = sun_t[pixels[:, 0], pixels[:, 1]]
+        out["surface_sky_radiance"] = sky_l[pixels[:, 0], pixels[:, 1]]
+
+    meta = dict(
+        name=name,
+        config=dict(config_kwargs),
+        planet_radius_m=planet_radius,
+        camera_radius_m=camera_radius,
+        camera_altitude_m=camera_altitude,
+        sun_local=[float(v) for v in sun],
+        solar_irradiance=list(solar_irradiance),
+        sun_disk_radiance=list(lighting.sun_disk_radiance),
+        sun_angular_radius_degrees=sun_angular_radius_degrees,
+        view_basis=[[float(v) for v in b] for b in basis],
+        tangent_half_fov=tanfov,
+        star_contrast=[4.0, 12.0],
+        width=width,
+        height=height,
+        views=[int(v) for v in views],
+        seed=seed,
+        sky_snapshot_altitude_m=renderer.sky_snapshot_altitude_m,
+        sky_snapshot_sun_cosine=renderer.sky_snapshot_sun_cosine,
+        rebuilds=[renderer.transmittance_rebuilds, renderer.multi_scattering_rebuilds,
+                  renderer.sky_view_rebuilds, renderer.aerial_rebuilds],
+        seconds=dict(update=t_update, prepare=t_prepare, composite=t_composite),
+        generator="tests/golden/make_golden.py (reference kernels under taichi_f32_shim)",
+    )
+    out["meta"] = np.array(json.dumps(meta))
+    print(f"[{name}] update {t_update:.1f}s prepare {t_prepare:.1f}s composite {t_composite:.1f}s", flush=True)
+    return out, renderer
+
+
+def _sample_pixels(width, height, rng, n_random, column_stride):
+    pts = {(int(x), int(y)) for x, y in zip(rng.integers(0, width, n_random), rng.integers(0, height, n_random))}
+    for y in range(0, height, column_stride):
+        pts.add((width // 2, y))
+        pts.add((width // 5, y))
+    return sorted(pts)
+
+
+def earth_config1_kwargs():
+    return dict(
+        mie_extinction_per_m=(3.996e-6 + 4.4e-6,) * 3,
+        sky_view_lut_height=108,
+        multi_scattering_directions=64,
+        multi_scattering_steps=20,
+        sky_view_steps=30,
+        aerial_lut_height=32,
+        aerial_horizon_raymarch_steps=48,
+    )
+
+
+def main() -> None:
+    parser = argparse.ArgumentParser()
+    parser.add_argument("--reference", type=Path, default=Path("/root/reference"))
+    parser.add_argument("--only", nargs="*")
+    parser.add_argument("--precision", choices=("f32", "f64"), default="f32",
+                        help="f64 runs the same reference source in double (tiny scenarios only)")
+    args = parser.parse_args()
+    shim.set_precision(args.precision)
+    suffix = "" if args.precision == "f32" else "_f64"
+    wanted = set(args.only or [])
+
+    def want(name):
+        return not wanted or name in wanted
+
+    if want("tiny_earth"):
+        out, _ = run_scenario("tiny_earth", args.reference, TINY_LUTS, 6_360_000.0, 1000.0, 40.0, 25.0, 0.0, -30.0,
+                              24, 16, seed=5)
+        np.savez_compressed(HERE / f"tiny_earth{suffix}.npz", **out)
+    if want("tiny_small_planet"):
+        kwargs = dict(TINY_LUTS, top_altitude_m=15_000.0, rayleigh_scale_height_m=3_000.0, mie_scale_height_m=800.0,
+                      absorption_peak_altitude_m=7_500.0, absorption_half_width_m=5_000.0)
+        out, _ = run_scenario("tiny_small_planet", args.reference, kwargs, 50_000.0, 3000.0, 91.0, 30.0, 10.0, -10.0,
+                              24, 16, seed=11)
+        np.savez_compressed(HERE / f"tiny_small_planet{suffix}.npz", **out)
+    if want("tiny_orbit"):
+        out, _ = run_scenario("tiny_orbit", args.reference, dict(TINY_LUTS, aerial_horizon_raymarch_steps=16),
+                              6_360_000.0, 2_000_000.0, 95.0, 60.0, 0.0, -35.0, 24, 16, seed=7)
+        np.savez_compressed(HERE / f"tiny_orbit{suffix}.npz", **out)
+    renderer = None
+    if args.precision == "f64":
+        return
+    if want("earth_config1") or want("earth_cameras"):
+        rng = np.random.default_rng(1234)
+        pixels = _sample_pixels(1920, 1080, rng, 60, 60)
+        out, renderer = run_scenario("earth_config1", args.reference, earth_config1_kwargs(), 6_360_000.0, 2000.0,
+                                     45.0, 30.0, 0.0, -35.0, 1920, 1080, sample_pixels=pixels, seed=2027,
+                                     views=[0, 1, 2, 6, 8])
+        np.savez_compressed(HERE / "earth_config1.npz", **out)
+    if want("earth_cameras"):
+        for altitude, zenith, azimuth, tag in ((50_000.0, 88.0, 140.0, "50km"), (2_000_000.0, 95.0, 60.0, "2000km")):
+            rng = np.random.default_rng(int(altitude))
+            pixels = _sample_pixels(1920, 1080, rng, 60, 60)
+            out, renderer = run_scenario(f"earth_camera_{tag}", args.reference, earth_config1_kwargs(), 6_360_000.0,
+                                         altitude, zenith, azimuth, 0.0, -35.0, 1920, 1080, sample_pixels=pixels,
+                                         seed=2027, reuse=renderer, views=[0, 2])
+            # T and MS are unchanged from earth_config1 (same keys); keep the file small
+            out.pop("transmittance_lut")
+            out.pop("multi_scattering_lut")
+            np.savez_compressed(HERE / f"earth_camera_{tag}.npz", **out)
+
+
+if __name__ == "__main__":
+    main()

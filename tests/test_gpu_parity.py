@@ -1,0 +1,211 @@
+"""GPU kernels vs the reference (golden vectors) and vs the CPU oracle.
+
+Criterion (conftest.assert_parity): per RGB channel
+|gpu - ref| <= 1e-3 |ref| + 1e-5 max|ref|.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+
+from conftest import assert_parity, load_golden, parity_report
+from scenario import Scenario, gpu_chain, gpu_stages, oracle_stages_with_luts
+
+pytestmark = pytest.mark.gpu
+
+TINY = ["tiny_earth", "tiny_small_planet", "tiny_orbit"]
+
+
+def _compare(out, ref, what):
+    return {k: assert_parity(v, ref[k], f"{what}:{k}") for k, v in out.items()}
+
+
+@pytest.mark.parametrize("name", TINY + ["earth_config1"])
+def test_gpu_kernels_match_reference(name):
+    data, meta = load_golden(name)
+    _compare(gpu_stages(Scenario(data, meta)), data, name)
+
+
+@pytest.mark.parametrize("name", ["earth_camera_50km", "earth_camera_2000km"])
+def test_gpu_kernels_match_reference_cameras(name):
+    base, _ = load_golden("earth_config1")
+    data, meta = load_golden(name)
+    out = gpu_stages(Scenario(data, meta), T=base["transmittance_lut"], M=base["multi_scattering_lut"])
+    _compare(out, data, name)
+
+
+@pytest.mark.parametrize("name", TINY)
+def test_gpu_public_chain_matches_reference(name):
+    data, meta = load_golden(name)
+    out, r = gpu_chain(Scenario(data, meta))
+    _compare(out, data, name)
+    assert [r.transmittance_rebuilds, r.multi_scattering_rebuilds, r.sky_view_rebuilds,
+            r.aerial_rebuilds] == meta["rebuilds"]
+    assert r.sky_snapshot_altitude_m == meta["sky_snapshot_altitude_m"]
+    assert r.sky_snapshot_sun_cosine == meta["sky_snapshot_sun_cosine"]
+
+
+def _camera_frame(width, height, altitude, sun_zenith, sun_azimuth, seed=2027):
+    import torch
+
+    from planet_renderer_gb300 import camera
+    from planet_renderer_gb300.atmosphere import scene
+
+    basis = camera.view_basis(0.0, -35.0)
+    tanfov = camera.tangent_half_fov(60.0)
+    sun = camera.sun_from_zenith(sun_zenith, sun_azimuth)
+    gb = scene.synthesize_gbuffer(width, height, 6_360_000.0, altitude, basis, tanfov, sun, seed=seed,
+                                  device="cuda")
+    return gb, basis, tanfov, sun
+
+
+@pytest.mark.parametrize("altitude,zenith,azimuth", [(2_000.0, 45.0, 30.0), (50_000.0, 88.0, 140.0),
+                                                     (2_000_000.0, 95.0, 60.0), (2_000_000.0, 60.0, 10.0)])
+def test_gpu_full_frame_matches_oracle(altitude, zenith, azimuth, oracle_f32):
+    """Every pixel of a 128x72 frame (Earth workload LUT sizes) vs the oracle,
+    including the radiance-sample count."""
+
+    import torch
+
+    from oracle.atm import OracleAtmosphere, sun_disk_radiance
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+
+    W, H = 128, 72
+    cfg = earth_baseline()
+    gb, basis, tanfov, sun = _camera_frame(W, H, altitude, zenith, azimuth)
+    R = 6_360_000.0
+    cr = R + altitude
+    E = (4.0, 3.9, 3.7)
+    disk = sun_disk_radiance(E, 0.266)
+    r = AtmosphereRenderer(W, H, cfg)
+    r.update(R, cr, sun.copy(), E, 0.266)
+    r.prepare_frame(gb["position_view"], gb["surface_id"], R, cr, sun, E, 0.266, basis, tanfov)
+    hdr = torch.zeros_like(gb["scene_hdr"])
+    r.radiance_samples(reset=True)
+    r.composite(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"], hdr, R, cr, sun, E, disk,
+                0.266, basis, tanfov, 4.0, 12.0)
+    gpu_samples = r.radiance_samples()
+    o = OracleAtmosphere(W, H, cfg)
+    o.update(R, cr, sun.copy(), E, 0.266)
+    host = {k: v.cpu().numpy() for k, v in gb.items()}
+    o.prepare_frame(host["position_view"], host["surface_id"], R, cr, sun, E, 0.266, basis, tanfov)
+    ref, cpu_samples = o.composite(host["scene_hdr"], host["space_hdr"], host["surface_id"], host["position_view"], R,
+                                   cr, sun, E, disk, 0.266, basis, tanfov, 4.0, 12.0, 0)
+    for key in ("transmittance_lut", "multi_scattering_lut", "sky_view_lut", "aerial_scattering_lut"):
+        assert_parity(getattr(r, key).to_numpy(), getattr(o, key), key)
+    assert_parity(r.surface_sun_transmittance.cpu().numpy(), o.surface_sun_transmittance, "sun_t")
+    assert_parity(r.surface_sky_radiance.cpu().numpy(), o.surface_sky_radiance, "sky")
+    assert_parity(hdr.cpu().numpy(), ref, "composite")
+    assert cpu_samples > 0
+    assert abs(gpu_samples - cpu_samples) <= 0.01 * cpu_samples
+
+
+def test_gpu_freeze_and_rebuild_counters():
+    """LUT freeze keeps the view-dependent snapshots; resume rebuilds; a 2 m
+    altitude change rebuilds the sky-view LUT once (reference
+    tests/test_m2_terrain.py:363-399)."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere import AtmosphereConfig, AtmosphereRenderer
+
+    cfg = AtmosphereConfig(transmittance_lut_width=16, transmittance_lut_height=16, multi_scattering_lut_width=8,
+                           multi_scattering_lut_height=8, sky_view_lut_width=16, sky_view_lut_height=16,
+                           aerial_lut_width=4, aerial_lut_height=4, aerial_lut_depth=8, transmittance_steps=4,
+                           multi_scattering_directions=4, multi_scattering_steps=4, sky_view_steps=4,
+                           aerial_steps_per_slice=1)
+    W, H = 32, 24
+    r = AtmosphereRenderer(W, H, cfg)
+    R = 6_360_000.0
+    cr = R + 1000.0
+    sun = np.array([0.2, 0.8, 0.4])
+    sun /= np.linalg.norm(sun)
+    pos = torch.zeros(W, H, 3, device="cuda")
+    sid = torch.full((W, H), -1, dtype=torch.int32, device="cuda")
+    basis = ((1.0, 0.0, 0.0), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0))
+
+    def frame(radius):
+        r.update(R, radius, sun.copy(), (4.0, 3.9, 3.7), 0.266)
+        r.prepare_frame(pos, sid, R, radius, sun, (4.0, 3.9, 3.7), 0.266, basis, 0.577)
+
+    frame(cr)
+    assert (r.transmittance_rebuilds, r.multi_scattering_rebuilds, r.sky_view_rebuilds, r.aerial_rebuilds) == (
+        1, 1, 1, 1)
+    r.set_luts_frozen(True)
+    frozen = (r.sky_view_rebuilds, r.aerial_rebuilds)
+    cr += 2.0
+    for _ in range(3):
+        frame(cr)
+    assert (r.sky_view_rebuilds, r.aerial_rebuilds) == frozen
+    assert r.luts_frozen
+    r.set_luts_frozen(False)
+    frame(cr)
+    assert r.sky_view_rebuilds > frozen[0] and r.aerial_rebuilds > frozen[1]
+    live = r.sky_view_rebuilds
+    cr += 2.0
+    frame(cr)
+    assert r.sky_view_rebuilds == live + 1
+    frame(cr)
+    assert r.sky_view_rebuilds == live + 1  # unchanged keys: no rebuild
+    assert r.transmittance_rebuilds == 1 and r.multi_scattering_rebuilds == 1
+    r.update(R + 10.0, cr, sun.copy(), (4.0, 3.9, 3.7), 0.266)  # new planet radius rebuilds everything
+    assert (r.transmittance_rebuilds, r.multi_scattering_rebuilds) == (2, 2)
+
+
+def test_gpu_layouts_agree():
+    """(H, W, 4) images give the same pixels as (W, H, 3) ones."""
+
+    import torch
+
+    from oracle.atm import sun_disk_radiance
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+
+    W, H = 64, 40
+    gb, basis, tanfov, sun = _camera_frame(W, H, 50_000.0, 70.0, 20.0)
+    R, cr, E = 6_360_000.0, 6_410_000.0, (4.0, 3.9, 3.7)
+    disk = sun_disk_radiance(E, 0.266)
+    outs = []
+    for layout, channels in (("wh", 3), ("hw", 4)):
+        r = AtmosphereRenderer(W, H, earth_baseline(), layout=layout)
+
+        def conv(t):
+            if t.dim() == 3:
+                t = torch.cat([t, torch.zeros_like(t[..., :1])], dim=-1) if channels == 4 else t
+            return t.transpose(0, 1).contiguous() if layout == "hw" else t.contiguous()
+
+        g = {k: conv(v) for k, v in gb.items()}
+        hdr = torch.zeros_like(g["scene_hdr"])
+        r.surface_sun_transmittance = torch.zeros_like(g["scene_hdr"])
+        r.surface_sky_radiance = torch.zeros_like(g["scene_hdr"])
+        r.update(R, cr, sun.copy(), E, 0.266)
+        r.prepare_frame(g["position_view"], g["surface_id"], R, cr, sun, E, 0.266, basis, tanfov)
+        r.composite(g["scene_hdr"], g["space_hdr"], g["surface_id"], g["position_view"], hdr, R, cr, sun, E, disk,
+                    0.266, basis, tanfov, 4.0, 12.0)
+        h = hdr[..., :3]
+        outs.append((h.transpose(0, 1) if layout == "hw" else h).cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
+
+
+def test_gpu_rejects_bad_arguments():
+    import torch
+
+    from planet_renderer_gb300.atmosphere import AtmosphereConfig, AtmosphereRenderer
+
+    with pytest.raises(ValueError):
+        AtmosphereConfig(sky_view_lut_width=8)
+    r = AtmosphereRenderer(16, 16, AtmosphereConfig())
+    good = torch.zeros(16, 16, 3, device="cuda")
+    sid = torch.zeros(16, 16, dtype=torch.int32, device="cuda")
+    with pytest.raises(ValueError):
+        r.composite(good, good, sid, good, torch.zeros(8, 16, 3, device="cuda"), 6.36e6, 6.361e6, (0, 1, 0),
+                    (4, 4, 4), (1, 1, 1), 0.266, ((1, 0, 0), (0, 1, 0), (0, 0, 1)), 0.5, 4.0, 12.0)
+    with pytest.raises(ValueError):
+        r.prepare_frame(good, sid.to(torch.int64), 6.36e6, 6.361e6, (0, 1, 0), (4, 4, 4), 0.266,
+                        ((1, 0, 0), (0, 1, 0), (0, 0, 1)), 0.5)
+    with pytest.raises(ValueError):
+        r.update(float("nan"), 6.361e6, (0, 1, 0), (4, 4, 4), 0.266)
