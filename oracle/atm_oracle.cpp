@@ -40,6 +40,19 @@ namespace {
 constexpr double kPi = 3.141592653589793;     // math.pi (renderer.py:12)
 constexpr double kLarge = 1.0e30;             // _LARGE_DISTANCE (:13)
 
+
+// Math entry points: plain libm for float/double, overloads for the counting
+// type below (found by argument-dependent lookup).
+template <class R> inline R m_sqrt(R x) { using std::sqrt; return sqrt(x); }
+template <class R> inline R m_exp(R x) { using std::exp; return exp(x); }
+template <class R> inline R m_acos(R x) { using std::acos; return acos(x); }
+template <class R> inline R m_cos(R x) { using std::cos; return cos(x); }
+template <class R> inline R m_sin(R x) { using std::sin; return sin(x); }
+template <class R> inline R m_pow(R x, R y) { using std::pow; return pow(x, y); }
+template <class R> inline R m_atan2(R y, R x) { using std::atan2; return atan2(y, x); }
+template <class R> inline R m_fabs(R x) { using std::fabs; return fabs(x); }
+template <class R> inline R m_floor(R x) { using std::floor; return floor(x); }
+
 template <class R>
 struct V3 {
   R x, y, z;
@@ -53,14 +66,14 @@ template <class R> inline V3<R> operator*(V3<R> a, R s) { return {a.x * s, a.y *
 template <class R> inline V3<R> operator/(V3<R> a, R s) { return {a.x / s, a.y / s, a.z / s}; }
 template <class R> inline V3<R> operator/(V3<R> a, V3<R> b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
 template <class R> inline R dot(V3<R> a, V3<R> b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
-template <class R> inline R norm(V3<R> a) { return std::sqrt(dot(a, a)); }
+template <class R> inline R norm(V3<R> a) { return m_sqrt(dot(a, a)); }
 template <class R> inline R mx(R a, R b) { return a > b ? a : b; }  // ti.max
 template <class R> inline R mn(R a, R b) { return a < b ? a : b; }  // ti.min
 template <class R> inline R clampr(R x, R lo, R hi) { return mn(mx(x, lo), hi); }
 template <class R> inline V3<R> vmax(V3<R> a, R s) { return {mx(a.x, s), mx(a.y, s), mx(a.z, s)}; }
 template <class R> inline V3<R> vmin(V3<R> a, R s) { return {mn(a.x, s), mn(a.y, s), mn(a.z, s)}; }
 template <class R> inline V3<R> vclamp(V3<R> a, R lo, R hi) { return vmin(vmax(a, lo), hi); }
-template <class R> inline V3<R> vexp(V3<R> a) { return {std::exp(a.x), std::exp(a.y), std::exp(a.z)}; }
+template <class R> inline V3<R> vexp(V3<R> a) { return {m_exp(a.x), m_exp(a.y), m_exp(a.z)}; }
 template <class R> inline V3<R> splat(R s) { return {s, s, s}; }
 
 // Read-only LUT views in the Taichi field layout (W, H[, D], 3).
@@ -103,9 +116,9 @@ struct Model {
   V3<R> density(R h) const {
     R ray = R(0), mie = R(0), ozone = R(0);
     if (R(0) <= h && h <= top()) {
-      ray = std::exp(-h / R(P.rayleigh_scale_height_m));
-      mie = std::exp(-h / R(P.mie_scale_height_m));
-      ozone = mx(R(1) - std::fabs(h - R(P.absorption_peak_altitude_m)) / R(P.absorption_half_width_m), R(0));
+      ray = m_exp(-h / R(P.rayleigh_scale_height_m));
+      mie = m_exp(-h / R(P.mie_scale_height_m));
+      ozone = mx(R(1) - m_fabs(h - R(P.absorption_peak_altitude_m)) / R(P.absorption_half_width_m), R(0));
     }
     return {ray, mie, ozone};
   }
@@ -129,7 +142,7 @@ struct Model {
     farv = -R(kLarge);
     if (hit) {
       R disc = mx(clearance, R(0)) * (radius + perpendicular);
-      R root = std::sqrt(mx(disc, R(0)));
+      R root = m_sqrt(mx(disc, R(0)));
       nearv = -projected - root;
       farv = -projected + root;
     }
@@ -137,14 +150,14 @@ struct Model {
   // _shell_rho :228-235
   R shell_rho(R h, R bottom) const {
     R a = mx(h, R(0));
-    return std::sqrt(a * (R(2) * bottom + a));
+    return m_sqrt(a * (R(2) * bottom + a));
   }
   // _altitude_on_ray :237-262
   R altitude_on_ray(R h0, R cosv, R t, R bottom) const {
     R a = mx(h0, R(0));
     R orad = bottom + a;
     R delta = (a * (R(2) * bottom + a) + R(2) * orad * cosv * t) + t * t;
-    R len = std::sqrt(mx(bottom * bottom + delta, R(0)));
+    R len = m_sqrt(mx(bottom * bottom + delta, R(0)));
     return delta / mx(len + bottom, R(1));
   }
   // _shell_roots_from_altitude :264-301
@@ -157,12 +170,12 @@ struct Model {
     nearv = R(kLarge);
     farv = -R(kLarge);
     if (hit) {
-      R root = std::sqrt(mx(disc, R(0)));
+      R root = m_sqrt(mx(disc, R(0)));
       R sign = hl < R(0) ? R(-1) : R(1);
       R q = -hl - sign * root;
       R r0 = -hl - root;
       R r1 = -hl + root;
-      if (std::fabs(q) > R(1.0e-12)) {
+      if (m_fabs(q) > R(1.0e-12)) {
         r0 = q;
         r1 = c / q;
       }
@@ -222,13 +235,13 @@ struct Model {
     R radius = bottom + mx(h, R(0));
     R delta = (top() - h) * ((R(2) * bottom + top()) + h);
     R disc = radius * radius * cosv * cosv + delta;
-    return mx(-radius * cosv + std::sqrt(mx(disc, R(0))), R(0));
+    return mx(-radius * cosv + m_sqrt(mx(disc, R(0))), R(0));
   }
   // _transmittance_uv_to_ray :410-432
   void t_uv_to_ray(R u, R v, R bottom, R& h, R& cosv, R& dist) const {
     R sh = shell_rho(top(), bottom);
     R rho = sh * clampr(v, R(0), R(1));
-    R rl = std::sqrt(rho * rho + bottom * bottom);
+    R rl = m_sqrt(rho * rho + bottom * bottom);
     h = rho * rho / mx(rl + bottom, R(1));
     R radius = bottom + h;
     R dmin = top() - h;
@@ -277,7 +290,7 @@ struct Model {
     R a = mx(h, R(0));
     R radius = bottom + a;
     R tc = shell_rho(a, bottom) / mx(radius, R(1));
-    return R(kPi) - std::acos(clampr(tc, R(0), R(1)));
+    return R(kPi) - m_acos(clampr(tc, R(0), R(1)));
   }
   // _sky_v_to_zenith :492-504
   R sky_v_to_zenith(R v, R h, R bottom) const {
@@ -294,10 +307,10 @@ struct Model {
     R hz = sky_horizon_zenith(h, bottom);
     if (z < hz) {
       R n = clampr(z / mx(hz, R(1.0e-6)), R(0), R(1));
-      return R(0.5) * (R(1) - std::sqrt(mx(R(1) - n, R(0))));
+      return R(0.5) * (R(1) - m_sqrt(mx(R(1) - n, R(0))));
     }
     R n = clampr((z - hz) / mx(R(kPi) - hz, R(1.0e-6)), R(0), R(1));
-    return R(0.5) + R(0.5) * std::sqrt(n);
+    return R(0.5) + R(0.5) * m_sqrt(n);
   }
   R horizon_cosine(R h, R bottom) const {
     R radius = bottom + mx(h, R(0));
@@ -321,10 +334,10 @@ struct Model {
     R hc = horizon_cosine(h, bottom);
     if (c < hc) {
       R n = clampr((hc - c) / mx(hc + R(1), R(1.0e-6)), R(0), R(1));
-      return R(0.5) * (R(1) - std::sqrt(n));
+      return R(0.5) * (R(1) - m_sqrt(n));
     }
     R n = clampr((c - hc) / mx(R(1) - hc, R(1.0e-6)), R(0), R(1));
-    return R(0.5) + R(0.5) * std::sqrt(n);
+    return R(0.5) + R(0.5) * m_sqrt(n);
   }
   // _integrate_extinction :570-607
   V3<R> integrate_extinction(V3<R> o, V3<R> d, R start, R end, R bottom) const {
@@ -346,8 +359,8 @@ struct Model {
   static V3<R> bilinear(const Lut2<R>& L, R u, R v) {
     R x = clampr(u * R(L.w) - R(0.5), R(0), R(L.w - 1));
     R y = clampr(v * R(L.h) - R(0.5), R(0), R(L.h - 1));
-    int x0 = static_cast<int>(std::floor(x));
-    int y0 = static_cast<int>(std::floor(y));
+    int x0 = static_cast<int>(m_floor(x));
+    int y0 = static_cast<int>(m_floor(y));
     int x1 = std::min(x0 + 1, L.w - 1);
     int y1 = std::min(y0 + 1, L.h - 1);
     R fx = x - R(x0);
@@ -366,7 +379,7 @@ struct Model {
   V3<R> sample_ms(R h, R sc, R bottom) const {
     R af = clampr(h / top(), R(0), R(1));
     R u = sun_cosine_to_u(sc, mx(h, R(0)), bottom);
-    R v = std::sqrt(af);
+    R v = m_sqrt(af);
     return bilinear(mslut, u, v);
   }
   // _solar_shadow_roots :685-726
@@ -380,7 +393,7 @@ struct Model {
     r0 = R(0); r1 = R(0); v0 = 0; v1 = 0;
     R disc = hl * hl - quad * c;
     if (quad > R(1.0e-8) && disc >= R(0)) {
-      R sr = std::sqrt(mx(disc, R(0)));
+      R sr = m_sqrt(mx(disc, R(0)));
       r0 = (-hl - sr) / quad;
       r1 = (-hl + sr) / quad;
       V3<R> p0 = o + d * r0;
@@ -392,20 +405,20 @@ struct Model {
   // _solar_disk_visibility :728-754
   R disk_visibility(R h, R sc, R bottom, R ar) const {
     R hc = horizon_cosine(h, bottom);
-    R hz = std::acos(clampr(hc, R(-1), R(1)));
-    R sz = std::acos(clampr(sc, R(-1), R(1)));
+    R hz = m_acos(clampr(hc, R(-1), R(1)));
+    R sz = m_acos(clampr(sc, R(-1), R(1)));
     R sep = hz - sz;
     R n = clampr(sep / mx(ar, R(1.0e-6)), R(-1), R(1));
-    return (std::acos(-n) + n * std::sqrt(mx(R(1) - n * n, R(0)))) / R(kPi);
+    return (m_acos(-n) + n * m_sqrt(mx(R(1) - n * n, R(0)))) / R(kPi);
   }
   // _sample_solar_transmittance :756-789
   V3<R> sample_solar_t(R h, R sc, R bottom, R ar) const {
     R vis = disk_visibility(h, sc, bottom, ar);
     R hc = horizon_cosine(h, bottom);
-    R hz = std::acos(clampr(hc, R(-1), R(1)));
-    R sz = std::acos(clampr(sc, R(-1), R(1)));
+    R hz = m_acos(clampr(hc, R(-1), R(1)));
+    R sz = m_acos(clampr(sc, R(-1), R(1)));
     R rz = mn(sz, hz - ar * R(0.25));
-    R rc = std::cos(mx(rz, R(0)));
+    R rc = m_cos(mx(rz, R(0)));
     return sample_t(h, rc, bottom) * vis;
   }
   // _rayleigh_phase :791-793
@@ -414,7 +427,7 @@ struct Model {
   R mie_phase(R c) const {
     const double g = P.mie_phase_g;  // a Python float: constant terms fold in double
     R den = mx(R(1.0 + g * g) - R(2.0 * g) * c, R(1.0e-8));
-    return R(3.0 * (1.0 - g * g)) * (R(1) + c * c) / (R(8.0 * kPi * (2.0 + g * g)) * std::pow(den, R(1.5)));
+    return R(3.0 * (1.0 - g * g)) * (R(1) + c * c) / (R(8.0 * kPi * (2.0 + g * g)) * m_pow(den, R(1.5)));
   }
   // _segment_integral :806-816
   void segment_integral(V3<R> ext, R step, V3<R>& tr, V3<R>& integ) const {
@@ -457,8 +470,8 @@ struct Model {
     R mid = (start + end) * R(0.5);
     R iw = mx(end - start, R(1.0e-4));
     R cr = R(1.0e30);
-    if (sv0 != 0) cr = mn(cr, std::fabs(mid - sr0));
-    if (sv1 != 0) cr = mn(cr, std::fabs(mid - sr1));
+    if (sv0 != 0) cr = mn(cr, m_fabs(mid - sr0));
+    if (sv1 != 0) cr = mn(cr, m_fabs(mid - sr1));
     R prox = clampr(R(2) - cr / iw, R(0), R(1));
     prox = prox * prox * (R(3) - R(2) * prox);
     V3<R> point = o + ray * mid;
@@ -497,12 +510,12 @@ struct Model {
   }
   // _sample_sky_view :1474-1525
   V3<R> sample_sky_view(V3<R> ray, V3<R> sun, R cam_alt, R bottom) const {
-    R zen = std::acos(clampr(ray.y, R(-1), R(1)));
-    R vl = std::sqrt(ray.x * ray.x + ray.z * ray.z);
-    R sl = std::sqrt(sun.x * sun.x + sun.z * sun.z);
+    R zen = m_acos(clampr(ray.y, R(-1), R(1)));
+    R vl = m_sqrt(ray.x * ray.x + ray.z * ray.z);
+    R sl = m_sqrt(sun.x * sun.x + sun.z * sun.z);
     R ra = R(0);
     if (vl > R(1.0e-6) && sl > R(1.0e-6))
-      ra = std::acos(clampr((ray.x * sun.x + ray.z * sun.z) / (vl * sl), R(-1), R(1)));
+      ra = m_acos(clampr((ray.x * sun.x + ray.z * sun.z) / (vl * sl), R(-1), R(1)));
     R u = ra / R(kPi);
     R v = sky_zenith_to_v(zen, cam_alt, bottom);
     return bilinear(svlut, u, v);
@@ -513,7 +526,7 @@ struct Model {
     R x = clampr(su * R(F.w) - R(0.5), R(0), R(F.w - 1));
     R y = clampr(sv * R(F.h) - R(0.5), R(0), R(F.h - 1));
     R z = clampr(df, R(0), R(1)) * R(F.d - 1);
-    int x0 = static_cast<int>(std::floor(x)), y0 = static_cast<int>(std::floor(y)), z0 = static_cast<int>(std::floor(z));
+    int x0 = static_cast<int>(m_floor(x)), y0 = static_cast<int>(m_floor(y)), z0 = static_cast<int>(m_floor(z));
     int x1 = std::min(x0 + 1, F.w - 1), y1 = std::min(y0 + 1, F.h - 1), z1 = std::min(z0 + 1, F.d - 1);
     R fx = x - R(x0), fy = y - R(y0), fz = z - R(z0);
     V3<R> a = F.at(x0, y0, z0) * (R(1) - fx) + F.at(x1, y0, z0) * fx;
@@ -619,7 +632,7 @@ void build_transmittance(const AtmParams& P, R bottom, R* out) {
     R v = (R(y) + R(0.5)) / R(H);
     R h, c, d;
     m.t_uv_to_ray(u, v, bottom, h, c, d);
-    R s = std::sqrt(mx(R(1) - c * c, R(0)));
+    R s = m_sqrt(mx(R(1) - c * c, R(0)));
     R radius = bottom + h;
     V3<R> o = v3(R(0), radius, R(0));
     V3<R> ray = v3(s, c, R(0));
@@ -645,16 +658,16 @@ void build_multi_scattering(const AtmParams& P, R bottom, const R* E3, R ar, con
     R h0 = v * v * m.top();
     R radius = bottom + h0;
     R sc = m.sun_u_to_cosine(u, h0, bottom);
-    R ss = std::sqrt(mx(R(1) - sc * sc, R(0)));
+    R ss = m_sqrt(mx(R(1) - sc * sc, R(0)));
     V3<R> sun = v3(ss, sc, R(0));
     V3<R> o = v3(R(0), radius, R(0));
     V3<R> Lsum = splat(R(0)), Fsum = splat(R(0));
     for (int di = 0; di < ndir; ++di) {
       R si = R(di) + R(0.5);
       R dc = R(1) - R(2) * si / R(ndir);
-      R ds = std::sqrt(mx(R(1) - dc * dc, R(0)));
+      R ds = m_sqrt(mx(R(1) - dc * dc, R(0)));
       R az = R(di) * R(2.39996323);
-      V3<R> ray = v3(ds * std::cos(az), dc, ds * std::sin(az));
+      V3<R> ray = v3(ds * m_cos(az), dc, ds * m_sin(az));
       R s, e; bool valid, ground;
       m.segment_vec(o, ray, bottom, s, e, valid, ground);
       V3<R> dL = splat(R(0)), dF = splat(R(0)), pT = splat(R(1));
@@ -705,7 +718,7 @@ void build_sky_view(const AtmParams& P, R bottom, R cam_alt, R sun_cos, const R*
   m.mslut = {mslut, P.multi_scattering_lut_width, P.multi_scattering_lut_height};
   const V3<R> E = load3(E3);
   const int W = P.sky_view_lut_width, H = P.sky_view_lut_height, n = P.sky_view_steps;
-  R ss = std::sqrt(mx(R(1) - sun_cos * sun_cos, R(0)));
+  R ss = m_sqrt(mx(R(1) - sun_cos * sun_cos, R(0)));
   V3<R> sun = v3(ss, sun_cos, R(0));
   R sh = mx(cam_alt, R(0));
   R sr = bottom + sh;
@@ -716,8 +729,8 @@ void build_sky_view(const AtmParams& P, R bottom, R cam_alt, R sun_cos, const R*
     R az = (R(x) + R(0.5)) / R(W) * R(kPi);
     R vv = (R(y) + R(0.5)) / R(H);
     R zen = m.sky_v_to_zenith(vv, sh, bottom);
-    R vc = std::cos(zen), vs = std::sin(zen);
-    V3<R> ray = v3(vs * std::cos(az), vc, vs * std::sin(az));
+    R vc = m_cos(zen), vs = m_sin(zen);
+    V3<R> ray = v3(vs * m_cos(az), vc, vs * m_sin(az));
     R s, e; bool valid, ground;
     m.segment_from_altitude(sh, vc, bottom, s, e, valid, ground);
     V3<R> rad = splat(R(0));
@@ -877,8 +890,8 @@ V3<R> composite_pixel(const Model<R>& m, const CompositeArgs& A, int px, int py,
       R vis = clampr((contrast - R(A.star_start)) / mx(R(A.star_end) - R(A.star_start), R(1.0e-5)), R(0), R(1));
       vis = vis * vis * (R(3) - R(2) * vis);
       color = (sky + color * tr) + star * vis;
-      R ad = std::acos(clampr(dot(ray, sun), R(-1), R(1)));
-      R pf = std::atan2(tanfov * R(1.41421356) / R(H), R(1));
+      R ad = m_acos(clampr(dot(ray, sun), R(-1), R(1)));
+      R pf = m_atan2(tanfov * R(1.41421356) / R(H), R(1));
       R cov = clampr((ar + pf - ad) / mx(R(2) * pf, R(1.0e-8)), R(0), R(1));
       cov = cov * cov * (R(3) - R(2) * cov);
       color = color + disk * tr * cov;
@@ -941,6 +954,43 @@ int64_t composite(const AtmParams& P, const CompositeArgs& A, Image img, const R
 
 }  // namespace
 
+
+// ---- operation counting --------------------------------------------------
+// CountF behaves as float and counts every arithmetic operation the
+// restatement performs: the algorithmic operation count of the reference's
+// kernels (comparisons, min/max and clamps are not counted).  Counters are
+// per thread; counting runs use one thread.
+namespace opcount {
+enum { kAdd, kMul, kDiv, kSqrt, kExp, kAcos, kCosSin, kPow, kAtan2, kN };
+thread_local uint64_t counts[kN];
+struct CountF {
+  float v;
+  CountF() = default;
+  constexpr CountF(double x) : v(float(x)) {}
+  explicit operator int() const { return int(v); }
+};
+inline CountF mkc(float x) { CountF r; r.v = x; return r; }
+inline CountF operator+(CountF a, CountF b) { ++counts[kAdd]; return mkc(a.v + b.v); }
+inline CountF operator-(CountF a, CountF b) { ++counts[kAdd]; return mkc(a.v - b.v); }
+inline CountF operator-(CountF a) { return mkc(-a.v); }
+inline CountF operator*(CountF a, CountF b) { ++counts[kMul]; return mkc(a.v * b.v); }
+inline CountF operator/(CountF a, CountF b) { ++counts[kDiv]; return mkc(a.v / b.v); }
+inline bool operator<(CountF a, CountF b) { return a.v < b.v; }
+inline bool operator>(CountF a, CountF b) { return a.v > b.v; }
+inline bool operator<=(CountF a, CountF b) { return a.v <= b.v; }
+inline bool operator>=(CountF a, CountF b) { return a.v >= b.v; }
+inline CountF sqrt(CountF x) { ++counts[kSqrt]; return mkc(std::sqrt(x.v)); }
+inline CountF exp(CountF x) { ++counts[kExp]; return mkc(std::exp(x.v)); }
+inline CountF acos(CountF x) { ++counts[kAcos]; return mkc(std::acos(x.v)); }
+inline CountF cos(CountF x) { ++counts[kCosSin]; return mkc(std::cos(x.v)); }
+inline CountF sin(CountF x) { ++counts[kCosSin]; return mkc(std::sin(x.v)); }
+inline CountF pow(CountF x, CountF y) { ++counts[kPow]; return mkc(std::pow(x.v, y.v)); }
+inline CountF atan2(CountF y, CountF x) { ++counts[kAtan2]; return mkc(std::atan2(y.v, x.v)); }
+inline CountF fabs(CountF x) { return mkc(std::fabs(x.v)); }
+inline CountF floor(CountF x) { return mkc(std::floor(x.v)); }
+static_assert(sizeof(CountF) == sizeof(float), "CountF must alias float buffers");
+}  // namespace opcount
+
 // ---- C entry points for ctypes -------------------------------------------
 #define ORC_EXPORT extern "C" __attribute__((visibility("default")))
 
@@ -990,6 +1040,16 @@ int64_t composite(const AtmParams& P, const CompositeArgs& A, Image img, const R
 
 ORC_DEFINE(f32, float)
 ORC_DEFINE(f64, double)
+ORC_DEFINE(cnt, opcount::CountF)
+
+// Operation counts of the calling thread since the last reset: add/sub, mul,
+// div, sqrt, exp, acos, cos+sin, pow, atan2.
+ORC_EXPORT void orc_op_counts(uint64_t out[9], int reset) {
+  for (int i = 0; i < opcount::kN; ++i) {
+    out[i] = opcount::counts[i];
+    if (reset) opcount::counts[i] = 0;
+  }
+}
 
 ORC_EXPORT int orc_max_threads(void) {
 #ifdef _OPENMP

@@ -200,7 +200,7 @@ int build_multi_scattering(AtmHandle* h, double R, const double E[3], double ar,
   float e[3];
   to_f32(E, e, 3);
   ATM_CUDA(atm::launch_multi_scattering(h->dev, float(R), e, float(ar), h->lut[ATM_LUT_TRANSMITTANCE],
-                                        h->lut[ATM_LUT_MULTI_SCATTERING], s),
+                                        h->lut[ATM_LUT_MULTI_SCATTERING], h->samples, s),
            "multi-scattering build");
   return ATM_OK;
 }
@@ -211,7 +211,7 @@ int build_sky_view(AtmHandle* h, double R, double alt, double sun_cos, const dou
   to_f32(E, e, 3);
   ATM_CUDA(atm::launch_sky_view(h->dev, float(R), float(alt), float(sun_cos), e, float(ar),
                                 h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
-                                h->lut[ATM_LUT_SKY_VIEW], s),
+                                h->lut[ATM_LUT_SKY_VIEW], h->samples, s),
            "sky-view build");
   return ATM_OK;
 }
@@ -224,7 +224,7 @@ int build_aerial(AtmHandle* h, int width, int height, double R, double alt, cons
   to_f32(basis, b, 9);
   ATM_CUDA(atm::launch_aerial(h->dev, width, height, float(R), float(alt), sn, e, float(ar), b, b + 3, b + 6,
                               float(tanfov), h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
-                              h->lut[ATM_LUT_AERIAL], s),
+                              h->lut[ATM_LUT_AERIAL], h->samples, s),
            "aerial-perspective build");
   return ATM_OK;
 }

@@ -65,6 +65,15 @@ __device__ __forceinline__ f3 from4(float4 v) { return {v.x, v.y, v.z}; }
 __device__ __forceinline__ float4 to4(f3 v) { return make_float4(v.x, v.y, v.z, 0.0f); }
 __device__ __forceinline__ f3 arr3(const float (&a)[3]) { return {a[0], a[1], a[2]}; }
 
+// Adds a per-lane count into a device counter: one atomic per warp.  Every
+// lane of the warp must call it (no lane may have exited before).
+__device__ __forceinline__ void warp_count(uint32_t n, unsigned long long* counter) {
+  __syncwarp();
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if (counter != nullptr && (threadIdx.x & 31) == 0 && n) atomicAdd(counter, (unsigned long long)n);
+}
+
 // Composition of two consecutive ray segments: (L1,T1) then (L2,T2).
 struct Seg {
   f3 L, T;

@@ -231,15 +231,6 @@ __device__ __forceinline__ f3 composite_sky(const DevParams& P, const Frame& F, 
   return color + arr3(A.disk) * tr * cov;
 }
 
-__device__ __forceinline__ void warp_count(uint32_t samples, unsigned long long* counter) {
-  // every lane of the warp reaches this point (no early exits before it)
-  __syncwarp();
-  uint32_t total = samples;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) total += __shfl_xor_sync(kFull, total, o);
-  if (counter != nullptr && (threadIdx.x & 31) == 0 && total) atomicAdd(counter, (unsigned long long)total);
-}
-
 // COMPOSITE view (:1860-1940): the per-frame path.
 __global__ void __launch_bounds__(256) k_composite(DevParams P, ImageLayout L, CompositeScalars A,
                                                    const float* __restrict__ scene, const float* __restrict__ space,

@@ -27,13 +27,17 @@ struct CompositeScalars {
 };
 
 cudaError_t launch_transmittance(const DevParams& P, float bottom, float4* out, cudaStream_t s);
+// The LUT builds and the composite add the radiance samples they evaluate to
+// `counter` (may be null).
 cudaError_t launch_multi_scattering(const DevParams& P, float bottom, const float E[3], float ar,
-                                    const float4* tlut, float4* out, cudaStream_t s);
+                                    const float4* tlut, float4* out, unsigned long long* counter, cudaStream_t s);
 cudaError_t launch_sky_view(const DevParams& P, float bottom, float cam_alt, float sun_cos, const float E[3],
-                            float ar, const float4* tlut, const float4* mslut, float4* out, cudaStream_t s);
+                            float ar, const float4* tlut, const float4* mslut, float4* out,
+                            unsigned long long* counter, cudaStream_t s);
 cudaError_t launch_aerial(const DevParams& P, int width, int height, float bottom, float cam_alt, const float sun[3],
                           const float E[3], float ar, const float right[3], const float up[3], const float fwd[3],
-                          float tanfov, const float4* tlut, const float4* mslut, float4* out, cudaStream_t s);
+                          float tanfov, const float4* tlut, const float4* mslut, float4* out,
+                          unsigned long long* counter, cudaStream_t s);
 cudaError_t launch_prepare_surface(const DevParams& P, const ImageLayout& L, const float* pos, const int32_t* sid,
                                    float bottom, float cam_alt, const float sun[3], float ar, const float right[3],
                                    const float up[3], const float fwd[3], const float4* tlut, const float4* mslut,

@@ -100,7 +100,8 @@ constexpr int kMaxDirs = 128;
 
 __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, float bottom, f3 E, float ar,
                                                                const float4* __restrict__ tlut,
-                                                               float4* __restrict__ out) {
+                                                               float4* __restrict__ out,
+                                                               unsigned long long* counter) {
   __shared__ f3 s_l[kMaxDirs];
   __shared__ f3 s_f[kMaxDirs];
   const int texel = blockIdx.x;
@@ -115,6 +116,7 @@ __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, floa
   Frame F{tlut, nullptr, bottom, shell_rho(P.top, bottom), ar, mk(ss, sc, 0.0f), E};
   f3 o = mk(0.0f, radius, 0.0f);
   f3 dL = splat(0.0f), dF = splat(0.0f);
+  uint32_t samples = 0;
   if (di < P.ms_dirs) {
     const int ndir = P.ms_dirs;
     float si = float(di) + 0.5f;
@@ -154,6 +156,7 @@ __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, floa
         pT = pT * sT;
         d0 = d1;
       }
+      samples = uint32_t(n);
       if (ground) {
         f3 gp = o + ray * end;
         f3 gn = gp * (1.0f / norm(gp));  // Taichi normalized(): v * (1/|v|)
@@ -165,6 +168,7 @@ __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, floa
       }
     }
   }
+  warp_count(samples, counter);
   s_l[di] = dL;
   s_f[di] = dF;
   __syncthreads();
@@ -183,7 +187,8 @@ __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, floa
 // ---- sky-view (:1208-1302) ----------------------------------------------------
 __global__ void __launch_bounds__(256) k_sky_view(DevParams P, float bottom, float cam_alt, float sun_cos, f3 E,
                                                   float ar, const float4* __restrict__ tlut,
-                                                  const float4* __restrict__ mslut, float4* __restrict__ out) {
+                                                  const float4* __restrict__ mslut, float4* __restrict__ out,
+                                                  unsigned long long* counter) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int n_texels = P.sv_w * P.sv_h;
@@ -204,6 +209,7 @@ __global__ void __launch_bounds__(256) k_sky_view(DevParams P, float bottom, flo
   bool valid, ground;
   segment_from_altitude(P, sh, vc, bottom, start, end, valid, ground);
   Seg acc = seg_identity();
+  uint32_t samples = 0;
   if (valid) {
     const float cr = clampf(dot(ray, F.sun), -1.0f, 1.0f);
     const float phase_r = rayleigh_phase(P, cr);
@@ -222,8 +228,10 @@ __global__ void __launch_bounds__(256) k_sky_view(DevParams P, float bottom, flo
         acc = seg_then(acc, s);
         d0 = d1;
       }
+      samples = uint32_t(i1 - i0);
     }
   }
+  warp_count(samples, counter);
   acc = warp_compose(acc);
   if (lane == 0) out[y * P.sv_w + x] = to4(vmax(acc.L, 0.0f));
 }
@@ -232,7 +240,7 @@ __global__ void __launch_bounds__(256) k_sky_view(DevParams P, float bottom, flo
 // Segment of depth slice k along a column's prefix interval [as, ae].
 __device__ __forceinline__ Seg aerial_slice(const DevParams& P, const Frame& F, float o_y, float cam_alt, f3 ray,
                                             float as, float ae, bool valid, int k, float phase_r, float phase_m,
-                                            float closest_raw) {
+                                            float closest_raw, uint32_t& samples) {
   Seg acc = seg_identity();
   const float denom = float(P.ap_d - 1);
   float prev = k == 0 ? as : as + (ae - as) * (float(k - 1) / denom);
@@ -249,6 +257,7 @@ __device__ __forceinline__ Seg aerial_slice(const DevParams& P, const Frame& F, 
         acc = seg_then(acc, source_segment<true>(P, F, o_y, cam_alt, ray, ray.y, d0, d1, phase_r, phase_m, vis));
         d0 = d1;
       }
+      samples += uint32_t(n);
     }
   }
   return acc;
@@ -257,7 +266,7 @@ __device__ __forceinline__ Seg aerial_slice(const DevParams& P, const Frame& F, 
 __global__ void __launch_bounds__(256) k_aerial(DevParams P, float aspect, float bottom, float cam_alt, f3 sun, f3 E,
                                                 float ar, f3 right, f3 up, f3 fwd, float tanfov,
                                                 const float4* __restrict__ tlut, const float4* __restrict__ mslut,
-                                                float4* __restrict__ out) {
+                                                float4* __restrict__ out, unsigned long long* counter) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp_id >= P.ap_w * P.ap_h) return;  // warp-uniform
@@ -282,8 +291,11 @@ __global__ void __launch_bounds__(256) k_aerial(DevParams P, float aspect, float
   const size_t plane = size_t(P.ap_w) * P.ap_h;
   // pass 1: each lane composes its own run of slices
   Seg run = seg_identity();
+  uint32_t samples = 0;
   for (int k = lane * per; k < min(lane * per + per, depth); ++k)
-    run = seg_then(run, aerial_slice(P, F, o_y, cam_alt, ray, as, ae, valid, k, phase_r, phase_m, closest_raw));
+    run = seg_then(run,
+                   aerial_slice(P, F, o_y, cam_alt, ray, as, ae, valid, k, phase_r, phase_m, closest_raw, samples));
+  warp_count(samples, counter);
   // exclusive prefix of the runs
   Seg incl = warp_scan(run);
   Seg prefix = shfl_up_seg(incl, 1);
@@ -294,8 +306,10 @@ __global__ void __launch_bounds__(256) k_aerial(DevParams P, float aspect, float
   }
   // pass 2 (depth > 32): walk the run again writing cumulative values
   Seg acc = prefix;
+  uint32_t recomputed = 0;  // second evaluation of the same samples: not counted
   for (int k = lane * per; k < min(lane * per + per, depth); ++k) {
-    acc = seg_then(acc, aerial_slice(P, F, o_y, cam_alt, ray, as, ae, valid, k, phase_r, phase_m, closest_raw));
+    acc = seg_then(acc,
+                   aerial_slice(P, F, o_y, cam_alt, ray, as, ae, valid, k, phase_r, phase_m, closest_raw, recomputed));
     out[size_t(k) * plane + size_t(y) * P.ap_w + x] = to4(vmax(acc.L, 0.0f));
   }
 }
@@ -332,31 +346,33 @@ cudaError_t launch_transmittance(const DevParams& P, float bottom, float4* out, 
 }
 
 cudaError_t launch_multi_scattering(const DevParams& P, float bottom, const float E[3], float ar,
-                                    const float4* tlut, float4* out, cudaStream_t s) {
+                                    const float4* tlut, float4* out, unsigned long long* counter, cudaStream_t s) {
   if (P.ms_dirs > kMaxDirs) return cudaErrorInvalidValue;
   const int threads = ((P.ms_dirs + 31) / 32) * 32;
-  k_multi_scattering<<<P.ms_w * P.ms_h, threads, 0, s>>>(P, bottom, host3(E), ar, tlut, out);
+  k_multi_scattering<<<P.ms_w * P.ms_h, threads, 0, s>>>(P, bottom, host3(E), ar, tlut, out, counter);
   return cudaGetLastError();
 }
 
 cudaError_t launch_sky_view(const DevParams& P, float bottom, float cam_alt, float sun_cos, const float E[3],
-                            float ar, const float4* tlut, const float4* mslut, float4* out, cudaStream_t s) {
+                            float ar, const float4* tlut, const float4* mslut, float4* out,
+                            unsigned long long* counter, cudaStream_t s) {
   const int threads = 256;
   const long long total = 32LL * P.sv_w * P.sv_h;
   k_sky_view<<<unsigned((total + threads - 1) / threads), threads, 0, s>>>(P, bottom, cam_alt, sun_cos, host3(E), ar,
-                                                                          tlut, mslut, out);
+                                                                          tlut, mslut, out, counter);
   return cudaGetLastError();
 }
 
 cudaError_t launch_aerial(const DevParams& P, int width, int height, float bottom, float cam_alt, const float sun[3],
                           const float E[3], float ar, const float right[3], const float up[3], const float fwd[3],
-                          float tanfov, const float4* tlut, const float4* mslut, float4* out, cudaStream_t s) {
+                          float tanfov, const float4* tlut, const float4* mslut, float4* out,
+                          unsigned long long* counter, cudaStream_t s) {
   const int threads = 256;
   const long long total = 32LL * P.ap_w * P.ap_h;
   const float aspect = float(width) / float(height);
   k_aerial<<<unsigned((total + threads - 1) / threads), threads, 0, s>>>(
       P, aspect, bottom, cam_alt, host3(sun), host3(E), ar, host3(right), host3(up), host3(fwd), tanfov, tlut, mslut,
-      out);
+      out, counter);
   return cudaGetLastError();
 }
 
