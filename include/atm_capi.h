@@ -201,6 +201,35 @@ int atm_load_lut(AtmHandle* handle, int32_t kind, const float* src_device, void*
  * reset.  Synchronises `stream`. */
 int atm_read_sample_counter(AtmHandle* handle, int32_t reset, uint64_t* out, void* stream);
 
+/* COMPOSITE view of atm_composite that allocates nothing.  No counterpart in
+ * the reference.  For callers that may not call cudaMalloc: an engine or
+ * plugin host that owns every device allocation through its own pool, a
+ * real-time frame loop where an allocation's implicit synchronisation and
+ * latency are not acceptable, a process running under a fixed device-memory
+ * budget.  Everything is caller-owned: the transmittance, multi-scattering
+ * and sky-view LUTs (device buffers of float4 texels, row-major [y][x], with
+ * the sizes in `params`, as atm_lut_info describes them), the images and
+ * `samples_out` (device, may be null).  The only scratch is a fixed array of
+ * 65,536 per-tile sample counts (256 KB) inside the library; every GPU that
+ * loads the library holds it until the process exits.  Frames needing more
+ * than 65,536 16x16 tiles (16.7 million pixels) are rejected with
+ * ATM_E_INVALID.  The first call on each device looks the array's address up
+ * (cudaGetSymbolAddress) with that device current: make that first call
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU (other streams, other threads) race on it and may report wrong
+ * sample counts.  Each call writes every tile slot it later sums, so nothing
+ * needs clearing between calls.  sky_lut_camera_altitude_m is the altitude
+ * the sky-view LUT was built for (atm_update's f32-rounded key).  Writes hdr
+ * and, when samples_out is set, the frame's radiance-sample count. */
+int atm_composite_noalloc(const AtmParams* params, const void* transmittance_lut, const void* multi_scattering_lut,
+                          const void* sky_view_lut, const float* scene_hdr, const float* space_hdr,
+                          const int32_t* surface_id, const float* position_view, float* hdr, const AtmImage* image,
+                          double planet_radius_m, double camera_radius_m, double sky_lut_camera_altitude_m,
+                          const double sun_local[3], const double solar_irradiance[3],
+                          const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                          const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                          double star_contrast_end, uint64_t* samples_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

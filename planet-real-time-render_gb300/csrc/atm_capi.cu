@@ -496,3 +496,61 @@ ATM_API int atm_read_sample_counter(AtmHandle* h, int32_t reset, uint64_t* out, 
   if (out) *out = v;
   return ATM_OK;
 }
+
+// Composite that allocates nothing (no counterpart in the reference).  See
+// include/atm_capi.h: caller-owned LUTs, images and count output; the only
+// scratch is the library's file-scope per-tile array.
+ATM_API int atm_composite_noalloc(const AtmParams* params, const void* transmittance_lut,
+                                  const void* multi_scattering_lut, const void* sky_view_lut,
+                                  const float* scene_hdr, const float* space_hdr, const int32_t* surface_id,
+                                  const float* position_view, float* hdr, const AtmImage* image,
+                                  double planet_radius_m, double camera_radius_m, double sky_lut_camera_altitude_m,
+                                  const double sun_local[3], const double solar_irradiance[3],
+                                  const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                                  const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                                  double star_contrast_end, uint64_t* samples_out, void* stream) {
+  if (params == nullptr) return fail(ATM_E_INVALID, "null AtmParams");
+  int rc = validate(*params);
+  if (rc) return rc;
+  if (!transmittance_lut || !multi_scattering_lut || !sky_view_lut || !scene_hdr || !space_hdr || !surface_id ||
+      !position_view || !hdr || !image || !sun_local || !solar_irradiance || !sun_disk_radiance || !view_basis)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_composite_noalloc");
+  if (image->width < 1 || image->height < 1 || image->stride_x <= 0 || image->stride_y <= 0 ||
+      (image->channels != 3 && image->channels != 4))
+    return fail(ATM_E_INVALID, "invalid AtmImage");
+  const long long tiles = (long long)((image->width + 15) / 16) * ((image->height + 15) / 16);
+  if (tiles > atm::noalloc_max_tiles())
+    return fail(ATM_E_INVALID,
+                "frame %dx%d needs %lld 16x16 tiles; atm_composite_noalloc's fixed scratch holds %d tiles "
+                "(16.7 million pixels): use atm_composite for larger frames",
+                image->width, image->height, tiles, atm::noalloc_max_tiles());
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0 || !std::isfinite(planet_radius_m) || !std::isfinite(camera_radius_m))
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  uint32_t* scratch = nullptr;
+  ATM_CUDA(atm::noalloc_tile_scratch(&scratch), "no-allocation scratch set-up (cudaGetSymbolAddress)");
+  const double alt = std::fmax(camera_radius_m - planet_radius_m, 0.0);
+  atm::CompositeScalars A{};
+  A.bottom = float(planet_radius_m);
+  A.cam_alt = float(alt);
+  A.sky_alt = float(sky_lut_camera_altitude_m);
+  A.ar = radians_f32(sun_angular_radius_degrees);
+  A.tanfov = float(tangent_half_fov);
+  A.star_start = float(star_contrast_start);
+  A.star_end = float(star_contrast_end);
+  to_f32(sun_local, A.sun, 3);
+  to_f32(solar_irradiance, A.E, 3);
+  to_f32(sun_disk_radiance, A.disk, 3);
+  to_f32(view_basis, A.right, 3);
+  to_f32(view_basis + 3, A.up, 3);
+  to_f32(view_basis + 6, A.fwd, 3);
+  A.view = ATM_VIEW_COMPOSITE;
+  ATM_CUDA(atm::launch_composite_noalloc(atm::make_dev_params(*params), layout_of(image), A, scene_hdr, space_hdr,
+                                         surface_id, position_view, static_cast<const float4*>(transmittance_lut),
+                                         static_cast<const float4*>(multi_scattering_lut),
+                                         static_cast<const float4*>(sky_view_lut), hdr, scratch,
+                                         reinterpret_cast<unsigned long long*>(samples_out),
+                                         static_cast<cudaStream_t>(stream)),
+           "composite (no allocation)");
+  return ATM_OK;
+}

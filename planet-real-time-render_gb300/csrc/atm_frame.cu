@@ -11,6 +11,8 @@
 // sample, which the reference computes twice from identical inputs.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "atm_device.cuh"
 #include "atm_kernels.h"
 
@@ -395,6 +397,118 @@ cudaError_t launch_composite(const DevParams& P, const ImageLayout& L, const Com
   else
     k_composite_views<<<tile_grid(L), 256, 0, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, aplut, hdr,
                                                    sample_counter);
+  return cudaGetLastError();
+}
+
+
+// ---- composite that allocates nothing -------------------------------------
+// Scratch of atm_composite_noalloc: one radiance-sample count per 16x16
+// pixel tile.  It lives in this file-scope device array, so a caller that
+// may not allocate device memory can still get the sample count; every GPU
+// that loads the library holds these 256 KB until the process exits.  Host
+// code must not use the symbol as an address: noalloc_tile_scratch() looks
+// the device address up with cudaGetSymbolAddress.
+constexpr int kNoAllocMaxTiles = 1 << 16;  // 65,536 tiles = 16.7 Mpx
+static __device__ __align__(256) uint32_t g_noalloc_tile_samples[kNoAllocMaxTiles];
+
+namespace {
+
+// COMPOSITE view of k_composite; the block's sample count goes to its tile
+// slot instead of an atomic counter (every launched block writes its slot).
+__global__ void __launch_bounds__(256) k_composite_tiles(DevParams P, ImageLayout L, CompositeScalars A,
+                                                         const float* __restrict__ scene,
+                                                         const float* __restrict__ space,
+                                                         const int32_t* __restrict__ sid,
+                                                         const float* __restrict__ pos,
+                                                         const float4* __restrict__ tlut,
+                                                         const float4* __restrict__ mslut,
+                                                         const float4* __restrict__ svlut, float* __restrict__ hdr,
+                                                         uint32_t* __restrict__ tile_samples) {
+  __shared__ uint32_t s_warp[8];
+  int x, y;
+  const bool inside = tile_pixel(L, x, y);
+  uint32_t samples = 0;
+  if (inside) {
+    const size_t e = pix_offset(L, x, y);
+    const size_t o = e * L.channels;
+    Frame F{tlut, mslut, A.bottom, shell_rho(P.top, A.bottom), A.ar, arr3(A.sun), arr3(A.E)};
+    PixelRay pr = pixel_ray(L, A, x, y);
+    f3 color = ld3(scene + o);
+    if (sid[e] >= 0) {
+      float sd = norm(ld3(pos + o));
+      float start, end;
+      if (surface_interval(P, A.cam_alt, pr.ray.y, A.bottom, sd, start, end)) {
+        f3 scat = integrate_surface(P, F, A.cam_alt, pr.ray, start, end, samples);
+        f3 tr = surface_segment_t(P, F, A.cam_alt, pr.ray, start, end);
+        color = scat + color * tr;
+      }
+    } else {
+      color = composite_sky(P, F, A, svlut, pr.ray, color, ld3(space + o), float(L.height));
+    }
+    color = vmax(color, 0.0f);
+    hdr[o + 0] = color.x;
+    hdr[o + 1] = color.y;
+    hdr[o + 2] = color.z;
+  }
+  __syncwarp();
+#pragma unroll
+  for (int k = 16; k > 0; k >>= 1) samples += __shfl_xor_sync(kFull, samples, k);
+  if ((threadIdx.x & 31) == 0) s_warp[threadIdx.x >> 5] = samples;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t total = 0;
+    for (int w = 0; w < 8; ++w) total += s_warp[w];
+    tile_samples[blockIdx.y * gridDim.x + blockIdx.x] = total;
+  }
+}
+
+// Sum of n tile counts into *out (one block, fixed order: deterministic).
+__global__ void __launch_bounds__(1024) k_sum_tiles(const uint32_t* __restrict__ tiles, int n,
+                                                    unsigned long long* __restrict__ out) {
+  __shared__ unsigned long long s[1024];
+  unsigned long long acc = 0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) acc += tiles[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = s[0];
+}
+
+std::mutex g_noalloc_mutex;
+uint32_t* g_noalloc_address[kMaxDevices] = {};
+
+}  // namespace
+
+int noalloc_max_tiles() { return kNoAllocMaxTiles; }
+
+cudaError_t noalloc_tile_scratch(uint32_t** out) {
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) return e;
+  if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (g_noalloc_address[device] == nullptr) {
+    void* address = nullptr;
+    e = cudaGetSymbolAddress(&address, g_noalloc_tile_samples);  // with `device` current
+    if (e != cudaSuccess) return e;
+    g_noalloc_address[device] = static_cast<uint32_t*>(address);
+  }
+  *out = g_noalloc_address[device];
+  return cudaSuccess;
+}
+
+cudaError_t launch_composite_noalloc(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                                     const float* scene, const float* space, const int32_t* sid, const float* pos,
+                                     const float4* tlut, const float4* mslut, const float4* svlut, float* hdr,
+                                     uint32_t* tile_scratch, unsigned long long* samples_out, cudaStream_t s) {
+  const dim3 grid = tile_grid(L);
+  k_composite_tiles<<<grid, 256, 0, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, hdr, tile_scratch);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || samples_out == nullptr) return e;
+  k_sum_tiles<<<1, 1024, 0, s>>>(tile_scratch, int(grid.x * grid.y), samples_out);
   return cudaGetLastError();
 }
 

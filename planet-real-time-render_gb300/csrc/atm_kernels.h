@@ -51,4 +51,15 @@ cudaError_t launch_lut_to_fields(const float4* lut, int w, int h, int d, float* 
 // Taichi field layout (W, H[, D], 3) floats -> LUT (float4 [z][y][x]).
 cudaError_t launch_fields_to_lut(const float* src, int w, int h, int d, float4* lut, cudaStream_t s);
 
+// atm_composite_noalloc: the per-device address of the file-scope tile
+// scratch (looked up on the first call on each device), its capacity in
+// 16x16 tiles, and the COMPOSITE-view launch that uses it.
+constexpr int kMaxDevices = 64;
+int noalloc_max_tiles();
+cudaError_t noalloc_tile_scratch(uint32_t** out);
+cudaError_t launch_composite_noalloc(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                                     const float* scene, const float* space, const int32_t* sid, const float* pos,
+                                     const float4* tlut, const float4* mslut, const float4* svlut, float* hdr,
+                                     uint32_t* tile_scratch, unsigned long long* samples_out, cudaStream_t s);
+
 }  // namespace atm

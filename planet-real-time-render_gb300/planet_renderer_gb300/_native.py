@@ -140,6 +140,11 @@ SIGNATURES = {
     "atm_read_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_load_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_read_sample_counter": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
+    "atm_composite_noalloc": (
+        ctypes.c_int,
+        [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,
+         c_double3, c_double3, _D, c_double9, _D, _D, _D, _P, _P],
+    ),
 }
 
 _LIB: ctypes.CDLL | None = None
