@@ -123,6 +123,10 @@ DevParams make_dev_params(const AtmParams& p) {
   d.mie_k1 = float(3.0 * (1.0 - g * g));
   d.mie_k2 = float(8.0 * kPi * (2.0 + g * g));
   d.ray_k = float(16.0 * kPi);
+  d.inv_h_r = float(1.0 / p.rayleigh_scale_height_m);
+  d.inv_h_m = float(1.0 / p.mie_scale_height_m);
+  d.inv_oz_half = float(1.0 / p.absorption_half_width_m);
+  d.inv_top = float(1.0 / p.top_altitude_m);
   d.t_w = p.transmittance_lut_width;
   d.t_h = p.transmittance_lut_height;
   d.ms_w = p.multi_scattering_lut_width;

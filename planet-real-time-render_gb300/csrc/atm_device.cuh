@@ -35,6 +35,7 @@ struct DevParams {
   float mie_c1, mie_c2;        // f32(1+g^2), f32(2g)
   float mie_k1, mie_k2;        // f32(3(1-g^2)), f32(8 pi (2+g^2))
   float ray_k;                 // f32(16 pi)
+  float inv_h_r, inv_h_m, inv_oz_half, inv_top;  // f32 reciprocals of the above
   int t_w, t_h, ms_w, ms_h, sv_w, sv_h, ap_w, ap_h, ap_d;
   int t_steps, ms_dirs, ms_steps, sv_steps, ap_steps, limb_steps, substeps;
 };
@@ -65,6 +66,20 @@ __device__ __forceinline__ f3 from4(float4 v) { return {v.x, v.y, v.z}; }
 __device__ __forceinline__ float4 to4(f3 v) { return make_float4(v.x, v.y, v.z, 0.0f); }
 __device__ __forceinline__ f3 arr3(const float (&a)[3]) { return {a[0], a[1], a[2]}; }
 
+// Fast forms used where no Earth-scale cancellation follows: division with
+// at most 2 ulp error (div.approx) and square root with at most 1 ulp
+// (sqrt.approx).  Differences ~1e-7 relative against the reference's IEEE
+// operations, far below the 1e-3 parity tolerance.  Subtractions of two
+// Earth-scale quantities keep IEEE sqrtf / division (see callers).
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ float frcp(float b) { return __fdividef(1.0f, b); }
+__device__ __forceinline__ float fsqrt(float x) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float fnorm(f3 a) { return fsqrt(dot(a, a)); }
+
 // Adds a per-lane count into a device counter: one atomic per warp.  Every
 // lane of the warp must call it (no lane may have exited before).
 __device__ __forceinline__ void warp_count(uint32_t n, unsigned long long* counter) {
@@ -87,9 +102,9 @@ struct Density {
 __device__ __forceinline__ Density density(const DevParams& P, float h) {
   Density d{0.0f, 0.0f, 0.0f};
   if (0.0f <= h && h <= P.top) {
-    d.r = expf(-h / P.h_r);
-    d.m = expf(-h / P.h_m);
-    d.o = mx(1.0f - fabsf(h - P.oz_peak) / P.oz_half, 0.0f);
+    d.r = __expf(-h * P.inv_h_r);
+    d.m = __expf(-h * P.inv_h_m);
+    d.o = mx(1.0f - fabsf(h - P.oz_peak) * P.inv_oz_half, 0.0f);
   }
   return d;
 }
@@ -116,14 +131,15 @@ __device__ __forceinline__ void sphere_roots(f3 o, f3 d, float radius, float& ne
 }
 __device__ __forceinline__ float shell_rho(float h, float bottom) {
   float a = mx(h, 0.0f);
-  return sqrtf(a * (2.0f * bottom + a));
+  return fsqrt(a * (2.0f * bottom + a));
 }
+// Cancellation-free form: the altitude never subtracts two Earth-scale radii.
 __device__ __forceinline__ float altitude_on_ray(float h0, float cosv, float t, float bottom) {
   float a = mx(h0, 0.0f);
   float orad = bottom + a;
   float delta = (a * (2.0f * bottom + a) + 2.0f * orad * cosv * t) + t * t;
-  float len = sqrtf(mx(bottom * bottom + delta, 0.0f));
-  return delta / mx(len + bottom, 1.0f);
+  float len = fsqrt(mx(bottom * bottom + delta, 0.0f));
+  return fdiv(delta, mx(len + bottom, 1.0f));
 }
 __device__ __forceinline__ void shell_roots(float h0, float cosv, float shell, float bottom, float& nearv,
                                             float& farv, bool& hit) {
@@ -142,7 +158,7 @@ __device__ __forceinline__ void shell_roots(float h0, float cosv, float shell, f
     float r1 = -hl + root;
     if (fabsf(q) > 1.0e-12f) {
       r0 = q;
-      r1 = c / q;
+      r1 = fdiv(c, q);
     }
     nearv = mn(r0, r1);
     farv = mx(r0, r1);
@@ -211,7 +227,7 @@ __device__ __forceinline__ float distance_to_top(const DevParams& P, float h, fl
   float radius = bottom + mx(h, 0.0f);
   float delta = (P.top - h) * ((2.0f * bottom + P.top) + h);
   float disc = radius * radius * cosv * cosv + delta;
-  return mx(-radius * cosv + sqrtf(mx(disc, 0.0f)), 0.0f);
+  return mx(-radius * cosv + fsqrt(mx(disc, 0.0f)), 0.0f);
 }
 
 // ---- LUT parameterisations (:410-568) ---------------------------------------
@@ -230,14 +246,14 @@ __device__ __forceinline__ void t_uv_to_ray(const DevParams& P, float u, float v
   cosv = clampf(c, -1.0f, 1.0f);
 }
 __device__ __forceinline__ void t_ray_to_uv(const DevParams& P, float h, float cosv, float bottom, float sh,
-                                            float& u, float& v) {
+                                            float inv_sh, float& u, float& v) {
   h = clampf(h, 0.0f, P.top);
   float rho = shell_rho(h, bottom);
   float d = distance_to_top(P, h, cosv, bottom);
   float dmin = P.top - h;
   float dmax = rho + sh;
-  u = clampf((d - dmin) / mx(dmax - dmin, 1.0e-6f), 0.0f, 1.0f);
-  v = clampf(rho / mx(sh, 1.0e-6f), 0.0f, 1.0f);
+  u = clampf(fdiv(d - dmin, mx(dmax - dmin, 1.0e-6f)), 0.0f, 1.0f);
+  v = clampf(rho * inv_sh, 0.0f, 1.0f);
 }
 __device__ __forceinline__ float warp_boundary(float closest_raw, float start, float end, float f) {
   float closest = clampf(closest_raw, start, end);
@@ -256,7 +272,7 @@ __device__ __forceinline__ float warp_boundary(float closest_raw, float start, f
 }
 __device__ __forceinline__ float horizon_cosine(float h, float bottom) {
   float radius = bottom + mx(h, 0.0f);
-  return -shell_rho(h, bottom) / mx(radius, 1.0f);
+  return fdiv(-shell_rho(h, bottom), mx(radius, 1.0f));
 }
 __device__ __forceinline__ float sky_horizon_zenith(float h, float bottom) {
   float a = mx(h, 0.0f);
@@ -294,11 +310,11 @@ __device__ __forceinline__ float sun_u_to_cosine(float u, float h, float bottom)
 }
 __device__ __forceinline__ float sun_cosine_to_u(float c, float hc) {
   if (c < hc) {
-    float n = clampf((hc - c) / mx(hc + 1.0f, 1.0e-6f), 0.0f, 1.0f);
-    return 0.5f * (1.0f - sqrtf(n));
+    float n = clampf(fdiv(hc - c, mx(hc + 1.0f, 1.0e-6f)), 0.0f, 1.0f);
+    return 0.5f * (1.0f - fsqrt(n));
   }
-  float n = clampf((c - hc) / mx(1.0f - hc, 1.0e-6f), 0.0f, 1.0f);
-  return 0.5f + 0.5f * sqrtf(n);
+  float n = clampf(fdiv(c - hc, mx(1.0f - hc, 1.0e-6f)), 0.0f, 1.0f);
+  return 0.5f + 0.5f * fsqrt(n);
 }
 
 // ---- LUT sampling -----------------------------------------------------------
@@ -331,45 +347,87 @@ struct Frame {
   float ar;         // sun angular radius (rad)
   f3 sun;
   f3 E;             // solar irradiance
+  float inv_shell_top;
+  float cos_ar, sin_ar;  // of the sun's angular radius
 };
+__device__ __forceinline__ Frame make_frame(const DevParams& P, const float4* tlut, const float4* mslut,
+                                            float bottom, float ar, f3 sun, f3 E) {
+  Frame F;
+  F.tlut = tlut;
+  F.mslut = mslut;
+  F.bottom = bottom;
+  F.shell_top = sqrtf(mx(P.top, 0.0f) * (2.0f * bottom + mx(P.top, 0.0f)));
+  F.ar = ar;
+  F.sun = sun;
+  F.E = E;
+  F.inv_shell_top = 1.0f / mx(F.shell_top, 1.0e-6f);
+  // thresholds of the whole-disk tests only: intrinsic accuracy suffices
+  F.sin_ar = __sinf(ar);
+  F.cos_ar = __cosf(ar);
+  return F;
+}
 
 // _sample_transmittance_unoccluded :609-640
 __device__ __forceinline__ f3 sample_t(const DevParams& P, const Frame& F, float h, float cosv) {
   float u, v;
-  t_ray_to_uv(P, mx(h, 0.0f), cosv, F.bottom, F.shell_top, u, v);
+  t_ray_to_uv(P, mx(h, 0.0f), cosv, F.bottom, F.shell_top, F.inv_shell_top, u, v);
   return bilinear(F.tlut, P.t_w, P.t_h, u, v);
 }
 // _sample_multi_scattering :642-683
 __device__ __forceinline__ f3 sample_ms(const DevParams& P, const Frame& F, float h, float sc, float hc) {
-  float af = clampf(h / P.top, 0.0f, 1.0f);
+  float af = clampf(h * P.inv_top, 0.0f, 1.0f);
   float u = sun_cosine_to_u(sc, hc);
-  float v = sqrtf(af);
+  float v = fsqrt(af);
   return bilinear(F.mslut, P.ms_w, P.ms_h, u, v);
 }
 
-// Horizon quantities at one sample altitude.
+// Horizon at one sample altitude: cosine hc = -rho/r of the horizon
+// zenith, and sin of that zenith, R/r (rho^2 = r^2 - R^2).
 struct Horizon {
-  float hc;  // horizon cosine
-  float hz;  // horizon zenith
+  float hc;        // horizon cosine
+  float sin_hz;    // sine of the horizon zenith
 };
 __device__ __forceinline__ Horizon horizon_at(float h, float bottom) {
   Horizon H;
-  H.hc = horizon_cosine(h, bottom);
-  H.hz = acosf(clampf(H.hc, -1.0f, 1.0f));
+  float radius = bottom + mx(h, 0.0f);
+  float inv_r = frcp(mx(radius, 1.0f));
+  H.hc = -shell_rho(h, bottom) * inv_r;
+  H.sin_hz = mn(bottom * inv_r, 1.0f);
   return H;
 }
-// _solar_disk_visibility :728-754, given horizon and sun zenith
+// _solar_disk_visibility :728-754, given horizon and sun zenith angles
 __device__ __forceinline__ float disk_visibility(float hz, float sz, float ar) {
-  float n = clampf((hz - sz) / mx(ar, 1.0e-6f), -1.0f, 1.0f);
-  return (acosf(-n) + n * sqrtf(mx(1.0f - n * n, 0.0f))) / kPiF;
+  float n = clampf(fdiv(hz - sz, mx(ar, 1.0e-6f)), -1.0f, 1.0f);
+  return (acosf(-n) + n * sqrtf(mx(1.0f - n * n, 0.0f))) * (1.0f / kPiF);
 }
-// _sample_solar_transmittance :756-789 (returns visibility too)
+// _sample_solar_transmittance :756-789 (returns the disk visibility too).
+// The reference compares the horizon and sun zenith angles; whole-disk
+// cases are decided here in cosine space without acos:
+//   disk fully above the horizon  <=> sz <= hz - ar <=> cos sz >= cos(hz - ar)
+//   disk fully below the horizon  <=> sz >= hz + ar <=> cos sz <= cos(hz + ar)
+// with cos(hz -+ ar) = hc cos ar +- sin hz sin ar.  There the reference's
+// visibility is exactly 1 (its representative zenith is then the sun's own,
+// whose cosine is sc) or exactly 0; within float rounding of the thresholds
+// its visibility differs from 1 or 0 by < 1e-6.  Only the penumbra band
+// evaluates the reference's acos formulation.
 __device__ __forceinline__ f3 sample_solar_t(const DevParams& P, const Frame& F, float h, float sc, Horizon H,
                                              float& vis) {
-  float sz = acosf(clampf(sc, -1.0f, 1.0f));
-  vis = disk_visibility(H.hz, sz, F.ar);
-  float rz = mn(sz, H.hz - F.ar * 0.25f);
-  float rc = cosf(mx(rz, 0.0f));
+  const float cs = clampf(sc, -1.0f, 1.0f);
+  const float a = H.hc * F.cos_ar;
+  const float b = H.sin_hz * F.sin_ar;
+  if (cs >= a + b) {
+    vis = 1.0f;
+    return sample_t(P, F, h, cs);
+  }
+  if (cs <= a - b && H.hc >= -F.cos_ar) {  // hz + ar <= pi
+    vis = 0.0f;
+    return splat(0.0f);
+  }
+  const float hz = acosf(clampf(H.hc, -1.0f, 1.0f));
+  const float sz = acosf(cs);
+  vis = disk_visibility(hz, sz, F.ar);
+  const float rz = mn(sz, hz - F.ar * 0.25f);
+  const float rc = cosf(mx(rz, 0.0f));
   return sample_t(P, F, h, rc) * vis;
 }
 // _rayleigh_phase / _mie_phase :791-804
@@ -383,9 +441,9 @@ __device__ __forceinline__ float mie_phase(const DevParams& P, float c) {
 // _segment_integral :806-816
 __device__ __forceinline__ void segment_integral(f3 ext, float step, f3& tr, f3& integ) {
   tr = vexp(-vmin(ext * step, 80.0f));
-  integ.x = ext.x > 1.0e-12f ? (1.0f - tr.x) / ext.x : step;
-  integ.y = ext.y > 1.0e-12f ? (1.0f - tr.y) / ext.y : step;
-  integ.z = ext.z > 1.0e-12f ? (1.0f - tr.z) / ext.z : step;
+  integ.x = ext.x > 1.0e-12f ? fdiv(1.0f - tr.x, ext.x) : step;
+  integ.y = ext.y > 1.0e-12f ? fdiv(1.0f - tr.y, ext.y) : step;
+  integ.z = ext.z > 1.0e-12f ? fdiv(1.0f - tr.z, ext.z) : step;
 }
 
 // One constant-source sample at `dist` along `ray` from the local-axis origin
@@ -405,8 +463,8 @@ __device__ __forceinline__ Seg source_segment(const DevParams& P, const Frame& F
   Seg s;
   f3 integ;
   segment_integral(ext, step, s.T, integ);
-  float radius = norm(point);
-  f3 radial = point / mx(radius, 1.0f);
+  float radius = fnorm(point);
+  f3 radial = point * frcp(mx(radius, 1.0f));
   float sc = dot(radial, F.sun);
   Horizon H = horizon_at(h, F.bottom);
   f3 st = sample_solar_t(P, F, h, sc, H, vis);

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayou
   if (!tile_pixel(L, x, y)) return;
   const size_t e = pix_offset(L, x, y);
   const size_t o = e * L.channels;
-  Frame F{tlut, mslut, bottom, shell_rho(P.top, bottom), ar, sun, splat(0.0f)};
+  Frame F = make_frame(P, tlut, mslut, bottom, ar, sun, splat(0.0f));
   f3 st = splat(1.0f), sky = splat(0.0f);
   if (sid[e] >= 0) {
     f3 vp = ld3(pos + o);
@@ -234,7 +234,7 @@ __device__ __forceinline__ f3 composite_sky(const DevParams& P, const Frame& F, 
 }
 
 // COMPOSITE view (:1860-1940): the per-frame path.
-__global__ void __launch_bounds__(256) k_composite(DevParams P, ImageLayout L, CompositeScalars A,
+__global__ void __launch_bounds__(256, 3) k_composite(DevParams P, ImageLayout L, CompositeScalars A,
                                                    const float* __restrict__ scene, const float* __restrict__ space,
                                                    const int32_t* __restrict__ sid, const float* __restrict__ pos,
                                                    const float4* __restrict__ tlut, const float4* __restrict__ mslut,
@@ -246,7 +246,7 @@ __global__ void __launch_bounds__(256) k_composite(DevParams P, ImageLayout L, C
   if (inside) {
     const size_t e = pix_offset(L, x, y);
     const size_t o = e * L.channels;
-    Frame F{tlut, mslut, A.bottom, shell_rho(P.top, A.bottom), A.ar, arr3(A.sun), arr3(A.E)};
+    Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
     PixelRay pr = pixel_ray(L, A, x, y);
     f3 color = ld3(scene + o);
     if (sid[e] >= 0) {
@@ -288,7 +288,7 @@ __device__ __forceinline__ f3 sample_aerial_field(const DevParams& P, const floa
 }
 
 // Diagnostic views (:1941-2052); not on the per-frame path.
-__global__ void __launch_bounds__(256) k_composite_views(DevParams P, ImageLayout L, CompositeScalars A,
+__global__ void __launch_bounds__(256, 3) k_composite_views(DevParams P, ImageLayout L, CompositeScalars A,
                                                          const float* __restrict__ scene,
                                                          const float* __restrict__ space,
                                                          const int32_t* __restrict__ sid,
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(256) k_composite_views(DevParams P, ImageLayou
   if (inside) {
     const size_t e = pix_offset(L, x, y);
     const size_t o = e * L.channels;
-    Frame F{tlut, mslut, A.bottom, shell_rho(P.top, A.bottom), A.ar, arr3(A.sun), arr3(A.E)};
+    Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
     PixelRay pr = pixel_ray(L, A, x, y);
     const bool surface = sid[e] >= 0;
     f3 color = ld3(scene + o);
@@ -415,7 +415,7 @@ namespace {
 
 // COMPOSITE view of k_composite; the block's sample count goes to its tile
 // slot instead of an atomic counter (every launched block writes its slot).
-__global__ void __launch_bounds__(256) k_composite_tiles(DevParams P, ImageLayout L, CompositeScalars A,
+__global__ void __launch_bounds__(256, 3) k_composite_tiles(DevParams P, ImageLayout L, CompositeScalars A,
                                                          const float* __restrict__ scene,
                                                          const float* __restrict__ space,
                                                          const int32_t* __restrict__ sid,
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(256) k_composite_tiles(DevParams P, ImageLayou
   if (inside) {
     const size_t e = pix_offset(L, x, y);
     const size_t o = e * L.channels;
-    Frame F{tlut, mslut, A.bottom, shell_rho(P.top, A.bottom), A.ar, arr3(A.sun), arr3(A.E)};
+    Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
     PixelRay pr = pixel_ray(L, A, x, y);
     f3 color = ld3(scene + o);
     if (sid[e] >= 0) {

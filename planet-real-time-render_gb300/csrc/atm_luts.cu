@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, floa
   float radius = bottom + h0;
   float sc = sun_u_to_cosine(u, h0, bottom);
   float ss = sqrtf(mx(1.0f - sc * sc, 0.0f));
-  Frame F{tlut, nullptr, bottom, shell_rho(P.top, bottom), ar, mk(ss, sc, 0.0f), E};
+  Frame F = make_frame(P, tlut, nullptr, bottom, ar, mk(ss, sc, 0.0f), E);
   f3 o = mk(0.0f, radius, 0.0f);
   f3 dL = splat(0.0f), dF = splat(0.0f);
   uint32_t samples = 0;
@@ -195,7 +195,7 @@ __global__ void __launch_bounds__(256) k_sky_view(DevParams P, float bottom, flo
   if (warp_id >= n_texels) return;  // warp-uniform
   const int x = warp_id % P.sv_w, y = warp_id / P.sv_w;
   float ss = sqrtf(mx(1.0f - sun_cos * sun_cos, 0.0f));
-  Frame F{tlut, mslut, bottom, shell_rho(P.top, bottom), ar, mk(ss, sun_cos, 0.0f), E};
+  Frame F = make_frame(P, tlut, mslut, bottom, ar, mk(ss, sun_cos, 0.0f), E);
   float sh = mx(cam_alt, 0.0f);
   float o_y = bottom + sh;
   float az = (float(x) + 0.5f) / float(P.sv_w) * kPiF;
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(256) k_aerial(DevParams P, float aspect, float
   const int lane = threadIdx.x & 31;
   if (warp_id >= P.ap_w * P.ap_h) return;  // warp-uniform
   const int x = warp_id % P.ap_w, y = warp_id / P.ap_w;
-  Frame F{tlut, mslut, bottom, shell_rho(P.top, bottom), ar, sun, E};
+  Frame F = make_frame(P, tlut, mslut, bottom, ar, sun, E);
   const float o_y = bottom + cam_alt;
   float u = (float(x) + 0.5f) / float(P.ap_w);
   float v = (float(y) + 0.5f) / float(P.ap_h);
