@@ -246,14 +246,16 @@ __device__ __forceinline__ void t_uv_to_ray(const DevParams& P, float u, float v
   cosv = clampf(c, -1.0f, 1.0f);
 }
 __device__ __forceinline__ void t_ray_to_uv(const DevParams& P, float h, float cosv, float bottom, float sh,
-                                            float inv_sh, float& u, float& v) {
+                                            float inv_sh, float& u, float& v, float rho_known = -1.0f) {
+  // rho_known: shell_rho(h) already evaluated by the caller for h in [0, top]
+  const bool inside = h >= 0.0f && h <= P.top;
   h = clampf(h, 0.0f, P.top);
-  float rho = shell_rho(h, bottom);
+  float rho = (inside && rho_known >= 0.0f) ? rho_known : shell_rho(h, bottom);
   float d = distance_to_top(P, h, cosv, bottom);
   float dmin = P.top - h;
   float dmax = rho + sh;
-  u = clampf(fdiv(d - dmin, mx(dmax - dmin, 1.0e-6f)), 0.0f, 1.0f);
-  v = clampf(rho * inv_sh, 0.0f, 1.0f);
+  u = __saturatef(fdiv(d - dmin, mx(dmax - dmin, 1.0e-6f)));
+  v = __saturatef(rho * inv_sh);
 }
 __device__ __forceinline__ float warp_boundary(float closest_raw, float start, float end, float f) {
   float closest = clampf(closest_raw, start, end);
@@ -270,6 +272,36 @@ __device__ __forceinline__ float warp_boundary(float closest_raw, float start, f
   float local = f * 2.0f - 1.0f;
   return closest + (end - closest) * local * local;
 }
+// Warped interval boundaries of one ray: the branch of warp_boundary depends
+// only on the ray's closest-approach distance and interval, so it is taken
+// once per ray; each boundary then costs the reference's own expression.
+struct RayWarp {
+  int mode;  // 0: dense at start, 1: dense at end, 2: dense around the closest point
+  float start, end, closest;
+};
+__device__ __forceinline__ RayWarp make_warp(float closest_raw, float start, float end) {
+  RayWarp w;
+  w.start = start;
+  w.end = end;
+  w.closest = clampf(closest_raw, start, end);
+  float eps = mx((end - start) * 1.0e-6f, 1.0e-5f);
+  w.mode = w.closest <= start + eps ? 0 : (w.closest >= end - eps ? 1 : 2);
+  return w;
+}
+__device__ __forceinline__ float warp_at(const RayWarp& w, float f) {
+  if (w.mode == 0) return w.start + (w.end - w.start) * f * f;
+  if (w.mode == 1) {
+    float inv = 1.0f - f;
+    return w.end - (w.end - w.start) * inv * inv;
+  }
+  if (f < 0.5f) {
+    float inv = 1.0f - f * 2.0f;
+    return w.closest - (w.closest - w.start) * inv * inv;
+  }
+  float local = f * 2.0f - 1.0f;
+  return w.closest + (w.end - w.closest) * local * local;
+}
+
 __device__ __forceinline__ float horizon_cosine(float h, float bottom) {
   float radius = bottom + mx(h, 0.0f);
   return fdiv(-shell_rho(h, bottom), mx(radius, 1.0f));
@@ -310,10 +342,10 @@ __device__ __forceinline__ float sun_u_to_cosine(float u, float h, float bottom)
 }
 __device__ __forceinline__ float sun_cosine_to_u(float c, float hc) {
   if (c < hc) {
-    float n = clampf(fdiv(hc - c, mx(hc + 1.0f, 1.0e-6f)), 0.0f, 1.0f);
+    float n = __saturatef(fdiv(hc - c, mx(hc + 1.0f, 1.0e-6f)));
     return 0.5f * (1.0f - fsqrt(n));
   }
-  float n = clampf(fdiv(c - hc, mx(1.0f - hc, 1.0e-6f)), 0.0f, 1.0f);
+  float n = __saturatef(fdiv(c - hc, mx(1.0f - hc, 1.0e-6f)));
   return 0.5f + 0.5f * fsqrt(n);
 }
 
@@ -323,12 +355,13 @@ __device__ __forceinline__ float sun_cosine_to_u(float c, float hc) {
 __device__ __forceinline__ f3 bilinear(const float4* __restrict__ lut, int w, int h, float u, float v) {
   float x = clampf(u * float(w) - 0.5f, 0.0f, float(w - 1));
   float y = clampf(v * float(h) - 0.5f, 0.0f, float(h - 1));
-  int x0 = int(floorf(x));
-  int y0 = int(floorf(y));
+  const float xf = floorf(x), yf = floorf(y);
+  int x0 = int(xf);
+  int y0 = int(yf);
   int x1 = min(x0 + 1, w - 1);
   int y1 = min(y0 + 1, h - 1);
-  float fx = x - float(x0);
-  float fy = y - float(y0);
+  float fx = x - xf;
+  float fy = y - yf;
   f3 a = from4(__ldg(lut + y0 * w + x0));
   f3 b = from4(__ldg(lut + y0 * w + x1));
   f3 c = from4(__ldg(lut + y1 * w + x0));
@@ -368,14 +401,15 @@ __device__ __forceinline__ Frame make_frame(const DevParams& P, const float4* tl
 }
 
 // _sample_transmittance_unoccluded :609-640
-__device__ __forceinline__ f3 sample_t(const DevParams& P, const Frame& F, float h, float cosv) {
+__device__ __forceinline__ f3 sample_t(const DevParams& P, const Frame& F, float h, float cosv,
+                                       float rho_known = -1.0f) {
   float u, v;
-  t_ray_to_uv(P, mx(h, 0.0f), cosv, F.bottom, F.shell_top, F.inv_shell_top, u, v);
+  t_ray_to_uv(P, mx(h, 0.0f), cosv, F.bottom, F.shell_top, F.inv_shell_top, u, v, rho_known);
   return bilinear(F.tlut, P.t_w, P.t_h, u, v);
 }
 // _sample_multi_scattering :642-683
 __device__ __forceinline__ f3 sample_ms(const DevParams& P, const Frame& F, float h, float sc, float hc) {
-  float af = clampf(h * P.inv_top, 0.0f, 1.0f);
+  float af = __saturatef(h * P.inv_top);
   float u = sun_cosine_to_u(sc, hc);
   float v = fsqrt(af);
   return bilinear(F.mslut, P.ms_w, P.ms_h, u, v);
@@ -386,12 +420,14 @@ __device__ __forceinline__ f3 sample_ms(const DevParams& P, const Frame& F, floa
 struct Horizon {
   float hc;        // horizon cosine
   float sin_hz;    // sine of the horizon zenith
+  float rho;       // shell_rho(h)
 };
 __device__ __forceinline__ Horizon horizon_at(float h, float bottom) {
   Horizon H;
   float radius = bottom + mx(h, 0.0f);
   float inv_r = frcp(mx(radius, 1.0f));
-  H.hc = -shell_rho(h, bottom) * inv_r;
+  H.rho = shell_rho(h, bottom);
+  H.hc = -H.rho * inv_r;
   H.sin_hz = mn(bottom * inv_r, 1.0f);
   return H;
 }
@@ -417,7 +453,7 @@ __device__ __forceinline__ f3 sample_solar_t(const DevParams& P, const Frame& F,
   const float b = H.sin_hz * F.sin_ar;
   if (cs >= a + b) {
     vis = 1.0f;
-    return sample_t(P, F, h, cs);
+    return sample_t(P, F, h, cs, H.rho);
   }
   if (cs <= a - b && H.hc >= -F.cos_ar) {  // hz + ar <= pi
     vis = 0.0f;
@@ -428,7 +464,7 @@ __device__ __forceinline__ f3 sample_solar_t(const DevParams& P, const Frame& F,
   vis = disk_visibility(hz, sz, F.ar);
   const float rz = mn(sz, hz - F.ar * 0.25f);
   const float rc = cosf(mx(rz, 0.0f));
-  return sample_t(P, F, h, rc) * vis;
+  return sample_t(P, F, h, rc, H.rho) * vis;
 }
 // _rayleigh_phase / _mie_phase :791-804
 __device__ __forceinline__ float rayleigh_phase(const DevParams& P, float c) {
@@ -440,35 +476,59 @@ __device__ __forceinline__ float mie_phase(const DevParams& P, float c) {
 }
 // _segment_integral :806-816
 __device__ __forceinline__ void segment_integral(f3 ext, float step, f3& tr, f3& integ) {
-  tr = vexp(-vmin(ext * step, 80.0f));
+  // __expf: ~2 ulp near 0 (as expf), up to ~95 ulp at the clamp (T ~ 1e-35)
+  const f3 x = vmin(ext * step, 80.0f);
+  tr = {__expf(-x.x), __expf(-x.y), __expf(-x.z)};
   integ.x = ext.x > 1.0e-12f ? fdiv(1.0f - tr.x, ext.x) : step;
   integ.y = ext.y > 1.0e-12f ? fdiv(1.0f - tr.y, ext.y) : step;
   integ.z = ext.z > 1.0e-12f ? fdiv(1.0f - tr.z, ext.z) : step;
 }
 
-// One constant-source sample at `dist` along `ray` from the local-axis origin
-// (0, bottom + h0, 0): _scattering_segment :858-899 with
-// _scattering_source :818-856.  `ray_cos_sun` = clamp(ray . sun).
-// Returns the segment (L, T) and the disk visibility at the sample.
+// Per-ray constants of the constant-source samples (everything of
+// _scattering_source :818-856 that does not depend on the sample).
+struct RaySource {
+  float o_y;   // origin (0, o_y, 0), o_y = bottom + h0
+  float h0;    // origin altitude
+  float ray_y;
+  float o_sun; // o_y * sun.y  (origin . sun)
+  float r_sun; // ray . sun
+  f3 ER, EM;   // E * beta_R * phase_R, E * beta_Ms * phase_M
+};
+__device__ __forceinline__ RaySource make_ray_source(const DevParams& P, const Frame& F, float o_y, float h0, f3 ray) {
+  RaySource R;
+  R.o_y = o_y;
+  R.h0 = h0;
+  R.ray_y = ray.y;
+  R.o_sun = o_y * F.sun.y;
+  R.r_sun = dot(ray, F.sun);
+  const float cr = clampf(R.r_sun, -1.0f, 1.0f);
+  R.ER = F.E * arr3(P.beta_r) * rayleigh_phase(P, cr);
+  R.EM = F.E * arr3(P.beta_ms) * mie_phase(P, cr);
+  return R;
+}
+
+// One constant-source segment [start, end] of the ray: _scattering_segment
+// :858-899 with _scattering_source :818-856.  Returns (L, T) and the finite
+// disk visibility at the sample.  The sample's radius is bottom + h (its
+// altitude on the ray) and its sun cosine (o . sun + t ray . sun) / radius;
+// the reference forms the point first - same quantities, rounding differs in
+// the last bits.
 template <bool kMultiple>
-__device__ __forceinline__ Seg source_segment(const DevParams& P, const Frame& F, float o_y, float h0, f3 ray,
-                                              float ray_y, float start, float end, float phase_r, float phase_m,
-                                              float& vis) {
+__device__ __forceinline__ Seg source_segment(const DevParams& P, const Frame& F, const RaySource& R, float start,
+                                              float end, float& vis) {
   float step = mx(end - start, 0.0f);
   float dist = (start + end) * 0.5f;
-  f3 point = mk(ray.x * dist, o_y + ray.y * dist, ray.z * dist);
-  float h = altitude_on_ray(h0, ray_y, dist, F.bottom);
+  float h = altitude_on_ray(R.h0, R.ray_y, dist, F.bottom);
   Density d = density(P, h);
   f3 ext = extinction_of(P, d);
   Seg s;
   f3 integ;
   segment_integral(ext, step, s.T, integ);
-  float radius = fnorm(point);
-  f3 radial = point * frcp(mx(radius, 1.0f));
-  float sc = dot(radial, F.sun);
+  const float radius = F.bottom + h;
+  const float sc = (R.o_sun + dist * R.r_sun) * frcp(mx(radius, 1.0f));
   Horizon H = horizon_at(h, F.bottom);
   f3 st = sample_solar_t(P, F, h, sc, H, vis);
-  f3 src = (F.E * st) * (arr3(P.beta_r) * d.r * phase_r + arr3(P.beta_ms) * d.m * phase_m);
+  f3 src = st * (R.ER * d.r + R.EM * d.m);
   if (kMultiple) src = src + scattering_of(P, d) * sample_ms(P, F, h, sc, H.hc);
   s.L = src * integ;
   return s;

@@ -34,6 +34,21 @@ __device__ __forceinline__ bool tile_pixel(const ImageLayout& L, int& x, int& y)
   return x < L.width && y < L.height;
 }
 
+// Pixel of a thread for memory-bound per-pixel kernels: consecutive threads
+// take consecutive elements along the image's contiguous dimension.
+__device__ __forceinline__ bool linear_pixel(const ImageLayout& L, int& x, int& y) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)L.width * L.height) return false;
+  if (L.sy <= L.sx) {  // y contiguous: the reference's (W, H, 3) layout
+    x = int(i / L.height);
+    y = int(i % L.height);
+  } else {
+    y = int(i / L.width);
+    x = int(i % L.width);
+  }
+  return true;
+}
+
 // _prepare_surface_lighting :1422-1472
 __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayout L, const float* __restrict__ pos,
                                                          const int32_t* __restrict__ sid, float bottom, float cam_alt,
@@ -42,7 +57,7 @@ __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayou
                                                          const float4* __restrict__ mslut, float* __restrict__ out_t,
                                                          float* __restrict__ out_sky) {
   int x, y;
-  if (!tile_pixel(L, x, y)) return;
+  if (!linear_pixel(L, x, y)) return;
   const size_t e = pix_offset(L, x, y);
   const size_t o = e * L.channels;
   Frame F = make_frame(P, tlut, mslut, bottom, ar, sun, splat(0.0f));
@@ -119,28 +134,31 @@ __device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame&
   float sr0, sr1;
   bool sv0, sv1;
   shadow_roots(origin, ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
-  const float cr = clampf(dot(ray, F.sun), -1.0f, 1.0f);
-  const float phase_r = rayleigh_phase(P, cr);
-  const float phase_m = mie_phase(P, cr);
-  const float closest_raw = -(o_y * ray.y);
+  const RaySource rs = make_ray_source(P, F, o_y, cam_alt, ray);
+  const RayWarp rw = make_warp(-(o_y * ray.y), start, end);
+  const bool roots = sv0 || sv1;
   const int n = P.limb_steps;
   const int nsub = P.substeps;
   Seg acc = {splat(0.0f), splat(1.0f)};
-  float d0 = warp_boundary(closest_raw, start, end, 0.0f);
+  float d0 = warp_at(rw, 0.0f);
   for (int i = 0; i < n; ++i) {
-    float d1 = warp_boundary(closest_raw, start, end, float(i + 1) / float(n));
+    float d1 = warp_at(rw, float(i + 1) / float(n));
     float vis;
-    Seg coarse = source_segment<true>(P, F, o_y, cam_alt, ray, ray.y, d0, d1, phase_r, phase_m, vis);
+    Seg coarse = source_segment<true>(P, F, rs, d0, d1, vis);
     ++samples;
-    // _terminator_refinement_weight :901-966
-    float mid = (d0 + d1) * 0.5f;
-    float iw = mx(d1 - d0, 1.0e-4f);
-    float closest_root = 1.0e30f;
-    if (sv0) closest_root = mn(closest_root, fabsf(mid - sr0));
-    if (sv1) closest_root = mn(closest_root, fabsf(mid - sr1));
-    float prox = clampf(2.0f - closest_root / iw, 0.0f, 1.0f);
-    prox = prox * prox * (3.0f - 2.0f * prox);
-    float w = mx(prox, 4.0f * vis * (1.0f - vis));
+    // _terminator_refinement_weight :901-966; zero unless a shadow-cylinder
+    // root exists or the disk is partly hidden at the midpoint
+    float w = 0.0f;
+    if (roots || (vis > 0.0f && vis < 1.0f)) {
+      float mid = (d0 + d1) * 0.5f;
+      float iw = mx(d1 - d0, 1.0e-4f);
+      float closest_root = 1.0e30f;
+      if (sv0) closest_root = mn(closest_root, fabsf(mid - sr0));
+      if (sv1) closest_root = mn(closest_root, fabsf(mid - sr1));
+      float prox = __saturatef(2.0f - fdiv(closest_root, iw));
+      prox = prox * prox * (3.0f - 2.0f * prox);
+      w = mx(prox, 4.0f * vis * (1.0f - vis));
+    }
     Seg interval = coarse;
     if (w > 0.0f) {
       // _integrate_adaptive_scattering_interval :998-1031
@@ -149,7 +167,7 @@ __device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame&
       for (int k = 0; k < nsub; ++k) {
         float c1 = d0 + (d1 - d0) * (float(k + 1) / float(nsub));
         float cvis;
-        fine = seg_then(fine, source_segment<true>(P, F, o_y, cam_alt, ray, ray.y, c0, c1, phase_r, phase_m, cvis));
+        fine = seg_then(fine, source_segment<true>(P, F, rs, c0, c1, cvis));
         c0 = c1;
       }
       samples += nsub;
@@ -382,7 +400,8 @@ cudaError_t launch_prepare_surface(const DevParams& P, const ImageLayout& L, con
                                    float bottom, float cam_alt, const float sun[3], float ar, const float right[3],
                                    const float up[3], const float fwd[3], const float4* tlut, const float4* mslut,
                                    float* out_sun_t, float* out_sky, cudaStream_t s) {
-  k_prepare_surface<<<tile_grid(L), 256, 0, s>>>(P, L, pos, sid, bottom, cam_alt, host3(sun), ar, host3(right),
+  const unsigned blocks = unsigned((static_cast<long long>(L.width) * L.height + 255) / 256);
+  k_prepare_surface<<<blocks, 256, 0, s>>>(P, L, pos, sid, bottom, cam_alt, host3(sun), ar, host3(right),
                                                  host3(up), host3(fwd), tlut, mslut, out_sun_t, out_sky);
   return cudaGetLastError();
 }

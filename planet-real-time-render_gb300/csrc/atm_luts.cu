@@ -21,44 +21,10 @@
 
 #include "atm_device.cuh"
 #include "atm_kernels.h"
+#include "atm_lut_warp.cuh"
 
 namespace atm {
 namespace {
-
-constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ f3 shfl_xor3(f3 v, int m) {
-  return {__shfl_xor_sync(kFull, v.x, m), __shfl_xor_sync(kFull, v.y, m), __shfl_xor_sync(kFull, v.z, m)};
-}
-__device__ __forceinline__ Seg shfl_down_seg(Seg s, int o) {
-  return {{__shfl_down_sync(kFull, s.L.x, o), __shfl_down_sync(kFull, s.L.y, o), __shfl_down_sync(kFull, s.L.z, o)},
-          {__shfl_down_sync(kFull, s.T.x, o), __shfl_down_sync(kFull, s.T.y, o), __shfl_down_sync(kFull, s.T.z, o)}};
-}
-__device__ __forceinline__ Seg shfl_up_seg(Seg s, int o) {
-  return {{__shfl_up_sync(kFull, s.L.x, o), __shfl_up_sync(kFull, s.L.y, o), __shfl_up_sync(kFull, s.L.z, o)},
-          {__shfl_up_sync(kFull, s.T.x, o), __shfl_up_sync(kFull, s.T.y, o), __shfl_up_sync(kFull, s.T.z, o)}};
-}
-__device__ __forceinline__ Seg seg_identity() { return {splat(0.0f), splat(1.0f)}; }
-
-// Ordered reduction of 32 consecutive segments; lane 0 receives the total.
-__device__ __forceinline__ Seg warp_compose(Seg s) {
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    Seg other = shfl_down_seg(s, o);
-    if ((threadIdx.x & 31) + o < 32) s = seg_then(s, other);
-  }
-  return s;
-}
-// Ordered inclusive scan: lane i receives segment 0 then ... then i.
-__device__ __forceinline__ Seg warp_scan(Seg s) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    Seg before = shfl_up_seg(s, o);
-    if (lane >= o) s = seg_then(before, s);
-  }
-  return s;
-}
 
 // ---- transmittance (:1034-1063, :570-607) ----------------------------------
 constexpr int kTLanes = 8;
@@ -184,83 +150,17 @@ __global__ void __launch_bounds__(kMaxDirs) k_multi_scattering(DevParams P, floa
   }
 }
 
-// ---- sky-view (:1208-1302) ----------------------------------------------------
+// ---- sky-view (:1208-1302) and aerial perspective (:1304-1420) -----------------
 __global__ void __launch_bounds__(256) k_sky_view(DevParams P, float bottom, float cam_alt, float sun_cos, f3 E,
                                                   float ar, const float4* __restrict__ tlut,
                                                   const float4* __restrict__ mslut, float4* __restrict__ out,
                                                   unsigned long long* counter) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  const int n_texels = P.sv_w * P.sv_h;
-  if (warp_id >= n_texels) return;  // warp-uniform
-  const int x = warp_id % P.sv_w, y = warp_id / P.sv_w;
+  if (warp_id >= P.sv_w * P.sv_h) return;  // warp-uniform
   float ss = sqrtf(mx(1.0f - sun_cos * sun_cos, 0.0f));
   Frame F = make_frame(P, tlut, mslut, bottom, ar, mk(ss, sun_cos, 0.0f), E);
-  float sh = mx(cam_alt, 0.0f);
-  float o_y = bottom + sh;
-  float az = (float(x) + 0.5f) / float(P.sv_w) * kPiF;
-  float vv = (float(y) + 0.5f) / float(P.sv_h);
-  float zen = sky_v_to_zenith(vv, sky_horizon_zenith(sh, bottom));
-  float vs, vc, saz, caz;
-  sincosf(zen, &vs, &vc);
-  sincosf(az, &saz, &caz);
-  f3 ray = mk(vs * caz, vc, vs * saz);
-  float start, end;
-  bool valid, ground;
-  segment_from_altitude(P, sh, vc, bottom, start, end, valid, ground);
-  Seg acc = seg_identity();
-  uint32_t samples = 0;
-  if (valid) {
-    const float cr = clampf(dot(ray, F.sun), -1.0f, 1.0f);
-    const float phase_r = rayleigh_phase(P, cr);
-    const float phase_m = mie_phase(P, cr);
-    const float closest_raw = -(o_y * ray.y);
-    const int n = P.sv_steps;
-    const int per = (n + 31) >> 5;
-    const int i0 = lane * per;
-    const int i1 = min(i0 + per, n);
-    if (i0 < i1) {
-      float d0 = warp_boundary(closest_raw, start, end, float(i0) / float(n));
-      for (int i = i0; i < i1; ++i) {
-        float d1 = warp_boundary(closest_raw, start, end, float(i + 1) / float(n));
-        float vis;
-        Seg s = source_segment<true>(P, F, o_y, sh, ray, vc, d0, d1, phase_r, phase_m, vis);
-        acc = seg_then(acc, s);
-        d0 = d1;
-      }
-      samples = uint32_t(i1 - i0);
-    }
-  }
+  uint32_t samples = sky_view_texel(P, F, cam_alt, warp_id % P.sv_w, warp_id / P.sv_w, out);
   warp_count(samples, counter);
-  acc = warp_compose(acc);
-  if (lane == 0) out[y * P.sv_w + x] = to4(vmax(acc.L, 0.0f));
-}
-
-// ---- aerial perspective (:1304-1420) --------------------------------------------
-// Segment of depth slice k along a column's prefix interval [as, ae].
-__device__ __forceinline__ Seg aerial_slice(const DevParams& P, const Frame& F, float o_y, float cam_alt, f3 ray,
-                                            float as, float ae, bool valid, int k, float phase_r, float phase_m,
-                                            float closest_raw, uint32_t& samples) {
-  Seg acc = seg_identity();
-  const float denom = float(P.ap_d - 1);
-  float prev = k == 0 ? as : as + (ae - as) * (float(k - 1) / denom);
-  float target = as + (ae - as) * (float(k) / denom);
-  if (valid) {
-    float is = mx(prev, as);
-    float ie = mn(target, ae);
-    if (ie > is) {
-      const int n = P.ap_steps;
-      float d0 = warp_boundary(closest_raw, is, ie, 0.0f);
-      for (int s = 0; s < n; ++s) {
-        float d1 = warp_boundary(closest_raw, is, ie, float(s + 1) / float(n));
-        float vis;
-        acc = seg_then(acc, source_segment<true>(P, F, o_y, cam_alt, ray, ray.y, d0, d1, phase_r, phase_m, vis));
-        d0 = d1;
-      }
-      samples += uint32_t(n);
-    }
-  }
-  return acc;
 }
 
 __global__ void __launch_bounds__(256) k_aerial(DevParams P, float aspect, float bottom, float cam_alt, f3 sun, f3 E,
@@ -268,50 +168,11 @@ __global__ void __launch_bounds__(256) k_aerial(DevParams P, float aspect, float
                                                 const float4* __restrict__ tlut, const float4* __restrict__ mslut,
                                                 float4* __restrict__ out, unsigned long long* counter) {
   const int warp_id = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
   if (warp_id >= P.ap_w * P.ap_h) return;  // warp-uniform
-  const int x = warp_id % P.ap_w, y = warp_id / P.ap_w;
   Frame F = make_frame(P, tlut, mslut, bottom, ar, sun, E);
-  const float o_y = bottom + cam_alt;
-  float u = (float(x) + 0.5f) / float(P.ap_w);
-  float v = (float(y) + 0.5f) / float(P.ap_h);
-  float sx = (u * 2.0f - 1.0f) * aspect;
-  float sy = v * 2.0f - 1.0f;
-  f3 rv = (right * sx + up * sy) + fwd / tanfov;
-  f3 ray = rv * (1.0f / norm(rv));
-  float as, ae;
-  bool valid;
-  aerial_prefix(P, cam_alt, ray.y, bottom, as, ae, valid);
-  const float cr = clampf(dot(ray, sun), -1.0f, 1.0f);
-  const float phase_r = rayleigh_phase(P, cr);
-  const float phase_m = mie_phase(P, cr);
-  const float closest_raw = -(o_y * ray.y);
-  const int depth = P.ap_d;
-  const int per = (depth + 31) >> 5;
-  const size_t plane = size_t(P.ap_w) * P.ap_h;
-  // pass 1: each lane composes its own run of slices
-  Seg run = seg_identity();
-  uint32_t samples = 0;
-  for (int k = lane * per; k < min(lane * per + per, depth); ++k)
-    run = seg_then(run,
-                   aerial_slice(P, F, o_y, cam_alt, ray, as, ae, valid, k, phase_r, phase_m, closest_raw, samples));
+  AerialView V{aspect, cam_alt, right, up, fwd, tanfov};
+  uint32_t samples = aerial_column(P, F, V, warp_id % P.ap_w, warp_id / P.ap_w, out);
   warp_count(samples, counter);
-  // exclusive prefix of the runs
-  Seg incl = warp_scan(run);
-  Seg prefix = shfl_up_seg(incl, 1);
-  if (lane == 0) prefix = seg_identity();
-  if (per == 1) {
-    if (lane < depth) out[size_t(lane) * plane + size_t(y) * P.ap_w + x] = to4(vmax(incl.L, 0.0f));
-    return;
-  }
-  // pass 2 (depth > 32): walk the run again writing cumulative values
-  Seg acc = prefix;
-  uint32_t recomputed = 0;  // second evaluation of the same samples: not counted
-  for (int k = lane * per; k < min(lane * per + per, depth); ++k) {
-    acc = seg_then(acc,
-                   aerial_slice(P, F, o_y, cam_alt, ray, as, ae, valid, k, phase_r, phase_m, closest_raw, recomputed));
-    out[size_t(k) * plane + size_t(y) * P.ap_w + x] = to4(vmax(acc.L, 0.0f));
-  }
 }
 
 __global__ void k_lut_to_fields(const float4* __restrict__ lut, int w, int h, int d, float* __restrict__ dst) {

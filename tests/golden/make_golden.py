@@ -208,6 +208,49 @@ def _sample_pixels(width, height, rng, n_random, column_stride):
     return sorted(pts)
 
 
+def model_reference(reference: Path) -> dict:
+    """Outputs of the reference's FP64 validation model (atmosphere/model.py):
+    shell intervals, transmittance and direct single scattering for seeded
+    rays on the Earth set and on the small planet of its own tests."""
+
+    _import_reference(reference)
+    from planet_renderer.atmosphere import AtmosphereConfig, AtmosphereModel  # type: ignore
+
+    rng = np.random.default_rng(77)
+    out = {}
+    sets = {
+        "earth": (6_360_000.0, AtmosphereConfig()),
+        "small": (50_000.0, AtmosphereConfig(top_altitude_m=15_000.0, rayleigh_scale_height_m=3_000.0,
+                                             mie_scale_height_m=800.0, absorption_peak_altitude_m=7_500.0,
+                                             absorption_half_width_m=5_000.0)),
+    }
+    for tag, (radius, cfg) in sets.items():
+        model = AtmosphereModel(radius, cfg)
+        n = 24
+        alt = np.concatenate([[1.0, 10.0, 2000.0], rng.uniform(0.0, 1.5 * cfg.top_altitude_m, n - 3)])
+        origins = np.stack([np.zeros(n), radius + alt, np.zeros(n)], axis=1)
+        dirs = rng.normal(size=(n, 3))
+        dirs[:, 1] = np.where(np.arange(n) % 3 == 0, -np.abs(dirs[:, 1]) * 0.05, dirs[:, 1])
+        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        suns = rng.normal(size=(n, 3))
+        suns /= np.linalg.norm(suns, axis=1, keepdims=True)
+        trans, single, starts, ends, ground = [], [], [], [], []
+        for o, d, s in zip(origins, dirs, suns):
+            iv = model.atmosphere_interval(o, d)
+            starts.append(np.nan if iv is None else iv.start_m)
+            ends.append(np.nan if iv is None else iv.end_m)
+            ground.append(False if iv is None else iv.ends_at_ground)
+            trans.append(model.transmittance(o, d, steps=96, ground_is_opaque=True))
+            single.append(model.single_scattering(o, d, s, (4.0, 3.9, 3.7), steps=10, sun_steps=10))
+        out.update({f"{tag}_origins": origins, f"{tag}_dirs": dirs, f"{tag}_suns": suns,
+                    f"{tag}_transmittance": np.array(trans), f"{tag}_single": np.array(single),
+                    f"{tag}_start": np.array(starts), f"{tag}_end": np.array(ends),
+                    f"{tag}_ground": np.array(ground)})
+    out["meta"] = np.array(json.dumps({"name": "model_reference", "radii": {"earth": 6_360_000.0, "small": 50_000.0},
+                                       "generator": "reference atmosphere/model.py"}))
+    return out
+
+
 def earth_config1_kwargs():
     return dict(
         mie_extinction_per_m=(3.996e-6 + 4.4e-6,) * 3,
@@ -248,6 +291,8 @@ def main() -> None:
         out, _ = run_scenario("tiny_orbit", args.reference, dict(TINY_LUTS, aerial_horizon_raymarch_steps=16),
                               6_360_000.0, 2_000_000.0, 95.0, 60.0, 0.0, -35.0, 24, 16, seed=7)
         np.savez_compressed(HERE / f"tiny_orbit{suffix}.npz", **out)
+    if want("model_reference") and args.precision == "f32":
+        np.savez_compressed(HERE / "model_reference.npz", **model_reference(args.reference))
     renderer = None
     if args.precision == "f64":
         return
