@@ -407,6 +407,7 @@ def main() -> None:
                         help="reference arm: pixel stride of each step's bounded sample")
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-4k", action="store_true")
+    parser.add_argument("--no-batch", action="store_true")
     args = parser.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -472,6 +473,7 @@ def main() -> None:
     frame_4k = None
     if not args.no_4k:
         frame_4k = _frame_4k(device, args)
+    batch = None if args.no_batch else _batch(device, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -493,6 +495,7 @@ def main() -> None:
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": _config_block(),
             "frame_ms_1080p": ms_per_step / 3.0,
             "frame_ms_4k": frame_4k,
+            "batch": batch,
             "samples_per_step": samples_per_step,
             "e2e": {"value": world * e2e_samples / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / e2e_steps,
@@ -523,6 +526,54 @@ def _composite_args(v, light):
 
     return (EARTH_RADIUS_M, v.camera_radius_m, v.sun_local, SOLAR_IRRADIANCE, light.sun_disk_radiance,
             SUN_ANGULAR_RADIUS_DEG, v.basis, v.tangent_half_fov, 4.0, 12.0)
+
+
+def _batch(device, args) -> dict:
+    """Batched LUT builds: 256 snapshots x 16 cameras x 2 parameter sets, a
+    sky-view LUT and an aerial volume each (16,384 LUTs of uneven sizes) in
+    one persistent launch per step, tiles from the autotuner."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere import autotune
+    from planet_renderer_gb300.atmosphere.batch import SKY_VIEW, BatchedLutBuilder
+    from planet_renderer_gb300.atmosphere.workloads import batched_lut_jobs, batched_lut_sets
+
+    sets = batched_lut_sets()
+    jobs = batched_lut_jobs(SEED)
+    builder = BatchedLutBuilder(sets, device=device)
+    tuning, report = autotune.tune(builder, jobs)
+    prepared = builder.prepare(jobs)
+    arena = torch.empty((prepared[1], 4), dtype=torch.float32, device=device)
+    for _ in range(2):
+        builder.build(jobs, tuning, arena=arena, prepared=prepared)
+    torch.cuda.synchronize(device)
+    builder.samples(reset=True)
+    steps = max(args.steps // 10, 3)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        builder.build(jobs, tuning, arena=arena, prepared=prepared)
+    end.record()
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    samples = builder.samples(reset=True) / steps
+    sky_keys = {j.sky_key() for j in jobs if j.kind == SKY_VIEW}
+    n_sky = sum(1 for j in jobs if j.kind == SKY_VIEW)
+    out = {
+        "workload": "256 snapshots (sun zenith 0-110 deg) x 16 cameras (1 m - 4000 km) x 2 parameter sets "
+                    "(Earth, 50 km planet); sky-view 96x54..384x216 and aerial 16^3..64^3 per (snapshot, camera, "
+                    "set); one persistent launch",
+        "luts": len(jobs), "ms_per_batch": ms, "luts_per_s": len(jobs) / (ms / 1e3),
+        "samples_per_batch": samples, "samples_per_s": samples / (ms / 1e3),
+        "sky_view_luts_raw": n_sky, "sky_view_luts_deduped": len(sky_keys),
+        "arena_gb": prepared[1] * 16 / 1e9,
+        "tuning": tuning.__dict__, "tuning_cached": report.get("cached", False), "steps": steps,
+    }
+    del arena
+    builder.close()
+    torch.cuda.empty_cache()
+    return out
 
 
 def _frame_4k(device, args) -> dict:

@@ -201,6 +201,58 @@ int atm_load_lut(AtmHandle* handle, int32_t kind, const float* src_device, void*
  * reset.  Synchronises `stream`. */
 int atm_read_sample_counter(AtmHandle* handle, int32_t reset, uint64_t* out, void* stream);
 
+/* ---- batched LUT builds --------------------------------------------------
+ * Many sky-view and aerial-perspective LUTs (time snapshots x cameras x
+ * parameter sets, each with its own LUT size) built by one persistent
+ * launch.  The reference builds one LUT per kernel launch
+ * (renderer.py:1208 _build_sky_view, :1304 _build_aerial_perspective), each
+ * job here computes exactly what one such launch computes. */
+typedef struct AtmBatchJob {
+  int32_t kind;            /* ATM_LUT_SKY_VIEW or ATM_LUT_AERIAL                   */
+  int32_t param_set;       /* index into the sets given to atm_batch_create       */
+  int32_t width;           /* LUT width  (sky-view 16..2048, aerial 4..256)       */
+  int32_t height;          /* LUT height (sky-view 16..2048, aerial 4..256)       */
+  int32_t depth;           /* aerial depth 8..256; 1 for sky-view                 */
+  int32_t frame_width;     /* aerial: frame aspect = frame_width / frame_height   */
+  int32_t frame_height;
+  int32_t reserved;
+  int64_t output_offset;   /* first float4 texel of this LUT in the output arena  */
+  double camera_altitude_m;
+  double sun_zenith_cosine; /* sky-view: f32-rounded key, as atm_update passes it */
+  double sun_local[3];      /* aerial                                            */
+  double view_basis[9];     /* aerial: right, up, forward                         */
+  double tangent_half_fov;  /* aerial                                            */
+} AtmBatchJob;
+
+/* Work split of a batch launch (chosen by the Python autotuner). */
+typedef struct AtmBatchTuning {
+  int32_t sky_view_texels_per_item; /* 1..4096 */
+  int32_t aerial_columns_per_item;  /* 1..4096 */
+  int32_t blocks_per_sm;            /* 1..8 resident 256-thread blocks */
+} AtmBatchTuning;
+
+typedef struct AtmBatch AtmBatch;
+
+/* Parameter sets of a batch with their planet radii; builds each set's
+ * transmittance and multi-scattering LUTs (irradiance and sun size are
+ * shared by all jobs, as the reference keys them). */
+int atm_batch_create(const AtmParams* sets, const double* planet_radius_m, int32_t n_sets,
+                     const double solar_irradiance[3], double sun_angular_radius_degrees, AtmBatch** out,
+                     void* stream);
+int atm_batch_destroy(AtmBatch* batch);
+/* Build n_jobs LUTs into `arena` (device, arena_texels float4 texels; each
+ * LUT row-major [z][y][x] at its output_offset) in one persistent launch.
+ * The job table is uploaded to device memory owned by the batch (grown on
+ * demand: the only allocations of this call). */
+int atm_batch_build(AtmBatch* batch, const AtmBatchJob* jobs, int32_t n_jobs, void* arena, int64_t arena_texels,
+                    const AtmBatchTuning* tuning, void* stream);
+/* Radiance samples evaluated by batch builds since the last reset
+ * (synchronises `stream`). */
+int atm_batch_read_samples(AtmBatch* batch, int32_t reset, uint64_t* out, void* stream);
+/* Device storage (float4 [y][x]) of a set's transmittance (kind 0) or
+ * multi-scattering (kind 1) LUT. */
+int atm_batch_static_lut(const AtmBatch* batch, int32_t param_set, int32_t kind, void** device_ptr);
+
 /* COMPOSITE view of atm_composite that allocates nothing.  No counterpart in
  * the reference.  For callers that may not call cudaMalloc: an engine or
  * plugin host that owns every device allocation through its own pool, a

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "atm_capi.h"
 #include "atm_kernels.h"
@@ -498,6 +499,181 @@ ATM_API int atm_read_sample_counter(AtmHandle* h, int32_t reset, uint64_t* out, 
   if (reset) ATM_CUDA(cudaMemsetAsync(h->samples, 0, sizeof(v), s), "sample counter reset");
   ATM_CUDA(cudaStreamSynchronize(s), "sample counter sync");
   if (out) *out = v;
+  return ATM_OK;
+}
+
+// ---- batched builds ------------------------------------------------------
+struct AtmBatch {
+  std::vector<AtmParams> params;
+  std::vector<atm::DevParams> dev;
+  std::vector<double> radius;
+  std::vector<float4*> tlut, mslut;
+  double E[3] = {0, 0, 0};
+  double ar_rad = 0.0;
+  unsigned char* d_jobs = nullptr;
+  size_t jobs_bytes = 0;
+  long long* d_prefix = nullptr;
+  size_t prefix_count = 0;
+  unsigned long long* d_ticket = nullptr;
+  unsigned long long* d_samples = nullptr;
+  std::vector<unsigned char> h_jobs;
+  std::vector<long long> h_prefix;
+  int sm_count = 0;
+};
+
+ATM_API int atm_batch_destroy(AtmBatch* b) {
+  if (b == nullptr) return ATM_OK;
+  for (float4* p : b->tlut) if (p) cudaFree(p);
+  for (float4* p : b->mslut) if (p) cudaFree(p);
+  if (b->d_jobs) cudaFree(b->d_jobs);
+  if (b->d_prefix) cudaFree(b->d_prefix);
+  if (b->d_ticket) cudaFree(b->d_ticket);
+  if (b->d_samples) cudaFree(b->d_samples);
+  delete b;
+  return ATM_OK;
+}
+
+ATM_API int atm_batch_create(const AtmParams* sets, const double* planet_radius_m, int32_t n_sets,
+                             const double solar_irradiance[3], double sun_angular_radius_degrees, AtmBatch** out,
+                             void* stream) {
+  if (!sets || !planet_radius_m || !solar_irradiance || !out || n_sets < 1 || n_sets > 1024)
+    return fail(ATM_E_INVALID, "atm_batch_create needs 1..1024 parameter sets, radii, irradiance and an output");
+  *out = nullptr;
+  if (!finite_nonneg3(solar_irradiance) || !std::isfinite(sun_angular_radius_degrees))
+    return fail(ATM_E_INVALID, "invalid irradiance or sun angular radius");
+  for (int i = 0; i < n_sets; ++i) {
+    int rc = validate(sets[i]);
+    if (rc) return rc;
+    if (!std::isfinite(planet_radius_m[i]) || planet_radius_m[i] <= 1.0)
+      return fail(ATM_E_INVALID, "planet radius of set %d must be > 1 m", i);
+  }
+  AtmBatch* b = new (std::nothrow) AtmBatch();
+  if (!b) return fail(ATM_E_NOMEM, "host allocation failed");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::memcpy(b->E, solar_irradiance, sizeof(b->E));
+  b->ar_rad = double(radians_f32(sun_angular_radius_degrees));
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_ticket, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_samples, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->d_samples, 0, sizeof(unsigned long long), s);
+  for (int i = 0; i < n_sets && e == cudaSuccess; ++i) {
+    b->params.push_back(sets[i]);
+    b->dev.push_back(atm::make_dev_params(sets[i]));
+    b->radius.push_back(planet_radius_m[i]);
+    float4 *t = nullptr, *m = nullptr;
+    e = cudaMalloc(&t, sizeof(float4) * sets[i].transmittance_lut_width * sets[i].transmittance_lut_height);
+    if (e == cudaSuccess)
+      e = cudaMalloc(&m, sizeof(float4) * sets[i].multi_scattering_lut_width * sets[i].multi_scattering_lut_height);
+    b->tlut.push_back(t);
+    b->mslut.push_back(m);
+    if (e != cudaSuccess) break;
+    float ef[3];
+    to_f32(solar_irradiance, ef, 3);
+    e = atm::launch_transmittance(b->dev[i], float(planet_radius_m[i]), t, s);
+    if (e == cudaSuccess)
+      e = atm::launch_multi_scattering(b->dev[i], float(planet_radius_m[i]), ef, float(b->ar_rad), t, m, b->d_samples,
+                                       s);
+  }
+  if (e != cudaSuccess) {
+    atm_batch_destroy(b);
+    return cuda_fail(e, "batch set-up");
+  }
+  *out = b;
+  return ATM_OK;
+}
+
+ATM_API int atm_batch_build(AtmBatch* b, const AtmBatchJob* jobs, int32_t n_jobs, void* arena, int64_t arena_texels,
+                            const AtmBatchTuning* tuning, void* stream) {
+  if (!b || !jobs || !arena || !tuning || n_jobs < 1) return fail(ATM_E_INVALID, "null argument to atm_batch_build");
+  const int sv_item = tuning->sky_view_texels_per_item, ap_item = tuning->aerial_columns_per_item;
+  if (sv_item < 1 || sv_item > 4096 || ap_item < 1 || ap_item > 4096 || tuning->blocks_per_sm < 1 ||
+      tuning->blocks_per_sm > 8)
+    return fail(ATM_E_INVALID, "tuning out of range");
+  const size_t jsz = atm::batch_job_size();
+  b->h_jobs.assign(size_t(n_jobs) * jsz, 0);
+  b->h_prefix.assign(size_t(n_jobs) + 1, 0);
+  float4* base = static_cast<float4*>(arena);
+  for (int i = 0; i < n_jobs; ++i) {
+    const AtmBatchJob& j = jobs[i];
+    if (j.param_set < 0 || j.param_set >= int(b->params.size()))
+      return fail(ATM_E_INVALID, "job %d: parameter set %d out of range", i, j.param_set);
+    long long texels = 0;
+    int units = 0, per = 0;
+    if (j.kind == ATM_LUT_SKY_VIEW) {
+      if (j.width < 16 || j.width > 2048 || j.height < 16 || j.height > 2048)
+        return fail(ATM_E_INVALID, "job %d: sky-view size %dx%d outside 16..2048", i, j.width, j.height);
+      texels = (long long)j.width * j.height;
+      units = j.width * j.height;
+      per = sv_item;
+    } else if (j.kind == ATM_LUT_AERIAL) {
+      if (j.width < 4 || j.width > 256 || j.height < 4 || j.height > 256 || j.depth < 8 || j.depth > 256)
+        return fail(ATM_E_INVALID, "job %d: aerial size %dx%dx%d outside 4..256 x 4..256 x 8..256", i, j.width,
+                    j.height, j.depth);
+      if (j.frame_width < 1 || j.frame_height < 1 || !(j.tangent_half_fov > 0.0) ||
+          !finite_n(j.view_basis, 9) || !finite_n(j.sun_local, 3))
+        return fail(ATM_E_INVALID, "job %d: invalid aerial camera", i);
+      texels = (long long)j.width * j.height * j.depth;
+      units = j.width * j.height;
+      per = ap_item;
+    } else {
+      return fail(ATM_E_INVALID, "job %d: kind %d is not sky-view or aerial", i, j.kind);
+    }
+    if (j.output_offset < 0 || j.output_offset + texels > arena_texels)
+      return fail(ATM_E_INVALID, "job %d: output [%lld, %lld) outside the arena of %lld texels", i,
+                  (long long)j.output_offset, (long long)(j.output_offset + texels), (long long)arena_texels);
+    if (!std::isfinite(j.camera_altitude_m) || !std::isfinite(j.sun_zenith_cosine))
+      return fail(ATM_E_INVALID, "job %d: non-finite camera or sun", i);
+    const int p = j.param_set;
+    atm::fill_batch_job(*reinterpret_cast<atm::BatchJobDev*>(b->h_jobs.data() + size_t(i) * jsz), b->dev[p], j,
+                        base, b->tlut[p], b->mslut[p], b->radius[p], b->E, b->ar_rad, per);
+    b->h_prefix[i + 1] = b->h_prefix[i] + (units + per - 1) / per;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (b->jobs_bytes < b->h_jobs.size()) {
+    if (b->d_jobs) cudaFree(b->d_jobs);
+    b->d_jobs = nullptr;
+    b->jobs_bytes = 0;
+    ATM_CUDA(cudaMalloc(&b->d_jobs, b->h_jobs.size()), "batch job table");
+    b->jobs_bytes = b->h_jobs.size();
+  }
+  if (b->prefix_count < b->h_prefix.size()) {
+    if (b->d_prefix) cudaFree(b->d_prefix);
+    b->d_prefix = nullptr;
+    b->prefix_count = 0;
+    ATM_CUDA(cudaMalloc(&b->d_prefix, b->h_prefix.size() * sizeof(long long)), "batch item prefix");
+    b->prefix_count = b->h_prefix.size();
+  }
+  ATM_CUDA(cudaMemcpyAsync(b->d_jobs, b->h_jobs.data(), b->h_jobs.size(), cudaMemcpyHostToDevice, s), "job upload");
+  ATM_CUDA(cudaMemcpyAsync(b->d_prefix, b->h_prefix.data(), b->h_prefix.size() * sizeof(long long),
+                           cudaMemcpyHostToDevice, s),
+           "prefix upload");
+  // the host tables are re-filled by the next call: make sure this one's copies are done
+  ATM_CUDA(cudaStreamSynchronize(s), "job upload sync");
+  ATM_CUDA(atm::launch_batch(reinterpret_cast<const atm::BatchJobDev*>(b->d_jobs), b->d_prefix, n_jobs,
+                             b->h_prefix[n_jobs], b->d_ticket, b->d_samples, b->sm_count * tuning->blocks_per_sm, s),
+           "batch launch");
+  return ATM_OK;
+}
+
+ATM_API int atm_batch_read_samples(AtmBatch* b, int32_t reset, uint64_t* out, void* stream) {
+  if (!b) return fail(ATM_E_INVALID, "null AtmBatch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  unsigned long long v = 0;
+  ATM_CUDA(cudaMemcpyAsync(&v, b->d_samples, sizeof(v), cudaMemcpyDeviceToHost, s), "batch samples read");
+  if (reset) ATM_CUDA(cudaMemsetAsync(b->d_samples, 0, sizeof(v), s), "batch samples reset");
+  ATM_CUDA(cudaStreamSynchronize(s), "batch samples sync");
+  if (out) *out = v;
+  return ATM_OK;
+}
+
+ATM_API int atm_batch_static_lut(const AtmBatch* b, int32_t param_set, int32_t kind, void** device_ptr) {
+  if (!b || !device_ptr) return fail(ATM_E_INVALID, "null argument");
+  if (param_set < 0 || param_set >= int(b->params.size())) return fail(ATM_E_INVALID, "set out of range");
+  if (kind == ATM_LUT_TRANSMITTANCE) *device_ptr = b->tlut[param_set];
+  else if (kind == ATM_LUT_MULTI_SCATTERING) *device_ptr = b->mslut[param_set];
+  else return fail(ATM_E_INVALID, "kind must be transmittance (0) or multi-scattering (1)");
   return ATM_OK;
 }
 

@@ -51,6 +51,15 @@ cudaError_t launch_lut_to_fields(const float4* lut, int w, int h, int d, float* 
 // Taichi field layout (W, H[, D], 3) floats -> LUT (float4 [z][y][x]).
 cudaError_t launch_fields_to_lut(const float* src, int w, int h, int d, float4* lut, cudaStream_t s);
 
+// Batched builds (atm_batch.cu): opaque device job descriptors.
+struct BatchJobDev;
+size_t batch_job_size();
+void fill_batch_job(BatchJobDev& d, const DevParams& set_params, const AtmBatchJob& j, float4* arena,
+                    const float4* tlut, const float4* mslut, double radius, const double E[3], double ar_rad,
+                    int per_item);
+cudaError_t launch_batch(const BatchJobDev* jobs, const long long* prefix, int n_jobs, long long n_items,
+                         unsigned long long* ticket, unsigned long long* samples, int blocks, cudaStream_t s);
+
 // atm_composite_noalloc: the per-device address of the file-scope tile
 // scratch (looked up on the first call on each device), its capacity in
 // 16x16 tiles, and the COMPOSITE-view launch that uses it.

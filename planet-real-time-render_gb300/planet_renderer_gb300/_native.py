@@ -114,6 +114,33 @@ class AtmBuildArgs(ctypes.Structure):
     ]
 
 
+class AtmBatchJob(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32),
+        ("param_set", ctypes.c_int32),
+        ("width", ctypes.c_int32),
+        ("height", ctypes.c_int32),
+        ("depth", ctypes.c_int32),
+        ("frame_width", ctypes.c_int32),
+        ("frame_height", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+        ("output_offset", ctypes.c_int64),
+        ("camera_altitude_m", ctypes.c_double),
+        ("sun_zenith_cosine", ctypes.c_double),
+        ("sun_local", c_double3),
+        ("view_basis", c_double9),
+        ("tangent_half_fov", ctypes.c_double),
+    ]
+
+
+class AtmBatchTuning(ctypes.Structure):
+    _fields_ = [
+        ("sky_view_texels_per_item", ctypes.c_int32),
+        ("aerial_columns_per_item", ctypes.c_int32),
+        ("blocks_per_sm", ctypes.c_int32),
+    ]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _D = ctypes.c_double
@@ -140,6 +167,17 @@ SIGNATURES = {
     "atm_read_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_load_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_read_sample_counter": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
+    "atm_batch_create": (
+        ctypes.c_int,
+        [ctypes.POINTER(AtmParams), ctypes.POINTER(ctypes.c_double), _I32, c_double3, _D, ctypes.POINTER(_P), _P],
+    ),
+    "atm_batch_destroy": (ctypes.c_int, [_P]),
+    "atm_batch_build": (
+        ctypes.c_int,
+        [_P, ctypes.POINTER(AtmBatchJob), _I32, _P, ctypes.c_int64, ctypes.POINTER(AtmBatchTuning), _P],
+    ),
+    "atm_batch_read_samples": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
+    "atm_batch_static_lut": (ctypes.c_int, [_P, _I32, _I32, ctypes.POINTER(_P)]),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,

@@ -59,3 +59,51 @@ def frame_chain_cameras(seed: int = 2027) -> list[CameraView]:
         azimuth = float(rng.uniform(0.0, 360.0))
         views.append(CameraView(altitude, zenith, azimuth))
     return views
+
+
+# ---- batched LUT builds ----------------------------------------------------
+SKY_VIEW_SIZES = ((96, 54), (128, 72), (192, 108), (256, 144), (384, 216))
+AERIAL_SIDES = (16, 24, 32, 48, 64)
+
+
+def batched_lut_sets():
+    """(config, planet radius) of the two parameter sets of the batch."""
+
+    from .config import EARTH_RADIUS_M as R_EARTH, SMALL_PLANET_RADIUS_M, earth_baseline, small_planet
+
+    return [(earth_baseline(), R_EARTH), (small_planet(), SMALL_PLANET_RADIUS_M)]
+
+
+def batched_lut_jobs(seed: int = 2027, snapshots: int = 256, cameras: int = 16):
+    """Jobs of the batched LUT-build workload: ``snapshots`` time snapshots
+    (sun zenith uniform 0-110 deg, azimuth uniform 0-360 deg) x ``cameras``
+    cameras (altitude log-uniform 1 m - 4000 km, yaw uniform, pitch uniform
+    -45..10 deg) x both parameter sets; each (snapshot, camera, set) gets a
+    sky-view LUT (96x54 .. 384x216) and an aerial volume (16^3 .. 64^3) with
+    sizes drawn uniformly from those ladders.  Seeded."""
+
+    from .batch import AERIAL, SKY_VIEW, BatchJob
+
+    rng = np.random.default_rng(seed)
+    zen = rng.uniform(0.0, 110.0, snapshots)
+    azi = rng.uniform(0.0, 360.0, snapshots)
+    alt = np.exp(rng.uniform(np.log(1.0), np.log(4.0e6), cameras))
+    yaw = rng.uniform(0.0, 360.0, cameras)
+    pitch = rng.uniform(-45.0, 10.0, cameras)
+    tanfov = camera.tangent_half_fov(VERTICAL_FOV_DEG)
+    bases = [camera.view_basis(float(y), float(p)) for y, p in zip(yaw, pitch)]
+    jobs = []
+    for s in range(snapshots):
+        sun = camera.sun_from_zenith(float(zen[s]), float(azi[s]))
+        sun_cos = float(np.float32(np.clip(sun[1], -1.0, 1.0)))
+        for c in range(cameras):
+            basis = tuple(tuple(float(v) for v in b) for b in bases[c])
+            for param_set in (0, 1):
+                sw, sh = SKY_VIEW_SIZES[rng.integers(len(SKY_VIEW_SIZES))]
+                side = AERIAL_SIDES[rng.integers(len(AERIAL_SIDES))]
+                jobs.append(BatchJob(SKY_VIEW, param_set, sw, sh, 1, camera_altitude_m=float(alt[c]),
+                                     sun_zenith_cosine=sun_cos))
+                jobs.append(BatchJob(AERIAL, param_set, side, side, side, camera_altitude_m=float(alt[c]),
+                                     sun_local=tuple(float(v) for v in sun), view_basis=basis,
+                                     tangent_half_fov=tanfov))
+    return jobs
