@@ -253,6 +253,35 @@ int atm_batch_read_samples(AtmBatch* batch, int32_t reset, uint64_t* out, void* 
  * multi-scattering (kind 1) LUT. */
 int atm_batch_static_lut(const AtmBatch* batch, int32_t param_set, int32_t kind, void** device_ptr);
 
+/* ---- MLP surrogates --------------------------------------------------------
+ * No counterpart in the reference (its atmosphere has no learned part): small
+ * networks n_in -> [64 SiLU] x n_hidden -> n_out standing in for the sky-view
+ * and aerial-perspective integrals.  Parameters live on the device as one
+ * float array (per layer W (out x in, row-major) then b).  Training: fused
+ * FP32 forward + backward of the mean squared error over the batch, Adam. */
+typedef struct AtmMlp AtmMlp;
+int atm_mlp_create(int32_t n_in, int32_t n_hidden_layers, int32_t n_out, uint64_t seed, AtmMlp** out);
+int atm_mlp_destroy(AtmMlp* mlp);
+int atm_mlp_info(const AtmMlp* mlp, int32_t* n_params, float** device_params);
+int atm_mlp_reset_optimizer(AtmMlp* mlp, void* stream);
+/* Device-to-device copies of the parameter array (checkpoint / restore). */
+int atm_mlp_get_params(const AtmMlp* mlp, float* dst_device, void* stream);
+int atm_mlp_set_params(AtmMlp* mlp, const float* src_device, void* stream);
+/* Gradient of the batch loss into grad_out (device, n_params floats, may be
+ * null) and the summed squared error into loss_out (device float, may be
+ * null); parameters unchanged. */
+int atm_mlp_gradient(AtmMlp* mlp, const float* inputs, const float* targets, int64_t n, float* grad_out,
+                     float* loss_out, void* stream);
+/* One Adam step on a batch (inputs n x n_in, targets n x n_out, device). */
+int atm_mlp_train_step(AtmMlp* mlp, const float* inputs, const float* targets, int64_t n, float lr, float beta1,
+                       float beta2, float eps, float* loss_out, void* stream);
+/* Copy the current parameters into the BF16 tensor-core layout. */
+int atm_mlp_pack_bf16(AtmMlp* mlp, void* stream);
+/* outputs (n x n_out) = network(inputs); precision 0 = FP32 CUDA cores,
+ * 1 = BF16 tensor cores with FP32 accumulation (after atm_mlp_pack_bf16). */
+int atm_mlp_forward(const AtmMlp* mlp, const float* inputs, float* outputs, int64_t n, int32_t precision,
+                    void* stream);
+
 /* COMPOSITE view of atm_composite that allocates nothing.  No counterpart in
  * the reference.  For callers that may not call cudaMalloc: an engine or
  * plugin host that owns every device allocation through its own pool, a

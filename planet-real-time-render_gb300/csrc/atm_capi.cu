@@ -677,6 +677,180 @@ ATM_API int atm_batch_static_lut(const AtmBatch* b, int32_t param_set, int32_t k
   return ATM_OK;
 }
 
+// ---- MLP surrogates -------------------------------------------------------
+struct AtmMlp {
+  atm::MlpShape shape{};
+  float* params = nullptr;
+  float* grad = nullptr;
+  float* m1 = nullptr;
+  float* m2 = nullptr;
+  float* partial = nullptr;
+  size_t partial_floats = 0;
+  float* loss_partial = nullptr;
+  size_t loss_floats = 0;
+  void* packed = nullptr;
+  long long step = 0;
+  int sm_count = 0;
+};
+
+ATM_API int atm_mlp_destroy(AtmMlp* m) {
+  if (!m) return ATM_OK;
+  for (void* p : {static_cast<void*>(m->params), static_cast<void*>(m->grad), static_cast<void*>(m->m1),
+                  static_cast<void*>(m->m2), static_cast<void*>(m->partial), static_cast<void*>(m->loss_partial),
+                  m->packed})
+    if (p) cudaFree(p);
+  delete m;
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_create(int32_t n_in, int32_t n_hidden_layers, int32_t n_out, uint64_t seed, AtmMlp** out) {
+  if (!out) return fail(ATM_E_INVALID, "null output");
+  *out = nullptr;
+  if (n_in < 1 || n_in > 8 || n_out < 1 || n_out > 8 || n_hidden_layers < 1 || n_hidden_layers > 4)
+    return fail(ATM_E_INVALID, "MLP shape must have 1..8 inputs, 1..8 outputs and 1..4 hidden layers of 64");
+  AtmMlp* m = new (std::nothrow) AtmMlp();
+  if (!m) return fail(ATM_E_NOMEM, "host allocation failed");
+  m->shape = atm::make_mlp_shape(n_in, n_hidden_layers, n_out);
+  const size_t np = size_t(m->shape.n_params);
+  // Glorot-uniform weights from a seeded xorshift generator, zero biases
+  std::vector<float> host(np, 0.0f);
+  uint64_t st = seed * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull;
+  auto next = [&st]() {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return double(st >> 11) * (1.0 / 9007199254740992.0);
+  };
+  for (int l = 0; l < m->shape.n_layers; ++l) {
+    const int in = m->shape.in_dim[l], o = m->shape.out_dim[l];
+    const double lim = std::sqrt(6.0 / double(in + o));
+    for (int i = 0; i < in * o; ++i) host[m->shape.off_w[l] + i] = float((2.0 * next() - 1.0) * lim);
+  }
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&m->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  for (float** p : {&m->params, &m->grad, &m->m1, &m->m2})
+    if (e == cudaSuccess) e = cudaMalloc(p, np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&m->packed, atm::mlp_bf16_bytes(m->shape));
+  if (e == cudaSuccess) e = cudaMemcpy(m->params, host.data(), np * sizeof(float), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(m->m1, 0, np * sizeof(float));
+  if (e == cudaSuccess) e = cudaMemset(m->m2, 0, np * sizeof(float));
+  if (e != cudaSuccess) {
+    atm_mlp_destroy(m);
+    return cuda_fail(e, "MLP allocation");
+  }
+  *out = m;
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_info(const AtmMlp* m, int32_t* n_params, float** device_params) {
+  if (!m) return fail(ATM_E_INVALID, "null AtmMlp");
+  if (n_params) *n_params = m->shape.n_params;
+  if (device_params) *device_params = m->params;
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_get_params(const AtmMlp* m, float* dst_device, void* stream) {
+  if (!m || !dst_device) return fail(ATM_E_INVALID, "null argument");
+  ATM_CUDA(cudaMemcpyAsync(dst_device, m->params, size_t(m->shape.n_params) * sizeof(float), cudaMemcpyDeviceToDevice,
+                           static_cast<cudaStream_t>(stream)),
+           "parameter read");
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_set_params(AtmMlp* m, const float* src_device, void* stream) {
+  if (!m || !src_device) return fail(ATM_E_INVALID, "null argument");
+  ATM_CUDA(cudaMemcpyAsync(m->params, src_device, size_t(m->shape.n_params) * sizeof(float), cudaMemcpyDeviceToDevice,
+                           static_cast<cudaStream_t>(stream)),
+           "parameter write");
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_reset_optimizer(AtmMlp* m, void* stream) {
+  if (!m) return fail(ATM_E_INVALID, "null AtmMlp");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ATM_CUDA(cudaMemsetAsync(m->m1, 0, size_t(m->shape.n_params) * sizeof(float), s), "optimizer reset");
+  ATM_CUDA(cudaMemsetAsync(m->m2, 0, size_t(m->shape.n_params) * sizeof(float), s), "optimizer reset");
+  m->step = 0;
+  return ATM_OK;
+}
+
+namespace {
+int mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n, float* loss_out, cudaStream_t s) {
+  if (!m || !inputs || !targets || n < 1) return fail(ATM_E_INVALID, "invalid MLP gradient arguments");
+  const size_t ctas = size_t(atm::mlp_train_ctas(n));
+  const size_t need = ctas * size_t(m->shape.n_params);
+  if (m->partial_floats < need) {
+    if (m->partial) cudaFree(m->partial);
+    m->partial = nullptr;
+    m->partial_floats = 0;
+    ATM_CUDA(cudaMalloc(&m->partial, need * sizeof(float)), "gradient workspace");
+    m->partial_floats = need;
+  }
+  if (m->loss_floats < ctas) {
+    if (m->loss_partial) cudaFree(m->loss_partial);
+    m->loss_partial = nullptr;
+    m->loss_floats = 0;
+    ATM_CUDA(cudaMalloc(&m->loss_partial, ctas * sizeof(float)), "loss workspace");
+    m->loss_floats = ctas;
+  }
+  ATM_CUDA(atm::launch_mlp_grad(m->shape, m->params, inputs, targets, n, m->partial, m->loss_partial, m->grad, s),
+           "MLP forward/backward");
+  if (loss_out) {
+    atm::MlpShape one{};
+    one.n_params = 1;
+    ATM_CUDA(atm::launch_reduce_partials(m->loss_partial, int(ctas), 1, loss_out, s), "loss reduction");
+  }
+  return ATM_OK;
+}
+}  // namespace
+
+ATM_API int atm_mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n, float* grad_out,
+                             float* loss_out, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int rc = mlp_gradient(m, inputs, targets, n, loss_out, s);
+  if (rc) return rc;
+  if (grad_out)
+    ATM_CUDA(cudaMemcpyAsync(grad_out, m->grad, size_t(m->shape.n_params) * sizeof(float), cudaMemcpyDeviceToDevice,
+                             s),
+             "gradient copy");
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_train_step(AtmMlp* m, const float* inputs, const float* targets, int64_t n, float lr, float beta1,
+                               float beta2, float eps, float* loss_out, void* stream) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!(lr > 0.0f) || !(beta1 >= 0.0f && beta1 < 1.0f) || !(beta2 >= 0.0f && beta2 < 1.0f) || !(eps > 0.0f))
+    return fail(ATM_E_INVALID, "invalid Adam hyper-parameters");
+  int rc = mlp_gradient(m, inputs, targets, n, loss_out, s);
+  if (rc) return rc;
+  m->step += 1;
+  ATM_CUDA(atm::launch_adam(m->params, m->grad, m->m1, m->m2, m->shape.n_params, lr, beta1, beta2, eps, m->step, s),
+           "Adam update");
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_pack_bf16(AtmMlp* m, void* stream) {
+  if (!m) return fail(ATM_E_INVALID, "null AtmMlp");
+  ATM_CUDA(atm::launch_mlp_pack_bf16(m->shape, m->params, m->packed, static_cast<cudaStream_t>(stream)),
+           "BF16 packing");
+  return ATM_OK;
+}
+
+ATM_API int atm_mlp_forward(const AtmMlp* m, const float* inputs, float* outputs, int64_t n, int32_t precision,
+                            void* stream) {
+  if (!m || !inputs || !outputs || n < 1) return fail(ATM_E_INVALID, "invalid MLP forward arguments");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (precision == 0)
+    ATM_CUDA(atm::launch_mlp_forward_f32(m->shape, m->params, inputs, outputs, n, s), "MLP forward (FP32)");
+  else if (precision == 1)
+    ATM_CUDA(atm::launch_mlp_forward_bf16(m->shape, m->packed, inputs, outputs, n, m->sm_count, s),
+             "MLP forward (BF16 tensor cores)");
+  else
+    return fail(ATM_E_INVALID, "precision must be 0 (FP32) or 1 (BF16)");
+  return ATM_OK;
+}
+
 // Composite that allocates nothing (no counterpart in the reference).  See
 // include/atm_capi.h: caller-owned LUTs, images and count output; the only
 // scratch is the library's file-scope per-tile array.

@@ -14,40 +14,13 @@
 #include <mutex>
 
 #include "atm_device.cuh"
+#include "atm_frame_paths.cuh"
 #include "atm_kernels.h"
 
 namespace atm {
 namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
-
-__device__ __forceinline__ size_t pix_offset(const ImageLayout& L, int x, int y) {
-  return size_t(int64_t(x) * L.sx + int64_t(y) * L.sy);
-}
-
-// Pixel of thread: blocks of 16x16 pixels, each warp an 8x4 sub-tile.
-__device__ __forceinline__ bool tile_pixel(const ImageLayout& L, int& x, int& y) {
-  const int lane = threadIdx.x & 31;
-  const int w = threadIdx.x >> 5;  // 0..7
-  x = blockIdx.x * 16 + (w & 1) * 8 + (lane & 7);
-  y = blockIdx.y * 16 + (w >> 1) * 4 + (lane >> 3);
-  return x < L.width && y < L.height;
-}
-
-// Pixel of a thread for memory-bound per-pixel kernels: consecutive threads
-// take consecutive elements along the image's contiguous dimension.
-__device__ __forceinline__ bool linear_pixel(const ImageLayout& L, int& x, int& y) {
-  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= (long long)L.width * L.height) return false;
-  if (L.sy <= L.sx) {  // y contiguous: the reference's (W, H, 3) layout
-    x = int(i / L.height);
-    y = int(i % L.height);
-  } else {
-    y = int(i / L.width);
-    x = int(i % L.width);
-  }
-  return true;
-}
 
 // _prepare_surface_lighting :1422-1472
 __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayout L, const float* __restrict__ pos,
@@ -84,171 +57,6 @@ __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayou
   out_sky[o + 0] = sky.x;
   out_sky[o + 1] = sky.y;
   out_sky[o + 2] = sky.z;
-}
-
-struct PixelRay {
-  f3 ray;
-  float su, sv;
-};
-__device__ __forceinline__ PixelRay pixel_ray(const ImageLayout& L, const CompositeScalars& A, int x, int y) {
-  PixelRay r;
-  const float aspect = float(L.width) / float(L.height);
-  r.su = (float(x) + 0.5f) / float(L.width);
-  r.sv = (float(y) + 0.5f) / float(L.height);
-  float sx = (r.su * 2.0f - 1.0f) * aspect;
-  float sy = r.sv * 2.0f - 1.0f;
-  f3 rv = (arr3(A.right) * sx + arr3(A.up) * sy) + arr3(A.fwd) / A.tanfov;
-  r.ray = rv * (1.0f / norm(rv));
-  return r;
-}
-
-// _solar_shadow_roots :685-726
-__device__ __forceinline__ void shadow_roots(f3 o, f3 d, f3 sun, float bottom, float& r0, float& r1, bool& v0,
-                                             bool& v1) {
-  f3 op = o - sun * dot(o, sun);
-  f3 rp = d - sun * dot(d, sun);
-  float quad = dot(rp, rp);
-  float hl = dot(op, rp);
-  float pl = norm(op);
-  float c = (pl - bottom) * (pl + bottom);
-  r0 = 0.0f;
-  r1 = 0.0f;
-  v0 = false;
-  v1 = false;
-  float disc = hl * hl - quad * c;
-  if (quad > 1.0e-8f && disc >= 0.0f) {
-    float sr = sqrtf(mx(disc, 0.0f));
-    r0 = (-hl - sr) / quad;
-    r1 = (-hl + sr) / quad;
-    v0 = dot(o + d * r0, sun) < 0.0f;
-    v1 = dot(o + d * r1, sun) < 0.0f;
-  }
-}
-
-// _integrate_surface_scattering :1667-1755 (with :901-1032).  `start`/`end`
-// are the shell-clipped interval; the caller has checked it is non-empty.
-__device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame& F, float cam_alt, f3 ray,
-                                                float start, float end, uint32_t& samples) {
-  const float o_y = F.bottom + cam_alt;
-  const f3 origin = mk(0.0f, o_y, 0.0f);
-  float sr0, sr1;
-  bool sv0, sv1;
-  shadow_roots(origin, ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
-  const RaySource rs = make_ray_source(P, F, o_y, cam_alt, ray);
-  const RayWarp rw = make_warp(-(o_y * ray.y), start, end);
-  const bool roots = sv0 || sv1;
-  const int n = P.limb_steps;
-  const int nsub = P.substeps;
-  Seg acc = {splat(0.0f), splat(1.0f)};
-  float d0 = warp_at(rw, 0.0f);
-  for (int i = 0; i < n; ++i) {
-    float d1 = warp_at(rw, float(i + 1) / float(n));
-    float vis;
-    Seg coarse = source_segment<true>(P, F, rs, d0, d1, vis);
-    ++samples;
-    // _terminator_refinement_weight :901-966; zero unless a shadow-cylinder
-    // root exists or the disk is partly hidden at the midpoint
-    float w = 0.0f;
-    if (roots || (vis > 0.0f && vis < 1.0f)) {
-      float mid = (d0 + d1) * 0.5f;
-      float iw = mx(d1 - d0, 1.0e-4f);
-      float closest_root = 1.0e30f;
-      if (sv0) closest_root = mn(closest_root, fabsf(mid - sr0));
-      if (sv1) closest_root = mn(closest_root, fabsf(mid - sr1));
-      float prox = __saturatef(2.0f - fdiv(closest_root, iw));
-      prox = prox * prox * (3.0f - 2.0f * prox);
-      w = mx(prox, 4.0f * vis * (1.0f - vis));
-    }
-    Seg interval = coarse;
-    if (w > 0.0f) {
-      // _integrate_adaptive_scattering_interval :998-1031
-      Seg fine = {splat(0.0f), splat(1.0f)};
-      float c0 = d0 + (d1 - d0) * 0.0f;
-      for (int k = 0; k < nsub; ++k) {
-        float c1 = d0 + (d1 - d0) * (float(k + 1) / float(nsub));
-        float cvis;
-        fine = seg_then(fine, source_segment<true>(P, F, rs, c0, c1, cvis));
-        c0 = c1;
-      }
-      samples += nsub;
-      interval.L = coarse.L * (1.0f - w) + fine.L * w;
-      interval.T = coarse.T * (1.0f - w) + fine.T * w;
-    }
-    acc = seg_then(acc, interval);
-    d0 = d1;
-  }
-  return vmax(acc.L, 0.0f);
-}
-
-// _surface_segment_transmittance :1603-1665 on an already clipped interval.
-__device__ __forceinline__ f3 surface_segment_t(const DevParams& P, const Frame& F, float cam_alt, f3 ray,
-                                                float start, float end) {
-  const f3 origin = mk(0.0f, F.bottom + cam_alt, 0.0f);
-  f3 np = origin + ray * start;
-  f3 sp = origin + ray * end;
-  f3 rr = -ray;
-  f3 nrad = np / mx(norm(np), 1.0f);
-  f3 srad = sp / mx(norm(sp), 1.0f);
-  float na = altitude_on_ray(cam_alt, ray.y, start, F.bottom);
-  float sa = altitude_on_ray(cam_alt, ray.y, end, F.bottom);
-  f3 s2t = sample_t(P, F, sa, dot(srad, rr));
-  f3 n2t = sample_t(P, F, na, dot(nrad, rr));
-  return vclamp(s2t / vmax(n2t, 1.0e-6f), 0.0f, 1.0f);
-}
-
-// _camera_transmittance :1788-1825
-__device__ __forceinline__ f3 camera_t(const DevParams& P, const Frame& F, float cam_alt, f3 ray) {
-  float s, e;
-  bool valid, ground;
-  segment_from_altitude(P, cam_alt, ray.y, F.bottom, s, e, valid, ground);
-  if (!valid) return splat(1.0f);
-  if (ground) return splat(0.0f);
-  f3 entry = mk(0.0f, F.bottom + cam_alt, 0.0f) + ray * s;
-  f3 radial = entry / mx(norm(entry), 1.0f);
-  float ea = altitude_on_ray(cam_alt, ray.y, s, F.bottom);
-  return sample_t(P, F, ea, dot(radial, ray));
-}
-
-// _sample_sky_view :1474-1525
-__device__ __forceinline__ f3 sample_sky_view(const DevParams& P, const float4* __restrict__ svlut, f3 ray, f3 sun,
-                                              float sky_alt, float bottom) {
-  float zen = acosf(clampf(ray.y, -1.0f, 1.0f));
-  float vl = sqrtf(ray.x * ray.x + ray.z * ray.z);
-  float sl = sqrtf(sun.x * sun.x + sun.z * sun.z);
-  float ra = 0.0f;
-  if (vl > 1.0e-6f && sl > 1.0e-6f) ra = acosf(clampf((ray.x * sun.x + ray.z * sun.z) / (vl * sl), -1.0f, 1.0f));
-  float u = ra / kPiF;
-  float v = sky_zenith_to_v(zen, sky_horizon_zenith(sky_alt, bottom));
-  return bilinear(svlut, P.sv_w, P.sv_h, u, v);
-}
-
-// Shell clip shared by the scattering integral and the transmittance ratio.
-__device__ __forceinline__ bool surface_interval(const DevParams& P, float cam_alt, float ray_y, float bottom,
-                                                 float surface_distance, float& start, float& end) {
-  float on, of;
-  bool oh;
-  shell_roots(cam_alt, ray_y, P.top, bottom, on, of, oh);
-  start = mx(on, 0.0f);
-  end = mn(surface_distance, of);
-  return oh && end > start;
-}
-
-__device__ __forceinline__ f3 composite_sky(const DevParams& P, const Frame& F, const CompositeScalars& A,
-                                            const float4* __restrict__ svlut, f3 ray, f3 color, f3 space,
-                                            float height) {
-  f3 tr = camera_t(P, F, A.cam_alt, ray);
-  f3 sky = sample_sky_view(P, svlut, ray, F.sun, A.sky_alt, F.bottom);
-  f3 star = space * tr;
-  const f3 lw = mk(0.2126f, 0.7152f, 0.0722f);
-  float contrast = dot(star, lw) / mx(dot(sky, lw), 1.0e-5f);
-  float vis = clampf((contrast - A.star_start) / mx(A.star_end - A.star_start, 1.0e-5f), 0.0f, 1.0f);
-  vis = vis * vis * (3.0f - 2.0f * vis);
-  color = (sky + color * tr) + star * vis;
-  float ad = acosf(clampf(dot(ray, F.sun), -1.0f, 1.0f));
-  float pf = atan2f(A.tanfov * 1.41421356f / height, 1.0f);
-  float cov = clampf((F.ar + pf - ad) / mx(2.0f * pf, 1.0e-8f), 0.0f, 1.0f);
-  cov = cov * cov * (3.0f - 2.0f * cov);
-  return color + arr3(A.disk) * tr * cov;
 }
 
 // COMPOSITE view (:1860-1940): the per-frame path.

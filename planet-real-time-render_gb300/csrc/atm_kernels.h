@@ -60,6 +60,54 @@ void fill_batch_job(BatchJobDev& d, const DevParams& set_params, const AtmBatchJ
 cudaError_t launch_batch(const BatchJobDev* jobs, const long long* prefix, int n_jobs, long long n_items,
                          unsigned long long* ticket, unsigned long long* samples, int blocks, cudaStream_t s);
 
+// MLP surrogates (atm_mlp.cu): n_in -> [64 SiLU] x (n_layers - 1) -> n_out.
+constexpr int kMaxMlpLayers = 5;
+struct MlpShape {
+  int n_in, n_out, n_layers, n_params;
+  int in_dim[kMaxMlpLayers], out_dim[kMaxMlpLayers], off_w[kMaxMlpLayers], off_b[kMaxMlpLayers];
+};
+MlpShape make_mlp_shape(int n_in, int n_hidden, int n_out);
+int mlp_train_ctas(long long n);
+size_t mlp_train_smem_bytes(const MlpShape& m);
+size_t mlp_bf16_bytes(const MlpShape& m);
+cudaError_t launch_mlp_grad(const MlpShape& m, const float* params, const float* inputs, const float* targets,
+                            long long n, float* grad_partial, float* loss_partial, float* grad, cudaStream_t s);
+cudaError_t launch_reduce_partials(const float* partial, int rows, int cols, float* out, cudaStream_t s);
+cudaError_t launch_adam(float* params, const float* grad, float* m1, float* m2, int n, float lr, float b1, float b2,
+                        float eps, long long step, cudaStream_t s);
+cudaError_t launch_mlp_forward_f32(const MlpShape& m, const float* params, const float* inputs, float* outputs,
+                                   long long n, cudaStream_t s);
+cudaError_t launch_mlp_pack_bf16(const MlpShape& m, const float* params, void* packed, cudaStream_t s);
+cudaError_t launch_mlp_forward_bf16(const MlpShape& m, const void* packed, const float* inputs, float* outputs,
+                                    long long n, int sm_count, cudaStream_t s);
+
+// Surrogates (atm_surrogate.cu).  Targets: log(L / E + floor) and optical
+// depth; segment lengths up to 2000 km.
+constexpr float kSurrogateFloor = 1.0e-7f;
+constexpr float kSurrogateMaxLength = 2.0e6f;
+constexpr float kSurrogateMaxDepth = 30.0f;
+struct SurrogateSetDev {
+  DevParams P;
+  const float4* tlut;
+  const float4* mslut;
+  float bottom;
+  float lhr_n, lhm_n;  // normalised log scale heights (features 4, 5)
+};
+struct SurrogateNets {
+  const unsigned char* ap;   // packed BF16 aerial network (7 -> 4x64 -> 6) or null
+  const unsigned char* sky;  // packed BF16 sky network (6 -> 3x64 -> 3) or null
+  int ap_bytes, sky_bytes;
+  float lhr_n, lhm_n;
+};
+cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
+                               const float E[3], float ar, float* features, float* targets,
+                               unsigned long long* counter, cudaStream_t s);
+cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                                       const float* scene, const float* space, const int32_t* sid, const float* pos,
+                                       const float4* tlut, const float4* mslut, const float4* svlut,
+                                       const SurrogateNets& nets, unsigned seed, float check_fraction, float* hdr,
+                                       float* stats, unsigned long long* counter, cudaStream_t s);
+
 // atm_composite_noalloc: the per-device address of the file-scope tile
 // scratch (looked up on the first call on each device), its capacity in
 // 16x16 tiles, and the COMPOSITE-view launch that uses it.

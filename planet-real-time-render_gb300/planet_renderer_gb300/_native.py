@@ -178,6 +178,17 @@ SIGNATURES = {
     ),
     "atm_batch_read_samples": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
     "atm_batch_static_lut": (ctypes.c_int, [_P, _I32, _I32, ctypes.POINTER(_P)]),
+    "atm_mlp_create": (ctypes.c_int, [_I32, _I32, _I32, ctypes.c_uint64, ctypes.POINTER(_P)]),
+    "atm_mlp_destroy": (ctypes.c_int, [_P]),
+    "atm_mlp_info": (ctypes.c_int, [_P, ctypes.POINTER(_I32), ctypes.POINTER(_P)]),
+    "atm_mlp_reset_optimizer": (ctypes.c_int, [_P, _P]),
+    "atm_mlp_get_params": (ctypes.c_int, [_P, _P, _P]),
+    "atm_mlp_set_params": (ctypes.c_int, [_P, _P, _P]),
+    "atm_mlp_gradient": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),
+    "atm_mlp_train_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                                          ctypes.c_float, ctypes.c_float, _P, _P]),
+    "atm_mlp_pack_bf16": (ctypes.c_int, [_P, _P]),
+    "atm_mlp_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _I32, _P]),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,
