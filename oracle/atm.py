@@ -117,16 +117,20 @@ class Oracle:
     """Kernel-level oracle.  ``precision`` "f32" mirrors Taichi f32; "f64"
     is the same algorithm in double."""
 
-    def __init__(self, precision: str = "f32", threads: int | None = None):
+    def __init__(self, precision: str = "f32", threads: int | None = None, series_weight: bool = False):
         if precision not in ("f32", "f64"):
             raise ValueError(precision)
         self.precision = precision
         self.dtype = np.float32 if precision == "f32" else np.float64
+        # series_weight: NOT the reference - the segment weight by its Taylor
+        # series where the reference's formula cancels (a diagnostic variant)
+        self.series_weight = bool(series_weight)
         self.lib = library()
         if threads:
             self.lib.orc_set_threads(int(threads))
 
     def _fn(self, name):
+        self.lib.orc_set_series_weight(int(self.series_weight))
         return getattr(self.lib, f"orc_{name}_{self.precision}")
 
     def _arr(self, a) -> np.ndarray:

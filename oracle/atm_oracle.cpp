@@ -27,6 +27,10 @@
 #include <omp.h>
 #endif
 
+// 1: the segment weight by its Taylor series where it cancels (not the
+// reference; see Model::series_weight).
+static int g_series_weight = 0;
+
 // Scalar arguments of the composite kernel (reference _composite :1827-1849);
 // values as the host passes them (Python floats), rounded on use.
 struct CompositeArgs {
@@ -435,6 +439,20 @@ struct Model {
     integ.x = ext.x > R(1.0e-12) ? (R(1) - tr.x) / ext.x : step;
     integ.y = ext.y > R(1.0e-12) ? (R(1) - tr.y) / ext.y : step;
     integ.z = ext.z > R(1.0e-12) ? (R(1) - tr.z) / ext.z : step;
+    if (g_series_weight) {
+      integ.x = series_weight(ext.x, step, integ.x);
+      integ.y = series_weight(ext.y, step, integ.y);
+      integ.z = series_weight(ext.z, step, integ.z);
+    }
+  }
+  // Not the reference: the weight (1 - exp(-x)) / ext by its Taylor series
+  // below x = 1/32, where the reference's float formula cancels.  Enabled
+  // only to show that this one step is what makes the reference's float
+  // result drift from its double result next to the ground.
+  R series_weight(R ext, R step, R plain) const {
+    R x = mn(ext * step, R(80));
+    if (!(x < R(0.03125))) return plain;
+    return step * (R(1) + x * (R(-0.5) + x * (R(1.0 / 6.0) + x * R(-1.0 / 24.0))));
   }
   // _scattering_source :818-856
   V3<R> scattering_source(V3<R> point, R h, V3<R> ray, V3<R> sun, V3<R> E, R bottom, R ar, bool multiple) const {
@@ -1050,6 +1068,8 @@ ORC_EXPORT void orc_op_counts(uint64_t out[9], int reset) {
     if (reset) opcount::counts[i] = 0;
   }
 }
+
+ORC_EXPORT void orc_set_series_weight(int on) { g_series_weight = on; }
 
 ORC_EXPORT int orc_max_threads(void) {
 #ifdef _OPENMP

@@ -474,14 +474,26 @@ __device__ __forceinline__ float mie_phase(const DevParams& P, float c) {
   float den = mx(P.mie_c1 - P.mie_c2 * c, 1.0e-8f);
   return P.mie_k1 * (1.0f + c * c) / (P.mie_k2 * (den * sqrtf(den)));
 }
+// In-scattering weight (1 - T) / ext of one segment, T = exp(-x), x =
+// ext * step.  The reference forms 1 - T directly, which cancels in f32 when
+// x is small: centimetre segments next to a camera standing on the ground
+// give x ~ 1e-7 and a weight with no significant digit left (its own f32
+// result is then percents away from its f64 one).  Below x = 1/32 the weight
+// is the Taylor series step * (1 - x/2 + x^2/6 - x^3/24) of the same quantity
+// (truncation under 1e-8 relative; step itself at ext = 0, as the
+// reference's ext <= 1e-12 branch); above it 1 - T keeps 5+ digits.
+__device__ __forceinline__ float in_scatter_weight(float ext, float step, float x, float tr) {
+  if (x < 0.03125f) return step * fmaf(x, fmaf(x, fmaf(x, -1.0f / 24.0f, 1.0f / 6.0f), -0.5f), 1.0f);
+  return fdiv(1.0f - tr, ext);
+}
 // _segment_integral :806-816
 __device__ __forceinline__ void segment_integral(f3 ext, float step, f3& tr, f3& integ) {
   // __expf: ~2 ulp near 0 (as expf), up to ~95 ulp at the clamp (T ~ 1e-35)
   const f3 x = vmin(ext * step, 80.0f);
   tr = {__expf(-x.x), __expf(-x.y), __expf(-x.z)};
-  integ.x = ext.x > 1.0e-12f ? fdiv(1.0f - tr.x, ext.x) : step;
-  integ.y = ext.y > 1.0e-12f ? fdiv(1.0f - tr.y, ext.y) : step;
-  integ.z = ext.z > 1.0e-12f ? fdiv(1.0f - tr.z, ext.z) : step;
+  integ.x = in_scatter_weight(ext.x, step, x.x, tr.x);
+  integ.y = in_scatter_weight(ext.y, step, x.y, tr.y);
+  integ.z = in_scatter_weight(ext.z, step, x.z, tr.z);
 }
 
 // Per-ray constants of the constant-source samples (everything of

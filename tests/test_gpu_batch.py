@@ -8,7 +8,7 @@ import math
 import numpy as np
 import pytest
 
-from conftest import assert_parity
+from conftest import assert_exact_parity, assert_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -55,13 +55,21 @@ def test_batch_matches_single_lut_kernels():
             ref = r.aerial_scattering_lut.to_torch()
         single_samples += r.radiance_samples(reset=True)
         got = result.lut(i)
-        assert torch.equal(got, ref), f"job {i} kind {j.kind} {j.width}x{j.height}x{j.depth}"
+        # same device functions in another kernel: FMA contraction may differ in the last bits
+        assert_parity(got.cpu().numpy(), ref.cpu().numpy(), f"job {i} kind {j.kind} {j.width}x{j.height}x{j.depth}",
+                      rtol=1e-5, atol_frac=1e-7)
         r.close()
     assert batch_samples == single_samples
     builder.close()
 
 
 def test_batch_matches_oracle():
+    """Batched LUTs against the oracle.  The small batch holds cameras 3 m
+    above the ground, where the reference's float32 segment weight cancels:
+    the comparison is against the float64 oracle with the reference's own
+    float32 deviation allowed (``assert_exact_parity``)."""
+    import dataclasses
+
     import torch
 
     from oracle.atm import Oracle
@@ -71,25 +79,26 @@ def test_batch_matches_oracle():
     builder = BatchedLutBuilder(sets)
     result = builder.build(jobs, Tuning(64, 1, 2))
     torch.cuda.synchronize()
-    oracle = Oracle("f32")
-    ar = float(np.float32(math.radians(0.266)))
     E = (4.0, 3.9, 3.7)
-    import dataclasses
-
+    oracles = {"f32": (Oracle("f32"), float(np.float32(math.radians(0.266)))),
+               "f64": (Oracle("f64"), math.radians(0.266))}
     for i in (0, 1, 2, 3, len(jobs) - 2, len(jobs) - 1):
         j = jobs[i]
         cfg, radius = sets[j.param_set]
-        tl = oracle.build_transmittance(cfg, radius)
-        ms = oracle.build_multi_scattering(cfg, radius, E, ar, tl)
-        if j.kind == SKY_VIEW:
-            c = dataclasses.replace(cfg, sky_view_lut_width=j.width, sky_view_lut_height=j.height)
-            ref = oracle.build_sky_view(c, radius, j.camera_altitude_m, j.sun_zenith_cosine, E, ar, tl, ms)
-        else:
-            c = dataclasses.replace(cfg, aerial_lut_width=j.width, aerial_lut_height=j.height,
-                                    aerial_lut_depth=j.depth)
-            ref = oracle.build_aerial(c, j.frame_width, j.frame_height, radius, j.camera_altitude_m, j.sun_local, E,
-                                      math.radians(0.266), j.view_basis, j.tangent_half_fov, tl, ms)
-        assert_parity(result.lut(i).cpu().numpy(), ref, f"batch job {i}")
+        refs = {}
+        for prec, (oracle, ar) in oracles.items():
+            tl = oracle.build_transmittance(cfg, radius)
+            ms = oracle.build_multi_scattering(cfg, radius, E, ar, tl)
+            if j.kind == SKY_VIEW:
+                c = dataclasses.replace(cfg, sky_view_lut_width=j.width, sky_view_lut_height=j.height)
+                refs[prec] = oracle.build_sky_view(c, radius, j.camera_altitude_m, j.sun_zenith_cosine, E, ar, tl, ms)
+            else:
+                c = dataclasses.replace(cfg, aerial_lut_width=j.width, aerial_lut_height=j.height,
+                                        aerial_lut_depth=j.depth)
+                refs[prec] = oracle.build_aerial(c, j.frame_width, j.frame_height, radius, j.camera_altitude_m,
+                                                 j.sun_local, E, math.radians(0.266), j.view_basis,
+                                                 j.tangent_half_fov, tl, ms)
+        assert_exact_parity(result.lut(i).cpu().numpy(), refs["f32"], refs["f64"], f"batch job {i}")
     builder.close()
 
 
