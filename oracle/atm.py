@@ -205,6 +205,36 @@ class Oracle:
            _ptr(sun_t), _ptr(sky))
         return sun_t, sky
 
+    def sky_rays(self, config, bottom_radius, altitudes, rays, suns, irradiance, angular_radius_rad, tlut, mslut):
+        """Sky radiance along each ray (n, 3) from its altitude (n,), sun (n, 3)."""
+
+        p = params_from_config(config)
+        h, r, s = self._arr(altitudes), self._arr(rays), self._arr(suns)
+        n = h.shape[0]
+        out = np.zeros((n, 3), self.dtype)
+        fn = self._fn("sky_rays")
+        fn.argtypes = [ctypes.POINTER(AtmParams), ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 3 + \
+            [ctypes.c_double * 3, ctypes.c_double] + [ctypes.c_void_p] * 3
+        fn(ctypes.byref(p), float(bottom_radius), n, _ptr(h), _ptr(r), _ptr(s), _d3(irradiance),
+           float(angular_radius_rad), _ptr(self._arr(tlut)), _ptr(self._arr(mslut)), _ptr(out))
+        return out
+
+    def surface_rays(self, config, bottom_radius, altitudes, rays, surface_distances, suns, irradiance,
+                     angular_radius_rad, tlut, mslut):
+        """(in-scattering, transmittance) (n, 3) each of camera-to-surface segments."""
+
+        p = params_from_config(config)
+        h, r, d, s = (self._arr(a) for a in (altitudes, rays, surface_distances, suns))
+        n = h.shape[0]
+        L = np.zeros((n, 3), self.dtype)
+        T = np.zeros((n, 3), self.dtype)
+        fn = self._fn("surface_rays")
+        fn.argtypes = [ctypes.POINTER(AtmParams), ctypes.c_double, ctypes.c_int] + [ctypes.c_void_p] * 4 + \
+            [ctypes.c_double * 3, ctypes.c_double] + [ctypes.c_void_p] * 4
+        fn(ctypes.byref(p), float(bottom_radius), n, _ptr(h), _ptr(r), _ptr(d), _ptr(s), _d3(irradiance),
+           float(angular_radius_rad), _ptr(self._arr(tlut)), _ptr(self._arr(mslut)), _ptr(L), _ptr(T))
+        return L, T
+
     def composite(self, config, scene_hdr, space_hdr, surface_id, position_view, bottom_radius,
                   camera_altitude, sky_lut_camera_altitude, sun, irradiance, disk_radiance, angular_radius_rad,
                   basis, tangent_half_fov, star_start, star_end, diagnostic_view, tlut, mslut, svlut, aplut,

@@ -830,6 +830,63 @@ void build_aerial(const AtmParams& P, int width, int height, R bottom, R cam_alt
   }
 }
 
+// Sky radiance along n arbitrary rays from altitudes h[i]: the march of
+// _build_sky_view :1208-1302 for a given direction and sun (per ray).
+template <class R>
+void sky_rays(const AtmParams& P, R bottom, int n_rays, const R* h, const R* rays, const R* suns, const R* E3, R ar,
+              const R* tlut, const R* mslut, R* out) {
+  Model<R> m(P);
+  m.tlut = {tlut, P.transmittance_lut_width, P.transmittance_lut_height};
+  m.mslut = {mslut, P.multi_scattering_lut_width, P.multi_scattering_lut_height};
+  const V3<R> E = load3(E3);
+  const int n = P.sky_view_steps;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < n_rays; ++i) {
+    const R sh = mx(h[i], R(0));
+    const V3<R> o = v3(R(0), bottom + sh, R(0));
+    const V3<R> ray = load3(rays + 3 * static_cast<size_t>(i)), sun = load3(suns + 3 * static_cast<size_t>(i));
+    R s, e; bool valid, ground;
+    m.segment_from_altitude(sh, ray.y, bottom, s, e, valid, ground);
+    V3<R> rad = splat(R(0));
+    if (valid) {
+      V3<R> vT = splat(R(1));
+      for (int k = 0; k < n; ++k) {
+        R d0 = m.warp(o, ray, s, e, R(k) / R(n));
+        R d1 = m.warp(o, ray, s, e, R(k + 1) / R(n));
+        R dist = (d0 + d1) * R(0.5);
+        R step = d1 - d0;
+        R hh = m.altitude_on_ray(sh, ray.y, dist, bottom);
+        V3<R> src = m.scattering_source(o + ray * dist, hh, ray, sun, E, bottom, ar, true);
+        V3<R> sT, sI;
+        m.segment_integral(m.extinction(hh), step, sT, sI);
+        rad = rad + vT * src * sI;
+        vT = vT * sT;
+      }
+    }
+    store3(out + 3 * static_cast<size_t>(i), vmax(rad, R(0)));
+  }
+}
+
+// Camera-to-surface in-scattering and transmittance of n rays from
+// altitudes h[i] to surface distances sd[i]: _surface_aerial_scattering
+// :1757-1786 and _surface_segment_transmittance :1603-1665.
+template <class R>
+void surface_rays(const AtmParams& P, R bottom, int n_rays, const R* h, const R* rays, const R* sd, const R* suns,
+                  const R* E3, R ar, const R* tlut, const R* mslut, R* out_L, R* out_T) {
+  Model<R> m(P);
+  m.tlut = {tlut, P.transmittance_lut_width, P.transmittance_lut_height};
+  m.mslut = {mslut, P.multi_scattering_lut_width, P.multi_scattering_lut_height};
+  const V3<R> E = load3(E3);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int i = 0; i < n_rays; ++i) {
+    const R sh = mx(h[i], R(0));
+    const V3<R> o = v3(R(0), bottom + sh, R(0));
+    const V3<R> ray = load3(rays + 3 * static_cast<size_t>(i)), sun = load3(suns + 3 * static_cast<size_t>(i));
+    store3(out_L + 3 * static_cast<size_t>(i), m.integrate_surface(o, sh, ray, sd[i], sun, E, bottom, ar, nullptr));
+    store3(out_T + 3 * static_cast<size_t>(i), m.surface_segment_t(o, sh, ray, sd[i], bottom));
+  }
+}
+
 struct Image {
   int stride_x, stride_y, channels;
   size_t off(int x, int y) const { return (static_cast<size_t>(x) * stride_x + static_cast<size_t>(y) * stride_y) * channels; }
@@ -1047,6 +1104,18 @@ static_assert(sizeof(CountF) == sizeof(float), "CountF must alias float buffers"
     R f[3] = {R(fwd[0]), R(fwd[1]), R(fwd[2])};                                                                      \
     prepare_surface<R>(*p, W, H, pos, sid, Image{stride_x, stride_y, channels}, R(bottom), R(cam_alt), s, R(ar), r,  \
                        u, f, tlut, mslut, out_sun_t, out_sky);                                                       \
+  }                                                                                                                  \
+  ORC_EXPORT void orc_sky_rays_##SUFFIX(const AtmParams* p, double bottom, int n, const R* h, const R* rays,         \
+                                        const R* suns, const double* E, double ar, const R* tlut, const R* mslut,   \
+                                        R* out) {                                                                    \
+    R e[3] = {R(E[0]), R(E[1]), R(E[2])};                                                                            \
+    sky_rays<R>(*p, R(bottom), n, h, rays, suns, e, R(ar), tlut, mslut, out);                                        \
+  }                                                                                                                  \
+  ORC_EXPORT void orc_surface_rays_##SUFFIX(const AtmParams* p, double bottom, int n, const R* h, const R* rays,     \
+                                            const R* sd, const R* suns, const double* E, double ar, const R* tlut,  \
+                                            const R* mslut, R* out_L, R* out_T) {                                    \
+    R e[3] = {R(E[0]), R(E[1]), R(E[2])};                                                                            \
+    surface_rays<R>(*p, R(bottom), n, h, rays, sd, suns, e, R(ar), tlut, mslut, out_L, out_T);                       \
   }                                                                                                                  \
   ORC_EXPORT int64_t orc_composite_##SUFFIX(                                                                         \
       const AtmParams* p, const CompositeArgs* a, int stride_x, int stride_y, int channels, const R* scene,           \
