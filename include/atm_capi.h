@@ -282,6 +282,79 @@ int atm_mlp_pack_bf16(AtmMlp* mlp, void* stream);
 int atm_mlp_forward(const AtmMlp* mlp, const float* inputs, float* outputs, int64_t n, int32_t precision,
                     void* stream);
 
+/* ---- learned surrogates ----------------------------------------------------
+ * No counterpart in the reference.  Feature vectors, every entry in [-1, 1]:
+ *   0     altitude h of the segment's first point inside the shell,
+ *         2 sqrt(h / top) - 1
+ *   1     view zenith there in the sky-view v mapping (renderer.py
+ *         :482-520), 2 v - 1
+ *   2     sun cosine there in the multi-scattering u mapping (:522-568),
+ *         2 u - 1
+ *   3     cosine of the relative azimuth of view and sun about the vertical
+ *   4, 5  Rayleigh / Mie scale height,
+ *         2 (ln H - ln H_min) / (ln H_max - ln H_min) - 1
+ *   6     aerial only: segment length, 2 ln(clamp(len, 1 m, 2000 km)) /
+ *         ln(2000 km) - 1
+ * Targets: sky (ATM_SURROGATE_SKY) ln(L / E + 1e-7) per channel of the sky
+ * radiance along the ray (the sky-view march, :1208-1302, from the ray's
+ * altitude); aerial (ATM_SURROGATE_AERIAL) the same for the in-scattering of
+ * the segment (the limb integrator, :1667-1755), then its optical depth per
+ * channel (-ln of :1603-1665, capped at 30). */
+#define ATM_SURROGATE_SKY 0
+#define ATM_SURROGATE_AERIAL 1
+
+/* Training samples computed by the plain integrator over the parameter sets
+ * of a batch (their transmittance and multi-scattering LUTs; the sets must
+ * share the planet radius and the shell top).  Features are uniform over the
+ * box above, drawn per sample index from `seed` (sample i does not depend on
+ * n), the parameter set uniform among the batch's.  scale_height_range:
+ * H_R min, max, H_M min, max in metres.  features: n x 6 (sky) or n x 7
+ * (aerial) floats, targets n x 3 or n x 6, device. */
+int atm_surrogate_samples(AtmBatch* batch, int32_t kind, int64_t n, uint64_t seed,
+                          const double scale_height_range[4], float* features, float* targets, void* stream);
+
+/* Networks and error check of atm_composite_surrogate. */
+typedef struct AtmSurrogate {
+  const AtmMlp* aerial;  /* 7 -> 4 x 64 -> 6, packed (atm_mlp_pack_bf16), or null:
+                            plain integrator for every surface pixel            */
+  const AtmMlp* sky;     /* 6 -> 3 x 64 -> 3, packed, or null: sky-view LUT    */
+  double scale_height_range[4];   /* of features 4, 5 (as in training)          */
+  double trained_planet_radius_m; /* the networks' planet; the frame must match */
+  double trained_top_altitude_m;
+  double check_fraction; /* share of MLP pixels re-integrated by the plain path */
+  double aerial_floor;   /* the aerial network's radiance outputs are
+                            ln(L / E + aerial_floor) ...                       */
+  double sky_floor;      /* ... and the sky network's ln(L / E + sky_floor)    */
+  int32_t aerial_per_opacity; /* 1: the aerial output is the in-scattering per
+                            unit of opacity (1 - T), T the segment's
+                            transmittance from the transmittance LUT          */
+  uint32_t seed;         /* picks the checked pixels                            */
+  float* stats;          /* device float[8] accumulated into, or null: checked
+                            pixels, sum and max of their relative error, gated
+                            surface pixels, MLP surface pixels, MLP sky pixels,
+                            sky-view-LUT sky pixels, 0                          */
+} AtmSurrogate;
+
+/* COMPOSITE view of atm_composite with the per-pixel limb integrator replaced
+ * by the aerial network and the sky-view lookup by the sky network (BF16
+ * tensor cores, FP32 accumulation).  Surface pixels keep the plain path's
+ * transmittance (the two-tap LUT ratio of :1603-1665); the network gives
+ * their in-scattering.  The plain integrator remains the
+ * per-pixel fallback where a gate trips (view ray within 0.5 deg of the
+ * limb; for surface pixels the sun within 0.1 of the local horizon at the
+ * segment's start, middle or end; for sky pixels the camera's sun cosine
+ * below 0.1 or the camera above the shell), and re-integrates
+ * check_fraction of the MLP pixels, whose error goes to stats; those pixels
+ * keep the plain result.  Allocates the handle's fallback queue (4 bytes a
+ * pixel) on first use; stream-ordered and capturable afterwards. */
+int atm_composite_surrogate(AtmHandle* handle, const float* scene_hdr, const float* space_hdr,
+                            const int32_t* surface_id, const float* position_view, float* hdr, const AtmImage* image,
+                            double planet_radius_m, double camera_radius_m, const double sun_local[3],
+                            const double solar_irradiance[3], const double sun_disk_radiance[3],
+                            double sun_angular_radius_degrees, const double view_basis[9], double tangent_half_fov,
+                            double star_contrast_start, double star_contrast_end, const AtmSurrogate* surrogate,
+                            void* stream);
+
 /* COMPOSITE view of atm_composite that allocates nothing.  No counterpart in
  * the reference.  For callers that may not call cudaMalloc: an engine or
  * plugin host that owns every device allocation through its own pool, a

@@ -165,6 +165,9 @@ struct AtmHandle {
   double sky_key[6] = {};  // altitude, sun cosine, E[3], angular radius
   bool aerial_available = false;
   AtmState state{};
+  // surrogate composite: fallback queue (width * height entries + 2 counters)
+  uint32_t* queue = nullptr;
+  int sm_count = 0;
 };
 
 namespace {
@@ -290,6 +293,7 @@ ATM_API int atm_destroy(AtmHandle* h) {
     p = nullptr;
   }
   if (h->samples) cudaFree(h->samples);
+  if (h->queue) cudaFree(h->queue);
   delete h;
   return ATM_OK;
 }
@@ -397,21 +401,13 @@ ATM_API int atm_prepare_frame(AtmHandle* h, const float* position_view, const in
   return ATM_OK;
 }
 
-ATM_API int atm_composite(AtmHandle* h, const float* scene_hdr, const float* space_hdr, const int32_t* surface_id,
-                          const float* position_view, float* hdr, const AtmImage* image, double planet_radius_m,
-                          double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
-                          const double sun_disk_radiance[3], double sun_angular_radius_degrees,
-                          const double view_basis[9], double tangent_half_fov, double star_contrast_start,
-                          double star_contrast_end, int32_t diagnostic_view, void* stream) {
-  int rc = check_handle(h);
-  if (rc) return rc;
-  if ((rc = check_image(h, image))) return rc;
-  if (!scene_hdr || !space_hdr || !surface_id || !position_view || !hdr || !sun_local || !solar_irradiance ||
-      !sun_disk_radiance || !view_basis)
-    return fail(ATM_E_INVALID, "null pointer argument to atm_composite");
-  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
-      tangent_half_fov <= 0.0)
-    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+namespace {
+// Scalar arguments of the composite (renderer.py :2210-2238 rounding points).
+atm::CompositeScalars composite_scalars(const AtmHandle* h, double planet_radius_m, double camera_radius_m,
+                                        const double sun_local[3], const double solar_irradiance[3],
+                                        const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                                        const double view_basis[9], double tangent_half_fov,
+                                        double star_contrast_start, double star_contrast_end) {
   const double alt = std::fmax(camera_radius_m - planet_radius_m, 0.0);
   const double sky_alt = h->state.has_sky_snapshot ? h->state.sky_snapshot_altitude_m : alt;  // :2215-2217
   atm::CompositeScalars A{};
@@ -428,6 +424,30 @@ ATM_API int atm_composite(AtmHandle* h, const float* scene_hdr, const float* spa
   to_f32(view_basis, A.right, 3);
   to_f32(view_basis + 3, A.up, 3);
   to_f32(view_basis + 6, A.fwd, 3);
+  A.view = ATM_VIEW_COMPOSITE;
+  return A;
+}
+}  // namespace
+
+ATM_API int atm_composite(AtmHandle* h, const float* scene_hdr, const float* space_hdr, const int32_t* surface_id,
+                          const float* position_view, float* hdr, const AtmImage* image, double planet_radius_m,
+                          double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
+                          const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                          const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                          double star_contrast_end, int32_t diagnostic_view, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!scene_hdr || !space_hdr || !surface_id || !position_view || !hdr || !sun_local || !solar_irradiance ||
+      !sun_disk_radiance || !view_basis)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_composite");
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  atm::CompositeScalars A =
+      composite_scalars(h, planet_radius_m, camera_radius_m, sun_local, solar_irradiance, sun_disk_radiance,
+                        sun_angular_radius_degrees, view_basis, tangent_half_fov, star_contrast_start,
+                        star_contrast_end);
   A.view = diagnostic_view;
   ATM_CUDA(atm::launch_composite(h->dev, layout_of(image), A, scene_hdr, space_hdr, surface_id, position_view,
                                  h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
@@ -519,6 +539,7 @@ struct AtmBatch {
   std::vector<unsigned char> h_jobs;
   std::vector<long long> h_prefix;
   int sm_count = 0;
+  atm::SurrogateSetDev* d_sets = nullptr;  // surrogate sample generation
 };
 
 ATM_API int atm_batch_destroy(AtmBatch* b) {
@@ -529,6 +550,7 @@ ATM_API int atm_batch_destroy(AtmBatch* b) {
   if (b->d_prefix) cudaFree(b->d_prefix);
   if (b->d_ticket) cudaFree(b->d_ticket);
   if (b->d_samples) cudaFree(b->d_samples);
+  if (b->d_sets) cudaFree(b->d_sets);
   delete b;
   return ATM_OK;
 }
@@ -689,6 +711,7 @@ struct AtmMlp {
   float* loss_partial = nullptr;
   size_t loss_floats = 0;
   void* packed = nullptr;
+  bool packed_current = false;  // packed holds the current parameters
   long long step = 0;
   int sm_count = 0;
 };
@@ -763,6 +786,7 @@ ATM_API int atm_mlp_set_params(AtmMlp* m, const float* src_device, void* stream)
   ATM_CUDA(cudaMemcpyAsync(m->params, src_device, size_t(m->shape.n_params) * sizeof(float), cudaMemcpyDeviceToDevice,
                            static_cast<cudaStream_t>(stream)),
            "parameter write");
+  m->packed_current = false;
   return ATM_OK;
 }
 
@@ -797,8 +821,6 @@ int mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n
   ATM_CUDA(atm::launch_mlp_grad(m->shape, m->params, inputs, targets, n, m->partial, m->loss_partial, m->grad, s),
            "MLP forward/backward");
   if (loss_out) {
-    atm::MlpShape one{};
-    one.n_params = 1;
     ATM_CUDA(atm::launch_reduce_partials(m->loss_partial, int(ctas), 1, loss_out, s), "loss reduction");
   }
   return ATM_OK;
@@ -825,6 +847,7 @@ ATM_API int atm_mlp_train_step(AtmMlp* m, const float* inputs, const float* targ
   int rc = mlp_gradient(m, inputs, targets, n, loss_out, s);
   if (rc) return rc;
   m->step += 1;
+  m->packed_current = false;
   ATM_CUDA(atm::launch_adam(m->params, m->grad, m->m1, m->m2, m->shape.n_params, lr, beta1, beta2, eps, m->step, s),
            "Adam update");
   return ATM_OK;
@@ -834,6 +857,7 @@ ATM_API int atm_mlp_pack_bf16(AtmMlp* m, void* stream) {
   if (!m) return fail(ATM_E_INVALID, "null AtmMlp");
   ATM_CUDA(atm::launch_mlp_pack_bf16(m->shape, m->params, m->packed, static_cast<cudaStream_t>(stream)),
            "BF16 packing");
+  m->packed_current = true;
   return ATM_OK;
 }
 
@@ -848,6 +872,134 @@ ATM_API int atm_mlp_forward(const AtmMlp* m, const float* inputs, float* outputs
              "MLP forward (BF16 tensor cores)");
   else
     return fail(ATM_E_INVALID, "precision must be 0 (FP32) or 1 (BF16)");
+  return ATM_OK;
+}
+
+// ---- learned surrogates ----------------------------------------------------
+namespace {
+bool valid_range(const double* r) {
+  return r && std::isfinite(r[0]) && std::isfinite(r[1]) && std::isfinite(r[2]) && std::isfinite(r[3]) &&
+         r[0] > 0.0 && r[1] > r[0] && r[2] > 0.0 && r[3] > r[2];
+}
+// Feature 4 or 5 of a scale height: 2 (ln H - ln lo) / (ln hi - ln lo) - 1.
+float log_feature(double H, double lo, double hi) {
+  return float(2.0 * (std::log(H) - std::log(lo)) / (std::log(hi) - std::log(lo)) - 1.0);
+}
+bool mlp_is(const AtmMlp* m, int n_in, int n_hidden, int n_out) {
+  return m->shape.n_in == n_in && m->shape.n_out == n_out && m->shape.n_layers == n_hidden + 1;
+}
+}  // namespace
+
+ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t seed,
+                                  const double scale_height_range[4], float* features, float* targets,
+                                  void* stream) {
+  if (!b || !features || !targets || n < 1) return fail(ATM_E_INVALID, "invalid surrogate sample arguments");
+  if (kind != ATM_SURROGATE_SKY && kind != ATM_SURROGATE_AERIAL) return fail(ATM_E_INVALID, "unknown kind %d", kind);
+  if (!valid_range(scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
+  const int n_sets = int(b->params.size());
+  for (int i = 1; i < n_sets; ++i)
+    if (b->radius[i] != b->radius[0] || b->params[i].top_altitude_m != b->params[0].top_altitude_m)
+      return fail(ATM_E_INVALID, "surrogate sample sets must share planet radius and shell top");
+  std::vector<atm::SurrogateSetDev> sets(n_sets);
+  for (int i = 0; i < n_sets; ++i) {
+    const AtmParams& p = b->params[i];
+    const double* r = scale_height_range;
+    if (p.rayleigh_scale_height_m < r[0] || p.rayleigh_scale_height_m > r[1] || p.mie_scale_height_m < r[2] ||
+        p.mie_scale_height_m > r[3])
+      return fail(ATM_E_INVALID, "set %d has scale heights outside the feature range", i);
+    sets[i].P = b->dev[i];
+    sets[i].tlut = b->tlut[i];
+    sets[i].mslut = b->mslut[i];
+    sets[i].bottom = float(b->radius[i]);
+    sets[i].lhr_n = log_feature(p.rayleigh_scale_height_m, r[0], r[1]);
+    sets[i].lhm_n = log_feature(p.mie_scale_height_m, r[2], r[3]);
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (!b->d_sets) ATM_CUDA(cudaMalloc(&b->d_sets, sizeof(atm::SurrogateSetDev) * 1024), "sample set table");
+  ATM_CUDA(cudaMemcpyAsync(b->d_sets, sets.data(), sizeof(atm::SurrogateSetDev) * n_sets, cudaMemcpyHostToDevice, s),
+           "sample set upload");
+  float ef[3];
+  to_f32(b->E, ef, 3);
+  ATM_CUDA(atm::launch_gen_samples(b->d_sets, n_sets, kind, n, seed, ef, float(b->ar_rad), features, targets,
+                                   b->d_samples, s),
+           "surrogate samples");
+  // the table is read by the launch: keep the host copy alive until it ran
+  ATM_CUDA(cudaStreamSynchronize(s), "surrogate samples");
+  return ATM_OK;
+}
+
+ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const float* space_hdr,
+                                    const int32_t* surface_id, const float* position_view, float* hdr,
+                                    const AtmImage* image, double planet_radius_m, double camera_radius_m,
+                                    const double sun_local[3], const double solar_irradiance[3],
+                                    const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                                    const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                                    double star_contrast_end, const AtmSurrogate* sg, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!scene_hdr || !space_hdr || !surface_id || !position_view || !hdr || !sun_local || !solar_irradiance ||
+      !sun_disk_radiance || !view_basis || !sg)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_composite_surrogate");
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  if (int64_t(image->width) * image->height > (int64_t(1) << 30))
+    return fail(ATM_E_INVALID, "frame larger than 2^30 pixels");
+  if (!valid_range(sg->scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
+  if (!(sg->check_fraction >= 0.0 && sg->check_fraction <= 1.0))
+    return fail(ATM_E_INVALID, "check_fraction must be in [0, 1]");
+  if (!(sg->aerial_floor > 0.0 && sg->aerial_floor < 1.0 && sg->sky_floor > 0.0 && sg->sky_floor < 1.0))
+    return fail(ATM_E_INVALID, "radiance floors must be in (0, 1)");
+  if (sg->aerial || sg->sky) {
+    if (std::fabs(sg->trained_planet_radius_m - planet_radius_m) > 1.0 ||
+        std::fabs(sg->trained_top_altitude_m - h->params.top_altitude_m) > 1.0)
+      return fail(ATM_E_INVALID, "the networks were trained for another planet radius or shell top");
+  }
+  atm::SurrogateNets nets{};
+  if (sg->aerial) {
+    if (!mlp_is(sg->aerial, atm::kSurrogateApIn, atm::kSurrogateApHidden, atm::kSurrogateApOut))
+      return fail(ATM_E_INVALID, "aerial network must be 7 -> 4 x 64 -> 6");
+    if (!sg->aerial->packed_current) return fail(ATM_E_STATE, "aerial network not packed (atm_mlp_pack_bf16)");
+    nets.ap = static_cast<const unsigned char*>(sg->aerial->packed);
+    nets.ap_bytes = int(atm::mlp_bf16_bytes(sg->aerial->shape));
+  }
+  if (sg->sky) {
+    if (!mlp_is(sg->sky, atm::kSurrogateSkyIn, atm::kSurrogateSkyHidden, atm::kSurrogateSkyOut))
+      return fail(ATM_E_INVALID, "sky network must be 6 -> 3 x 64 -> 3");
+    if (!sg->sky->packed_current) return fail(ATM_E_STATE, "sky network not packed (atm_mlp_pack_bf16)");
+    nets.sky = static_cast<const unsigned char*>(sg->sky->packed);
+    nets.sky_bytes = int(atm::mlp_bf16_bytes(sg->sky->shape));
+  }
+  if (nets.ap_bytes % 16 || nets.sky_bytes % 16) return fail(ATM_E_STATE, "packed network size not a multiple of 16");
+  const double* r = sg->scale_height_range;
+  nets.lhr_n = log_feature(h->params.rayleigh_scale_height_m, r[0], r[1]);
+  nets.lhm_n = log_feature(h->params.mie_scale_height_m, r[2], r[3]);
+  nets.floor = float(sg->aerial_floor);
+  nets.sky_floor = float(sg->sky_floor);
+  nets.per_opacity = sg->aerial_per_opacity != 0;
+  if (!h->queue) {
+    const size_t cap = size_t(h->width) * size_t(h->height);
+    ATM_CUDA(cudaMalloc(&h->queue, (cap + 2) * sizeof(uint32_t)), "fallback queue");
+    int dev = 0;
+    ATM_CUDA(cudaGetDevice(&dev), "device query");
+    ATM_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev), "device query");
+  }
+  atm::SurrogateQueue Q{};
+  Q.count = h->queue;
+  Q.items = h->queue + 2;
+  Q.stats = sg->stats;
+  Q.check_fraction = float(sg->check_fraction);
+  Q.seed = sg->seed;
+  const atm::CompositeScalars A =
+      composite_scalars(h, planet_radius_m, camera_radius_m, sun_local, solar_irradiance, sun_disk_radiance,
+                        sun_angular_radius_degrees, view_basis, tangent_half_fov, star_contrast_start,
+                        star_contrast_end);
+  ATM_CUDA(atm::launch_composite_surrogate(h->dev, layout_of(image), A, scene_hdr, space_hdr, surface_id,
+                                           position_view, h->lut[ATM_LUT_TRANSMITTANCE],
+                                           h->lut[ATM_LUT_MULTI_SCATTERING], h->lut[ATM_LUT_SKY_VIEW], nets, Q, hdr,
+                                           h->samples, h->sm_count, static_cast<cudaStream_t>(stream)),
+           "surrogate composite");
   return ATM_OK;
 }
 

@@ -223,6 +223,122 @@ __device__ __forceinline__ void aerial_prefix(const DevParams& P, float h, float
   }
   valid = v && end > start;
 }
+
+// ---- per-ray geometry ---------------------------------------------------------
+// r(t)^2 - R^2 along a camera ray, t the distance from the camera at
+// (0, R + h0, 0), is the quadratic q(u) = (q0 + q1 u) + u^2, u = t - t0.
+// Cameras within half a planet radius of the ground use the reference's own
+// coefficients about the camera (t0 = 0: _altitude_on_ray :237-262,
+// _shell_roots_from_altitude :264-301).  Farther out, every sample is far
+// from the camera and those terms, ~r_cam^2, cancel down to r^2 - R^2 ~ R H:
+// float keeps no digit of a grazing ray's altitude (a 50 km planet seen from
+// 1800 km: 10 m altitude errors against a 300 m Mie scale height, the
+// reference's own float result then off by tens of percent).  Such rays
+// pivot at the closest approach t_c = -(R + h0) cos v, where q0 = r_c^2 - R^2
+// and the shell discriminants are formed in FP64 from the ray's sine, once
+// per ray.
+struct RayGeom {
+  float h0, cosv;    // camera altitude, view cosine
+  float t0, q0, q1;  // pivot and coefficients of q
+  float tc;          // closest-approach distance
+  float disc_top, disc_ground;  // far: (shell radius)^2 - r_c^2 of the top and the ground
+  bool far;          // pivot at t_c (far_camera)
+};
+// Camera far enough for the closest-approach pivot: above the shell and more
+// than half a planet radius up.
+__device__ __forceinline__ bool far_camera(const DevParams& P, float bottom, float h0) {
+  return h0 > P.top && h0 > 0.5f * bottom;
+}
+__device__ __forceinline__ RayGeom ray_geom(const DevParams& P, float bottom, float h0, float cosv, float sinv) {
+  RayGeom G;
+  G.h0 = h0;
+  G.cosv = cosv;
+  const float a = mx(h0, 0.0f);
+  G.far = far_camera(P, bottom, a);
+  if (!G.far) {
+    const float orad = bottom + a;
+    G.t0 = 0.0f;
+    G.q0 = a * (2.0f * bottom + a);
+    G.q1 = 2.0f * orad * cosv;
+    G.tc = -orad * cosv;
+    G.disc_top = G.disc_ground = 0.0f;
+  } else {
+    const double b = bottom, o = double(bottom) + double(a), top = P.top;
+    const double rc = o * double(sinv);
+    const double K = (rc - b) * (rc + b);
+    G.t0 = G.tc = float(-o * double(cosv));
+    G.q0 = float(K);
+    G.q1 = 0.0f;
+    G.disc_top = float(top * (2.0 * b + top) - K);
+    G.disc_ground = float(-K);
+  }
+  return G;
+}
+// Altitude at distance t along the ray (the reference's form of :237-262).
+__device__ __forceinline__ float altitude_at(const RayGeom& G, float t, float bottom) {
+  const float u = t - G.t0;
+  const float delta = (G.q0 + G.q1 * u) + u * u;
+  const float len = fsqrt(mx(bottom * bottom + delta, 0.0f));
+  return fdiv(delta, mx(len + bottom, 1.0f));
+}
+// Cosine between the ray and the local vertical at distance t, r = R + h.
+__device__ __forceinline__ float vertical_cosine_at(const RayGeom& G, float t, float radius) {
+  return (t - G.tc) * frcp(mx(radius, 1.0f));
+}
+// Roots of the ray with the sphere of radius bottom + shell.
+__device__ __forceinline__ void shell_roots_g(const RayGeom& G, float shell, float bottom, float& nearv, float& farv,
+                                              bool& hit) {
+  if (!G.far) {
+    shell_roots(G.h0, G.cosv, shell, bottom, nearv, farv, hit);
+    return;
+  }
+  const float disc = shell > 0.0f ? G.disc_top : G.disc_ground;  // shell is the top or 0
+  hit = disc >= 0.0f;
+  nearv = kLargeF;
+  farv = -kLargeF;
+  if (hit) {
+    const float root = sqrtf(disc);
+    nearv = G.tc - root;
+    farv = G.tc + root;
+  }
+}
+// _atmosphere_segment_from_altitude :303-340 on a ray's geometry.
+__device__ __forceinline__ void segment_of(const DevParams& P, const RayGeom& G, float bottom, float& start,
+                                           float& end, bool& valid, bool& ground) {
+  if (!G.far) {
+    segment_from_altitude(P, G.h0, G.cosv, bottom, start, end, valid, ground);
+    return;
+  }
+  float on, of;
+  bool oh;
+  shell_roots_g(G, P.top, bottom, on, of, oh);
+  start = mx(on, 0.0f);
+  end = of;
+  valid = oh && end > start;
+  ground = false;
+  float gn, gf;
+  bool gh;
+  shell_roots_g(G, 0.0f, bottom, gn, gf, gh);
+  if (valid && gh) {
+    float gd = kLargeF;
+    if (gn > start + 1.0e-3f)
+      gd = gn;
+    else if (gf > start + 1.0e-3f)
+      gd = gf;
+    if (gd < end) {
+      end = gd;
+      ground = true;
+    }
+  }
+}
+// _aerial_prefix_segment_from_altitude :376-395 on a ray's geometry.
+__device__ __forceinline__ void aerial_prefix_of(const DevParams& P, const RayGeom& G, float bottom, float& start,
+                                                 float& end, bool& valid) {
+  bool v, g;
+  segment_of(P, G, bottom, start, end, v, g);
+  if (v && !g && G.tc > start && G.tc < end) end = G.tc;
+  valid = v && end > start;
+}
 __device__ __forceinline__ float distance_to_top(const DevParams& P, float h, float cosv, float bottom) {
   float radius = bottom + mx(h, 0.0f);
   float delta = (P.top - h) * ((2.0f * bottom + P.top) + h);
@@ -499,20 +615,23 @@ __device__ __forceinline__ void segment_integral(f3 ext, float step, f3& tr, f3&
 // Per-ray constants of the constant-source samples (everything of
 // _scattering_source :818-856 that does not depend on the sample).
 struct RaySource {
-  float o_y;   // origin (0, o_y, 0), o_y = bottom + h0
-  float h0;    // origin altitude
-  float ray_y;
-  float o_sun; // o_y * sun.y  (origin . sun)
-  float r_sun; // ray . sun
-  f3 ER, EM;   // E * beta_R * phase_R, E * beta_Ms * phase_M
+  float t0, q0, q1;  // the ray's altitude quadratic (RayGeom)
+  float s0;          // (origin + t0 ray) . sun
+  float r_sun;       // ray . sun
+  f3 ER, EM;         // E * beta_R * phase_R, E * beta_Ms * phase_M
 };
-__device__ __forceinline__ RaySource make_ray_source(const DevParams& P, const Frame& F, float o_y, float h0, f3 ray) {
+__device__ __forceinline__ RaySource make_ray_source(const DevParams& P, const Frame& F, const RayGeom& G, f3 ray) {
   RaySource R;
-  R.o_y = o_y;
-  R.h0 = h0;
-  R.ray_y = ray.y;
-  R.o_sun = o_y * F.sun.y;
+  R.t0 = G.t0;
+  R.q0 = G.q0;
+  R.q1 = G.q1;
   R.r_sun = dot(ray, F.sun);
+  const float o_y = F.bottom + mx(G.h0, 0.0f);
+  if (G.far)
+    R.s0 = float(double(o_y) * double(F.sun.y) + double(G.t0) * (double(ray.x) * F.sun.x + double(ray.y) * F.sun.y +
+                                                                  double(ray.z) * F.sun.z));
+  else
+    R.s0 = o_y * F.sun.y;
   const float cr = clampf(R.r_sun, -1.0f, 1.0f);
   R.ER = F.E * arr3(P.beta_r) * rayleigh_phase(P, cr);
   R.EM = F.E * arr3(P.beta_ms) * mie_phase(P, cr);
@@ -522,22 +641,24 @@ __device__ __forceinline__ RaySource make_ray_source(const DevParams& P, const F
 // One constant-source segment [start, end] of the ray: _scattering_segment
 // :858-899 with _scattering_source :818-856.  Returns (L, T) and the finite
 // disk visibility at the sample.  The sample's radius is bottom + h (its
-// altitude on the ray) and its sun cosine (o . sun + t ray . sun) / radius;
-// the reference forms the point first - same quantities, rounding differs in
-// the last bits.
+// altitude on the ray) and its sun cosine (p(t0) . sun + (t - t0) ray . sun) /
+// radius; the reference forms the point first - same quantities, rounding
+// differs in the last bits.
 template <bool kMultiple>
 __device__ __forceinline__ Seg source_segment(const DevParams& P, const Frame& F, const RaySource& R, float start,
                                               float end, float& vis) {
   float step = mx(end - start, 0.0f);
   float dist = (start + end) * 0.5f;
-  float h = altitude_on_ray(R.h0, R.ray_y, dist, F.bottom);
+  const float u = dist - R.t0;
+  const float delta = (R.q0 + R.q1 * u) + u * u;
+  float h = fdiv(delta, mx(fsqrt(mx(F.bottom * F.bottom + delta, 0.0f)) + F.bottom, 1.0f));
   Density d = density(P, h);
   f3 ext = extinction_of(P, d);
   Seg s;
   f3 integ;
   segment_integral(ext, step, s.T, integ);
   const float radius = F.bottom + h;
-  const float sc = (R.o_sun + dist * R.r_sun) * frcp(mx(radius, 1.0f));
+  const float sc = (R.s0 + u * R.r_sun) * frcp(mx(radius, 1.0f));
   Horizon H = horizon_at(h, F.bottom);
   f3 st = sample_solar_t(P, F, h, sc, H, vis);
   f3 src = st * (R.ER * d.r + R.EM * d.m);

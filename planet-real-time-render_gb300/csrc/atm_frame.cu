@@ -43,8 +43,19 @@ __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayou
     f3 radial = pp / mx(radius, 1.0f);
     float sd = norm(lp);
     f3 lr = lp / mx(sd, 1.0f);
-    float h = altitude_on_ray(cam_alt, lr.y, sd, bottom);
-    float sc = dot(radial, sun);
+    float h, sc;
+    if (!far_camera(P, bottom, cam_alt)) {
+      h = altitude_on_ray(cam_alt, lr.y, sd, bottom);
+      sc = dot(radial, sun);
+    } else {  // camera above the shell: pivot at the closest approach (RayGeom)
+      const RayGeom G = camera_ray_geom(P, bottom, cam_alt, lr);
+      h = altitude_at(G, sd, bottom);
+      // p . sun = o . sun + t_c lr . sun + (t - t_c) lr . sun, the first two in
+      // FP64 (the point's own coordinates cancel like its altitude)
+      const double s0 = (double(bottom) + double(cam_alt)) * double(sun.y) +
+                        double(G.tc) * (double(lr.x) * sun.x + double(lr.y) * sun.y + double(lr.z) * sun.z);
+      sc = (float(s0) + (sd - G.tc) * dot(lr, sun)) * frcp(bottom + h);
+    }
     Horizon H = horizon_at(h, bottom);
     float vis;
     st = sample_solar_t(P, F, h, sc, H, vis);
@@ -76,11 +87,12 @@ __global__ void __launch_bounds__(256, 3) k_composite(DevParams P, ImageLayout L
     PixelRay pr = pixel_ray(L, A, x, y);
     f3 color = ld3(scene + o);
     if (sid[e] >= 0) {
+      const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
       float sd = norm(ld3(pos + o));
       float start, end;
-      if (surface_interval(P, A.cam_alt, pr.ray.y, A.bottom, sd, start, end)) {
-        f3 scat = integrate_surface(P, F, A.cam_alt, pr.ray, start, end, samples);
-        f3 tr = surface_segment_t(P, F, A.cam_alt, pr.ray, start, end);
+      if (surface_interval(P, G, A.bottom, sd, start, end)) {
+        f3 scat = integrate_surface(P, F, G, pr.ray, start, end, samples);
+        f3 tr = surface_segment_t(P, F, G, pr.ray, start, end);
         color = scat + color * tr;
       }
     } else {
@@ -132,6 +144,7 @@ __global__ void __launch_bounds__(256, 3) k_composite_views(DevParams P, ImageLa
     const size_t o = e * L.channels;
     Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
     PixelRay pr = pixel_ray(L, A, x, y);
+    const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
     const bool surface = sid[e] >= 0;
     f3 color = ld3(scene + o);
     switch (A.view) {
@@ -139,7 +152,7 @@ __global__ void __launch_bounds__(256, 3) k_composite_views(DevParams P, ImageLa
         color = sample_sky_view(P, svlut, pr.ray, F.sun, A.sky_alt, A.bottom);
         break;
       case ATM_VIEW_CAMERA_TRANSMITTANCE:
-        color = camera_t(P, F, A.cam_alt, pr.ray);
+        color = camera_t(P, F, G, pr.ray);
         break;
       case ATM_VIEW_TRANSMITTANCE_LUT: {
         int lx = min(int(pr.su * float(P.t_w)), P.t_w - 1);
@@ -157,8 +170,8 @@ __global__ void __launch_bounds__(256, 3) k_composite_views(DevParams P, ImageLa
       case ATM_VIEW_AERIAL_DIRECT_ONLY: {
         color = splat(0.0f);
         float start, end;
-        if (surface && surface_interval(P, A.cam_alt, pr.ray.y, A.bottom, norm(ld3(pos + o)), start, end))
-          color = integrate_surface(P, F, A.cam_alt, pr.ray, start, end, samples);
+        if (surface && surface_interval(P, G, A.bottom, norm(ld3(pos + o)), start, end))
+          color = integrate_surface(P, F, G, pr.ray, start, end, samples);
         break;
       }
       case ATM_VIEW_AERIAL_FROXEL_ONLY: {
@@ -166,7 +179,7 @@ __global__ void __launch_bounds__(256, 3) k_composite_views(DevParams P, ImageLa
         if (surface) {
           float s, e2;
           bool valid;
-          aerial_prefix(P, A.cam_alt, pr.ray.y, A.bottom, s, e2, valid);
+          aerial_prefix_of(P, G, A.bottom, s, e2, valid);
           float df = 0.0f;
           if (valid) df = clampf((norm(ld3(pos + o)) - s) / mx(e2 - s, 1.0f), 0.0f, 1.0f);
           color = sample_aerial_field(P, aplut, pr.su, pr.sv, df);
@@ -181,8 +194,8 @@ __global__ void __launch_bounds__(256, 3) k_composite_views(DevParams P, ImageLa
         if (surface) {
           float start, end;
           color = splat(1.0f);
-          if (surface_interval(P, A.cam_alt, pr.ray.y, A.bottom, norm(ld3(pos + o)), start, end))
-            color = surface_segment_t(P, F, A.cam_alt, pr.ray, start, end);
+          if (surface_interval(P, G, A.bottom, norm(ld3(pos + o)), start, end))
+            color = surface_segment_t(P, F, G, pr.ray, start, end);
         }
         break;
       }
@@ -262,11 +275,12 @@ __global__ void __launch_bounds__(256, 3) k_composite_tiles(DevParams P, ImageLa
     PixelRay pr = pixel_ray(L, A, x, y);
     f3 color = ld3(scene + o);
     if (sid[e] >= 0) {
+      const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
       float sd = norm(ld3(pos + o));
       float start, end;
-      if (surface_interval(P, A.cam_alt, pr.ray.y, A.bottom, sd, start, end)) {
-        f3 scat = integrate_surface(P, F, A.cam_alt, pr.ray, start, end, samples);
-        f3 tr = surface_segment_t(P, F, A.cam_alt, pr.ray, start, end);
+      if (surface_interval(P, G, A.bottom, sd, start, end)) {
+        f3 scat = integrate_surface(P, F, G, pr.ray, start, end, samples);
+        f3 tr = surface_segment_t(P, F, G, pr.ray, start, end);
         color = scat + color * tr;
       }
     } else {

@@ -75,18 +75,52 @@ __device__ __forceinline__ void shadow_roots(f3 o, f3 d, f3 sun, float bottom, f
     v1 = dot(o + d * r1, sun) < 0.0f;
   }
 }
+// The same roots in FP64 for a camera above the shell, whose distance to the
+// shadow cylinder's axis makes hl^2 and quad c cancel in float.  The origin
+// is (0, o_y, 0) with o_y = bottom + h0 formed in double.
+__device__ __forceinline__ void shadow_roots_far(float h0, f3 df, f3 sf, float bottom, float& r0, float& r1,
+                                                 bool& v0, bool& v1) {
+  const double oy = double(bottom) + double(h0), b = bottom;
+  const double dx = df.x, dy = df.y, dz = df.z, sx = sf.x, sy = sf.y, sz = sf.z;
+  const double os = oy * sy, ds = dx * sx + dy * sy + dz * sz;
+  const double opx = -sx * os, opy = oy - sy * os, opz = -sz * os;
+  const double rpx = dx - sx * ds, rpy = dy - sy * ds, rpz = dz - sz * ds;
+  const double quad = rpx * rpx + rpy * rpy + rpz * rpz;
+  const double hl = opx * rpx + opy * rpy + opz * rpz;
+  const double pl = sqrt(opx * opx + opy * opy + opz * opz);
+  const double c = (pl - b) * (pl + b);
+  const double disc = hl * hl - quad * c;
+  r0 = 0.0f;
+  r1 = 0.0f;
+  v0 = false;
+  v1 = false;
+  if (quad > 1.0e-8 && disc >= 0.0) {
+    const double sr = sqrt(disc);
+    const double t0 = (-hl - sr) / quad, t1 = (-hl + sr) / quad;
+    r0 = float(t0);
+    r1 = float(t1);
+    v0 = os + t0 * ds < 0.0;
+    v1 = os + t1 * ds < 0.0;
+  }
+}
+
+// Geometry of a camera ray (sine from the horizontal components).
+__device__ __forceinline__ RayGeom camera_ray_geom(const DevParams& P, float bottom, float h0, f3 ray) {
+  return ray_geom(P, bottom, h0, ray.y, sqrtf(ray.x * ray.x + ray.z * ray.z));
+}
 
 // _integrate_surface_scattering :1667-1755 (with :901-1032).  `start`/`end`
 // are the shell-clipped interval; the caller has checked it is non-empty.
-__device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame& F, float cam_alt, f3 ray,
+__device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame& F, const RayGeom& G, f3 ray,
                                                 float start, float end, uint32_t& samples) {
-  const float o_y = F.bottom + cam_alt;
-  const f3 origin = mk(0.0f, o_y, 0.0f);
   float sr0, sr1;
   bool sv0, sv1;
-  shadow_roots(origin, ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
-  const RaySource rs = make_ray_source(P, F, o_y, cam_alt, ray);
-  const RayWarp rw = make_warp(-(o_y * ray.y), start, end);
+  if (G.far)
+    shadow_roots_far(G.h0, ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
+  else
+    shadow_roots(mk(0.0f, F.bottom + G.h0, 0.0f), ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
+  const RaySource rs = make_ray_source(P, F, G, ray);
+  const RayWarp rw = make_warp(G.tc, start, end);
   const bool roots = sv0 || sv1;
   const int n = P.limb_steps;
   const int nsub = P.substeps;
@@ -132,31 +166,43 @@ __device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame&
 }
 
 // _surface_segment_transmittance :1603-1665 on an already clipped interval.
-__device__ __forceinline__ f3 surface_segment_t(const DevParams& P, const Frame& F, float cam_alt, f3 ray,
+__device__ __forceinline__ f3 surface_segment_t(const DevParams& P, const Frame& F, const RayGeom& G, f3 ray,
                                                 float start, float end) {
-  const f3 origin = mk(0.0f, F.bottom + cam_alt, 0.0f);
-  f3 np = origin + ray * start;
-  f3 sp = origin + ray * end;
-  f3 rr = -ray;
-  f3 nrad = np / mx(norm(np), 1.0f);
-  f3 srad = sp / mx(norm(sp), 1.0f);
-  float na = altitude_on_ray(cam_alt, ray.y, start, F.bottom);
-  float sa = altitude_on_ray(cam_alt, ray.y, end, F.bottom);
-  f3 s2t = sample_t(P, F, sa, dot(srad, rr));
-  f3 n2t = sample_t(P, F, na, dot(nrad, rr));
+  f3 s2t, n2t;
+  if (!G.far) {
+    const float cam_alt = G.h0;
+    const f3 origin = mk(0.0f, F.bottom + cam_alt, 0.0f);
+    f3 np = origin + ray * start;
+    f3 sp = origin + ray * end;
+    f3 rr = -ray;
+    f3 nrad = np / mx(norm(np), 1.0f);
+    f3 srad = sp / mx(norm(sp), 1.0f);
+    float na = altitude_on_ray(cam_alt, ray.y, start, F.bottom);
+    float sa = altitude_on_ray(cam_alt, ray.y, end, F.bottom);
+    s2t = sample_t(P, F, sa, dot(srad, rr));
+    n2t = sample_t(P, F, na, dot(nrad, rr));
+  } else {  // radial . (-ray) = -(t - t_c) / r
+    const float na = altitude_at(G, start, F.bottom), sa = altitude_at(G, end, F.bottom);
+    s2t = sample_t(P, F, sa, -vertical_cosine_at(G, end, F.bottom + sa));
+    n2t = sample_t(P, F, na, -vertical_cosine_at(G, start, F.bottom + na));
+  }
   return vclamp(s2t / vmax(n2t, 1.0e-6f), 0.0f, 1.0f);
 }
 
 // _camera_transmittance :1788-1825
-__device__ __forceinline__ f3 camera_t(const DevParams& P, const Frame& F, float cam_alt, f3 ray) {
+__device__ __forceinline__ f3 camera_t(const DevParams& P, const Frame& F, const RayGeom& G, f3 ray) {
   float s, e;
   bool valid, ground;
-  segment_from_altitude(P, cam_alt, ray.y, F.bottom, s, e, valid, ground);
+  segment_of(P, G, F.bottom, s, e, valid, ground);
   if (!valid) return splat(1.0f);
   if (ground) return splat(0.0f);
-  f3 entry = mk(0.0f, F.bottom + cam_alt, 0.0f) + ray * s;
+  if (G.far) {
+    const float ea = altitude_at(G, s, F.bottom);
+    return sample_t(P, F, ea, vertical_cosine_at(G, s, F.bottom + ea));
+  }
+  f3 entry = mk(0.0f, F.bottom + G.h0, 0.0f) + ray * s;
   f3 radial = entry / mx(norm(entry), 1.0f);
-  float ea = altitude_on_ray(cam_alt, ray.y, s, F.bottom);
+  float ea = altitude_on_ray(G.h0, ray.y, s, F.bottom);
   return sample_t(P, F, ea, dot(radial, ray));
 }
 
@@ -174,11 +220,11 @@ __device__ __forceinline__ f3 sample_sky_view(const DevParams& P, const float4* 
 }
 
 // Shell clip shared by the scattering integral and the transmittance ratio.
-__device__ __forceinline__ bool surface_interval(const DevParams& P, float cam_alt, float ray_y, float bottom,
+__device__ __forceinline__ bool surface_interval(const DevParams& P, const RayGeom& G, float bottom,
                                                  float surface_distance, float& start, float& end) {
   float on, of;
   bool oh;
-  shell_roots(cam_alt, ray_y, P.top, bottom, on, of, oh);
+  shell_roots_g(G, P.top, bottom, on, of, oh);
   start = mx(on, 0.0f);
   end = mn(surface_distance, of);
   return oh && end > start;
@@ -187,7 +233,7 @@ __device__ __forceinline__ bool surface_interval(const DevParams& P, float cam_a
 // Sky branch of the COMPOSITE view (:1883-1940) given the sky radiance.
 __device__ __forceinline__ f3 composite_sky_with(const DevParams& P, const Frame& F, const CompositeScalars& A, f3 sky,
                                                  f3 ray, f3 color, f3 space, float height) {
-  f3 tr = camera_t(P, F, A.cam_alt, ray);
+  f3 tr = camera_t(P, F, camera_ray_geom(P, F.bottom, A.cam_alt, ray), ray);
   f3 star = space * tr;
   const f3 lw = mk(0.2126f, 0.7152f, 0.0722f);
   float contrast = dot(star, lw) / mx(dot(sky, lw), 1.0e-5f);

@@ -86,6 +86,8 @@ cudaError_t launch_mlp_forward_bf16(const MlpShape& m, const void* packed, const
 constexpr float kSurrogateFloor = 1.0e-7f;
 constexpr float kSurrogateMaxLength = 2.0e6f;
 constexpr float kSurrogateMaxDepth = 30.0f;
+constexpr int kSurrogateApIn = 7, kSurrogateApOut = 6, kSurrogateApHidden = 4;
+constexpr int kSurrogateSkyIn = 6, kSurrogateSkyOut = 3, kSurrogateSkyHidden = 3;
 struct SurrogateSetDev {
   DevParams P;
   const float4* tlut;
@@ -96,17 +98,34 @@ struct SurrogateSetDev {
 struct SurrogateNets {
   const unsigned char* ap;   // packed BF16 aerial network (7 -> 4x64 -> 6) or null
   const unsigned char* sky;  // packed BF16 sky network (6 -> 3x64 -> 3) or null
-  int ap_bytes, sky_bytes;
-  float lhr_n, lhm_n;
+  int ap_bytes, sky_bytes;   // multiples of 16
+  float lhr_n, lhm_n;        // the frame's normalised log scale heights
+  float floor, sky_floor;    // outputs are ln(L / E + floor)
+  int per_opacity;           // aerial output is the in-scattering per unit of (1 - T)
 };
+// Pixels the surrogate composite hands to the plain integrator: entry =
+// kind << 30 | (y * width + x).  count and next are reset by each frame.
+enum : uint32_t { kQueueSurface = 0u, kQueueSurfaceCheck = 1u, kQueueSkyCheck = 2u };
+struct SurrogateQueue {
+  uint32_t* items;    // capacity = width * height
+  uint32_t* count;    // [0] = entries, [1] = fallback ticket
+  float* stats;       // null or kSurrogateStats floats, accumulated
+  float check_fraction;
+  uint32_t seed;
+};
+// stats: checked pixels, sum of their relative errors, max relative error,
+// gated surface pixels (plain integrator), MLP surface pixels, MLP sky
+// pixels, gated sky pixels (sky-view LUT)
+constexpr int kSurrogateStats = 8;
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
                                const float E[3], float ar, float* features, float* targets,
                                unsigned long long* counter, cudaStream_t s);
+size_t surrogate_smem_bytes(const SurrogateNets& nets);
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,
                                        const float4* tlut, const float4* mslut, const float4* svlut,
-                                       const SurrogateNets& nets, unsigned seed, float check_fraction, float* hdr,
-                                       float* stats, unsigned long long* counter, cudaStream_t s);
+                                       const SurrogateNets& nets, const SurrogateQueue& Q, float* hdr,
+                                       unsigned long long* counter, int sm_count, cudaStream_t s);
 
 // atm_composite_noalloc: the per-device address of the file-scope tile
 // scratch (looked up on the first call on each device), its capacity in

@@ -52,22 +52,32 @@ __device__ __forceinline__ uint32_t sky_view_texel(const DevParams& P, const Fra
   const int lane = threadIdx.x & 31;
   const float bottom = F.bottom;
   const float sh = mx(cam_alt, 0.0f);
-  const float o_y = bottom + sh;
   float az = (float(x) + 0.5f) / float(P.sv_w) * kPiF;
   float vv = (float(y) + 0.5f) / float(P.sv_h);
   float zen = sky_v_to_zenith(vv, sky_horizon_zenith(sh, bottom));
   float vs, vc, saz, caz;
   sincosf(zen, &vs, &vc);
+  if (far_camera(P, bottom, sh) && vv >= 0.5f) {
+    // below the horizon seen from above the shell: the nadir angle
+    // pi - zen = (pi - hz)(1 - local^2) of the same mapping keeps the digits
+    // that zen itself, near pi, loses (pi - hz = acos(rho / r))
+    const float local = 2.0f * vv - 1.0f;
+    const float nadir = acosf(clampf(shell_rho(sh, bottom) / mx(bottom + sh, 1.0f), 0.0f, 1.0f)) *
+                        (1.0f - local * local);
+    sincosf(nadir, &vs, &vc);
+    vc = -vc;
+  }
   sincosf(az, &saz, &caz);
   f3 ray = mk(vs * caz, vc, vs * saz);
+  const RayGeom G = ray_geom(P, bottom, sh, vc, vs);
   float start, end;
   bool valid, ground;
-  segment_from_altitude(P, sh, vc, bottom, start, end, valid, ground);
+  segment_of(P, G, bottom, start, end, valid, ground);
   Seg acc = seg_identity();
   uint32_t samples = 0;
   if (valid) {
-    const RaySource rs = make_ray_source(P, F, o_y, sh, ray);
-    const RayWarp rw = make_warp(-(o_y * ray.y), start, end);
+    const RaySource rs = make_ray_source(P, F, G, ray);
+    const RayWarp rw = make_warp(G.tc, start, end);
     const int n = P.sv_steps;
     const int per = (n + 31) >> 5;
     const int i0 = lane * per;
@@ -128,7 +138,6 @@ __device__ __forceinline__ uint32_t aerial_column(const DevParams& P, const Fram
                                                   int y, float4* __restrict__ out) {
   const int lane = threadIdx.x & 31;
   const float bottom = F.bottom;
-  const float o_y = bottom + V.cam_alt;
   float u = (float(x) + 0.5f) / float(P.ap_w);
   float v = (float(y) + 0.5f) / float(P.ap_h);
   float sx = (u * 2.0f - 1.0f) * V.aspect;
@@ -137,9 +146,10 @@ __device__ __forceinline__ uint32_t aerial_column(const DevParams& P, const Fram
   f3 ray = rv * (1.0f / norm(rv));
   float as, ae;
   bool valid;
-  aerial_prefix(P, V.cam_alt, ray.y, bottom, as, ae, valid);
-  const RaySource rs = make_ray_source(P, F, o_y, V.cam_alt, ray);
-  const float closest_raw = -(o_y * ray.y);
+  const RayGeom G = ray_geom(P, bottom, V.cam_alt, ray.y, sqrtf(ray.x * ray.x + ray.z * ray.z));
+  aerial_prefix_of(P, G, bottom, as, ae, valid);
+  const RaySource rs = make_ray_source(P, F, G, ray);
+  const float closest_raw = G.tc;
   const int depth = P.ap_d;
   const int per = (depth + 31) >> 5;
   const size_t plane = size_t(P.ap_w) * P.ap_h;

@@ -3,11 +3,14 @@
 //
 //  * k_gen_samples: training samples produced by the plain integrator itself
 //    (the same device functions as the LUT builds and the composite).
-//  * k_composite_surrogate: the COMPOSITE view with the per-pixel limb
-//    integrator (renderer.py :1667-1786) replaced by a BF16 tensor-core MLP,
-//    and optionally the sky-view lookup by a second MLP; the plain integrator
-//    remains the per-pixel fallback where a gate trips (limb, twilight) and
-//    re-integrates a random fraction of pixels to measure the MLP's error.
+//  * k_composite_surrogate + k_surrogate_fallback: the COMPOSITE view with
+//    the per-pixel limb integrator (renderer.py :1667-1786) replaced by a
+//    BF16 tensor-core MLP and the sky-view lookup (:1474-1525) by a second
+//    one.  Pixels where a gate trips (view ray within 0.5 deg of the limb,
+//    sun within 0.1 of the local horizon) and a random fraction of the MLP
+//    pixels (the error check) go to a queue; the second kernel runs the plain
+//    integrator over the queue densely, so a few plain pixels do not stall
+//    whole warps of MLP pixels.
 //
 // Geometry is reparameterised exactly: the atmosphere is spherically
 // symmetric, so a segment is described by the altitude of its first point
@@ -29,10 +32,6 @@ namespace atm {
 namespace {
 
 constexpr unsigned kAll = 0xffffffffu;
-
-__host__ __device__ inline float norm_log(float v, float lo, float hi) {
-  return 2.0f * (logf(v) - logf(lo)) / (logf(hi) - logf(lo)) - 1.0f;
-}
 
 // x[0..3]: altitude, view, sun, relative azimuth at the segment's first point.
 __device__ __forceinline__ void geometry_features(const DevParams& P, float bottom, float h, float mu_v, float mu_s,
@@ -57,12 +56,12 @@ __device__ __forceinline__ float uniform01(unsigned long long seed, unsigned lon
 __device__ f3 sky_radiance(const DevParams& P, const Frame& F, float h, f3 ray) {
   float start, end;
   bool valid, ground;
-  segment_from_altitude(P, h, ray.y, F.bottom, start, end, valid, ground);
+  const RayGeom G = camera_ray_geom(P, F.bottom, h, ray);
+  segment_of(P, G, F.bottom, start, end, valid, ground);
   Seg acc = {splat(0.0f), splat(1.0f)};
   if (valid) {
-    const float o_y = F.bottom + h;
-    const RaySource rs = make_ray_source(P, F, o_y, h, ray);
-    const RayWarp rw = make_warp(-(o_y * ray.y), start, end);
+    const RaySource rs = make_ray_source(P, F, G, ray);
+    const RayWarp rw = make_warp(G.tc, start, end);
     const int n = P.sv_steps;
     float d0 = warp_at(rw, 0.0f);
     for (int i = 0; i < n; ++i) {
@@ -115,9 +114,10 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
       x[6] = 2.0f * u - 1.0f;
       f3 L = splat(0.0f), T = splat(1.0f);
       float start, end;
-      if (surface_interval(P, h, mu_v, R, len, start, end)) {
-        L = integrate_surface(P, F, h, ray, start, end, samples) * inv_e;
-        T = surface_segment_t(P, F, h, ray, start, end);
+      const RayGeom G = ray_geom(P, R, h, mu_v, sv);
+      if (surface_interval(P, G, R, len, start, end)) {
+        L = integrate_surface(P, F, G, ray, start, end, samples) * inv_e;
+        T = surface_segment_t(P, F, G, ray, start, end);
       }
       for (int k = 0; k < 7; ++k) features[i * 7 + k] = x[k];
       targets[i * 6 + 0] = logf(L.x + kSurrogateFloor);
@@ -131,42 +131,43 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
   warp_count(samples, counter);
 }
 
-// Lane `src`'s packed feature pair q of this lane's quad position.
-__device__ __forceinline__ uint32_t gather_pair(const uint32_t (&xp)[4], int src, int q) {
-  uint32_t v0 = __shfl_sync(kAll, xp[0], src), v1 = __shfl_sync(kAll, xp[1], src);
-  uint32_t v2 = __shfl_sync(kAll, xp[2], src), v3 = __shfl_sync(kAll, xp[3], src);
-  return q == 0 ? v0 : (q == 1 ? v1 : (q == 2 ? v2 : v3));
-}
+// ---- network evaluation for a warp's 32 pixels -----------------------------
+// Features go through shared memory into the mma A-fragment layout and the
+// outputs back to one row per lane.
+struct alignas(16) WarpSlot {
+  uint32_t in[32][4];  // 8 BF16 features per pixel
+  float out[32][8];    // outputs (the first n_out used)
+};
 
-// Evaluates a network on the warp's 32 pixels (two 16-row tiles; every lane
-// must call).  x: this lane's 8 features; out: this lane's outputs 0..7.
+// All 32 lanes call.  x: this lane's 8 features; y: its 8 outputs.
 template <int kHidden>
-__device__ __forceinline__ void warp_mlp(const unsigned char* __restrict__ w, int in0_row, const float (&x)[8],
-                                         float (&out)[8]) {
+__device__ __forceinline__ void warp_mlp(const unsigned char* __restrict__ w, int in0_row, WarpSlot& s,
+                                         const float (&x)[8], float (&y)[8]) {
   const int lane = threadIdx.x & 31;
   const int g = lane >> 2, q = lane & 3;
-  uint32_t xp[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) xp[k] = pack_bf16(x[2 * k], x[2 * k + 1]);
-#pragma unroll
+  __syncwarp();  // an earlier use of the slot is complete
+  *reinterpret_cast<uint4*>(s.in[lane]) =
+      make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
+  __syncwarp();
+#pragma unroll 1
   for (int tile = 0; tile < 2; ++tile) {
-    const uint32_t frag[4] = {gather_pair(xp, tile * 16 + g, q), gather_pair(xp, tile * 16 + g + 8, q), 0u, 0u};
-    float y[4];
-    mlp_tile_bf16<kHidden>(w, frag, in0_row, y);
-    // row r of this tile lives in lanes (r % 8) * 4 + c/2, registers (r >= 8) * 2 + c % 2
-    const int r = lane & 15;
-    const bool mine = (lane >> 4) == tile;
-#pragma unroll
-    for (int cp = 0; cp < 4; ++cp) {
-      const int src = (r & 7) * 4 + cp;
-      const float lo = __shfl_sync(kAll, y[0], src), hi = __shfl_sync(kAll, y[1], src);
-      const float lo8 = __shfl_sync(kAll, y[2], src), hi8 = __shfl_sync(kAll, y[3], src);
-      if (mine) {
-        out[2 * cp] = r >= 8 ? lo8 : lo;
-        out[2 * cp + 1] = r >= 8 ? hi8 : hi;
-      }
-    }
+    const uint32_t frag[4] = {s.in[tile * 16 + g][q], s.in[tile * 16 + g + 8][q], 0u, 0u};
+    float t[4];
+    mlp_tile_bf16<kHidden>(w, frag, in0_row, t);
+    *reinterpret_cast<float2*>(&s.out[tile * 16 + g][2 * q]) = make_float2(t[0], t[1]);
+    *reinterpret_cast<float2*>(&s.out[tile * 16 + g + 8][2 * q]) = make_float2(t[2], t[3]);
   }
+  __syncwarp();
+  const float4 a = *reinterpret_cast<const float4*>(&s.out[lane][0]);
+  const float4 b = *reinterpret_cast<const float4*>(&s.out[lane][4]);
+  y[0] = a.x;
+  y[1] = a.y;
+  y[2] = a.z;
+  y[3] = a.w;
+  y[4] = b.x;
+  y[5] = b.y;
+  y[6] = b.z;
+  y[7] = b.w;
 }
 
 __device__ __forceinline__ bool check_pixel(int x, int y, unsigned seed, float fraction) {
@@ -177,20 +178,33 @@ __device__ __forceinline__ bool check_pixel(int x, int y, unsigned seed, float f
   return float(h >> 8) * (1.0f / 16777216.0f) < fraction;
 }
 
+// Largest per-channel error of `got` relative to `ref` (floor 1e-6 E).
+__device__ __forceinline__ float color_error(f3 got, f3 ref, f3 E) {
+  const f3 d = vmax(got - ref, 0.0f) + vmax(ref - got, 0.0f);
+  return mx(mx(d.x / mx(ref.x, 1e-6f * E.x), d.y / mx(ref.y, 1e-6f * E.y)), d.z / mx(ref.z, 1e-6f * E.z));
+}
+
+// Radiance of a network's log output ln(L / E + floor), per channel.
+__device__ __forceinline__ f3 net_radiance(const float (&y)[8], const float* E, float floor) {
+  return vmax(mk((__expf(y[0]) - floor) * E[0], (__expf(y[1]) - floor) * E[1], (__expf(y[2]) - floor) * E[2]), 0.0f);
+}
+
+enum PixelKind : int { kNone = 0, kSurfMlp, kSurfPlain, kSurfEmpty, kSkyMlp, kSkyLut };
+
 __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
     DevParams P, ImageLayout L, CompositeScalars A, const float* __restrict__ scene, const float* __restrict__ space,
     const int32_t* __restrict__ sid, const float* __restrict__ pos, const float4* __restrict__ tlut,
-    const float4* __restrict__ mslut, const float4* __restrict__ svlut, SurrogateNets nets, unsigned seed,
-    float check_fraction, float* __restrict__ hdr, float* __restrict__ stats, unsigned long long* counter) {
-  extern __shared__ __align__(16) unsigned char sw[];
-  const int total = nets.ap_bytes + nets.sky_bytes;
-  for (int i = threadIdx.x * 4; i < total; i += blockDim.x * 4) {
+    const float4* __restrict__ mslut, const float4* __restrict__ svlut, SurrogateNets nets, SurrogateQueue Q,
+    float* __restrict__ hdr) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  // the aerial network, the sky network, then one slot per warp
+  const int wbytes = nets.ap_bytes + nets.sky_bytes;
+  for (int i = threadIdx.x * 16; i < wbytes; i += blockDim.x * 16) {
     const unsigned char* src = i < nets.ap_bytes ? nets.ap + i : nets.sky + (i - nets.ap_bytes);
-    *reinterpret_cast<uint32_t*>(sw + i) = *reinterpret_cast<const uint32_t*>(src);
+    *reinterpret_cast<uint4*>(smem + i) = __ldg(reinterpret_cast<const uint4*>(src));
   }
   __syncthreads();
-  const unsigned char* w_ap = sw;
-  const unsigned char* w_sky = sw + nets.ap_bytes;
+  WarpSlot& slot = reinterpret_cast<WarpSlot*>(smem + wbytes)[threadIdx.x >> 5];
 
   int x, y;
   const bool inside = tile_pixel(L, x, y);
@@ -198,120 +212,186 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
   const size_t e = pix_offset(L, cx, cy);
   const size_t o = e * L.channels;
   const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
-  const PixelRay pr = pixel_ray(L, A, cx, cy);
-  const f3 ray = pr.ray;
-  const bool surface = inside && sid[e] >= 0;
-  const float deg = 0.0174532925f;
-  const float hz_cam = sky_horizon_zenith(A.cam_alt, A.bottom);
-  const bool near_limb = fabsf(acosf(clampf(ray.y, -1.0f, 1.0f)) - hz_cam) < 0.5f * deg;
+  const f3 ray = pixel_ray(L, A, cx, cy).ray;
+  const float kHalfDeg = 0.5f * 0.0174532925f;
+  const bool near_limb = fabsf(acosf(clampf(ray.y, -1.0f, 1.0f)) - sky_horizon_zenith(A.cam_alt, A.bottom)) < kHalfDeg;
 
-  // ---- surface pixels: features of the shell-clipped camera-to-surface segment
-  float start = 0.0f, end = 0.0f;
-  bool seg_ok = false, use_ap = false;
+  int kind = kNone;
   float fx[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (surface && nets.ap != nullptr) {
-    seg_ok = surface_interval(P, A.cam_alt, ray.y, A.bottom, norm(ld3(pos + o)), start, end);
-    if (seg_ok) {
-      const float o_y = A.bottom + A.cam_alt;
-      const float hs = altitude_on_ray(A.cam_alt, ray.y, start, A.bottom);
-      const f3 ps = mk(ray.x * start, o_y + ray.y * start, ray.z * start);
-      const f3 up = ps * (1.0f / mx(norm(ps), 1.0f));
-      const float mu_v = dot(ray, up), mu_s = dot(F.sun, up);
-      const f3 tv = ray - up * mu_v, ts = F.sun - up * mu_s;
-      const float nv = norm(tv), ns = norm(ts);
-      const float cphi = (nv > 1e-6f && ns > 1e-6f) ? dot(tv, ts) / (nv * ns) : 1.0f;
-      // twilight gate: the sun within 0.1 of the local horizon at either end or the middle
-      float mu_far = 1.0f;
-      for (int k = 1; k <= 2; ++k) {
-        const float t = start + (end - start) * 0.5f * float(k);
-        const f3 pt = mk(ray.x * t, o_y + ray.y * t, ray.z * t);
-        mu_far = mn(mu_far, fabsf(dot(F.sun, pt) / mx(norm(pt), 1.0f)));
+  float start = 0.0f, end = 0.0f;
+  if (inside) {
+    if (sid[e] >= 0) {
+      const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, ray);
+      if (!surface_interval(P, G, A.bottom, norm(ld3(pos + o)), start, end)) {
+        kind = kSurfEmpty;
+      } else if (nets.ap == nullptr || near_limb) {
+        kind = kSurfPlain;
+      } else {
+        // features at the segment's first point inside the shell
+        const float o_y = A.bottom + A.cam_alt;
+        const float hs = altitude_at(G, start, A.bottom);
+        const f3 ps = mk(ray.x * start, o_y + ray.y * start, ray.z * start);
+        const f3 up = ps * (1.0f / mx(norm(ps), 1.0f));
+        const float mu_v = dot(ray, up), mu_s = dot(F.sun, up);
+        const f3 tv = ray - up * mu_v, ts = F.sun - up * mu_s;
+        const float nv = norm(tv), ns = norm(ts);
+        const float cphi = (nv > 1e-6f && ns > 1e-6f) ? dot(tv, ts) / (nv * ns) : 1.0f;
+        // twilight gate: the sun within 0.1 of the local horizon at the start, middle or end
+        float mu_min = fabsf(mu_s);
+        for (int k = 1; k <= 2; ++k) {
+          const float t = start + (end - start) * 0.5f * float(k);
+          const f3 pt = mk(ray.x * t, o_y + ray.y * t, ray.z * t);
+          mu_min = mn(mu_min, fabsf(dot(F.sun, pt) / mx(norm(pt), 1.0f)));
+        }
+        kind = mu_min < 0.1f ? kSurfPlain : kSurfMlp;
+        geometry_features(P, A.bottom, hs, mu_v, mu_s, cphi, fx);
+        fx[4] = nets.lhr_n;
+        fx[5] = nets.lhm_n;
+        fx[6] = 2.0f * __logf(clampf(end - start, 1.0f, kSurrogateMaxLength)) / logf(kSurrogateMaxLength) - 1.0f;
       }
-      const bool twilight = fabsf(mu_s) < 0.1f || mu_far < 0.1f;
-      use_ap = !twilight && !near_limb;
-      geometry_features(P, A.bottom, hs, mu_v, mu_s, cphi, fx);
+    } else if (nets.sky != nullptr && A.cam_alt <= P.top && fabsf(F.sun.y) >= 0.1f && !near_limb) {
+      kind = kSkyMlp;
+      const float vl = sqrtf(ray.x * ray.x + ray.z * ray.z), sl = sqrtf(F.sun.x * F.sun.x + F.sun.z * F.sun.z);
+      const float cphi = (vl > 1e-6f && sl > 1e-6f) ? (ray.x * F.sun.x + ray.z * F.sun.z) / (vl * sl) : 1.0f;
+      geometry_features(P, A.bottom, A.cam_alt, ray.y, F.sun.y, cphi, fx);
       fx[4] = nets.lhr_n;
       fx[5] = nets.lhm_n;
-      fx[6] = 2.0f * logf(clampf(end - start, 1.0f, kSurrogateMaxLength)) / logf(kSurrogateMaxLength) - 1.0f;
+    } else {
+      kind = kSkyLut;
     }
   }
-  // ---- sky pixels: features of the camera's ray (cameras inside the shell)
-  bool use_sky = false;
-  float fs[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (inside && !surface && nets.sky != nullptr && A.cam_alt <= P.top) {
-    const float mu_s = F.sun.y;
-    const float vl = sqrtf(ray.x * ray.x + ray.z * ray.z), sl = sqrtf(F.sun.x * F.sun.x + F.sun.z * F.sun.z);
-    const float cphi = (vl > 1e-6f && sl > 1e-6f) ? (ray.x * F.sun.x + ray.z * F.sun.z) / (vl * sl) : 1.0f;
-    use_sky = fabsf(mu_s) >= 0.1f && !near_limb;
-    geometry_features(P, A.bottom, A.cam_alt, ray.y, mu_s, cphi, fs);
-    fs[4] = nets.lhr_n;
-    fs[5] = nets.lhm_n;
+
+  float yv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (__any_sync(kAll, kind == kSurfMlp)) {
+    float t[8];
+    warp_mlp<kSurrogateApHidden>(smem, mlp_bf16_layer_row(kSurrogateApIn), slot, fx, t);
+    if (kind == kSurfMlp)
+      for (int k = 0; k < 8; ++k) yv[k] = t[k];
+  }
+  if (__any_sync(kAll, kind == kSkyMlp)) {
+    float t[8];
+    warp_mlp<kSurrogateSkyHidden>(smem + nets.ap_bytes, mlp_bf16_layer_row(kSurrogateSkyIn), slot, fx, t);
+    if (kind == kSkyMlp)
+      for (int k = 0; k < 8; ++k) yv[k] = t[k];
   }
 
-  float yap[8] = {0, 0, 0, 0, 0, 0, 0, 0}, ysky[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (__any_sync(kAll, use_ap)) warp_mlp<4>(w_ap, mlp_bf16_layer_row(7), fx, yap);
-  if (__any_sync(kAll, use_sky)) warp_mlp<3>(w_sky, mlp_bf16_layer_row(6), fs, ysky);
-
-  uint32_t samples = 0;
-  float err = -1.0f;
-  if (inside) {
+  bool queued = false;
+  uint32_t qkind = kQueueSurface;
+  if (inside && kind != kSurfPlain) {
     f3 color = ld3(scene + o);
-    if (surface) {
-      if (seg_ok) {
-        const bool check = use_ap && check_pixel(x, y, seed, check_fraction);
-        f3 Lm = splat(0.0f), Tm = splat(1.0f);
-        if (use_ap) {
-          Lm = vmax(mk((__expf(yap[0]) - kSurrogateFloor) * A.E[0], (__expf(yap[1]) - kSurrogateFloor) * A.E[1],
-                       (__expf(yap[2]) - kSurrogateFloor) * A.E[2]),
-                    0.0f);
-          Tm = mk(__expf(-mx(yap[3], 0.0f)), __expf(-mx(yap[4], 0.0f)), __expf(-mx(yap[5], 0.0f)));
-        }
-        if (!use_ap || check) {
-          const f3 Lp = integrate_surface(P, F, A.cam_alt, ray, start, end, samples);
-          const f3 Tp = surface_segment_t(P, F, A.cam_alt, ray, start, end);
-          if (check) {
-            const f3 cm = Lm + color * Tm, cp = Lp + color * Tp;
-            const f3 d = vmax(cm - cp, 0.0f) + vmax(cp - cm, 0.0f);
-            err = mx(mx(d.x / mx(cp.x, 1e-12f), d.y / mx(cp.y, 1e-12f)), d.z / mx(cp.z, 1e-12f));
-          }
-          Lm = Lp;  // re-integrated and gated pixels keep the plain result
-          Tm = Tp;
-        }
-        color = Lm + color * Tm;
+    if (kind == kSurfMlp) {
+      // transmittance: the plain path's own two-tap LUT ratio (:1603-1665);
+      // in-scattering: the network, optionally per unit of (1 - T)
+      const f3 Tm = surface_segment_t(P, F, camera_ray_geom(P, A.bottom, A.cam_alt, ray), ray, start, end);
+      f3 Lm = net_radiance(yv, A.E, nets.floor);
+      if (nets.per_opacity) Lm = Lm * (splat(1.0f) - Tm);
+      color = Lm + color * Tm;
+      if (check_pixel(x, y, Q.seed, Q.check_fraction)) {
+        queued = true;
+        qkind = kQueueSurfaceCheck;
       }
-    } else if (use_sky) {
-      const f3 sky = vmax(mk((__expf(ysky[0]) - kSurrogateFloor) * A.E[0],
-                             (__expf(ysky[1]) - kSurrogateFloor) * A.E[1],
-                             (__expf(ysky[2]) - kSurrogateFloor) * A.E[2]),
-                          0.0f);
+    } else if (kind == kSkyMlp) {
+      const f3 sky = net_radiance(yv, A.E, nets.sky_floor);
       color = composite_sky_with(P, F, A, sky, ray, color, ld3(space + o), float(L.height));
-    } else {
+      if (check_pixel(x, y, Q.seed, Q.check_fraction)) {
+        queued = true;
+        qkind = kQueueSkyCheck;
+      }
+    } else if (kind == kSkyLut) {
       color = composite_sky(P, F, A, svlut, ray, color, ld3(space + o), float(L.height));
     }
     color = vmax(color, 0.0f);
     hdr[o + 0] = color.x;
     hdr[o + 1] = color.y;
     hdr[o + 2] = color.z;
+  } else if (kind == kSurfPlain) {
+    queued = true;
+  }
+
+  // warp-aggregated append to the fallback queue
+  const int lane = threadIdx.x & 31;
+  const unsigned qm = __ballot_sync(kAll, queued);
+  if (qm) {
+    const int leader = __ffs(qm) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(Q.count, uint32_t(__popc(qm)));
+    base = __shfl_sync(kAll, base, leader);
+    if (queued)
+      Q.items[base + __popc(qm & ((1u << lane) - 1u))] = (qkind << 30) | uint32_t(cy * L.width + cx);
+  }
+  if (Q.stats != nullptr) {
+    const unsigned gs = __ballot_sync(kAll, kind == kSurfPlain), ms = __ballot_sync(kAll, kind == kSurfMlp);
+    const unsigned mk_ = __ballot_sync(kAll, kind == kSkyMlp), ls = __ballot_sync(kAll, kind == kSkyLut);
+    if (lane == 0) {
+      if (gs) atomicAdd(Q.stats + 3, float(__popc(gs)));
+      if (ms) atomicAdd(Q.stats + 4, float(__popc(ms)));
+      if (mk_) atomicAdd(Q.stats + 5, float(__popc(mk_)));
+      if (ls) atomicAdd(Q.stats + 6, float(__popc(ls)));
+    }
+  }
+}
+
+// The plain integrator over the queued pixels: gated surface pixels get it
+// as their result; checked pixels compare the MLP's color (in hdr) with it,
+// then keep the plain result.  Warps take 32 entries per ticket.
+__global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
+    DevParams P, ImageLayout L, CompositeScalars A, const float* __restrict__ scene, const float* __restrict__ space,
+    const float* __restrict__ pos, const float4* __restrict__ tlut, const float4* __restrict__ mslut,
+    SurrogateQueue Q, float* __restrict__ hdr, unsigned long long* counter) {
+  const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+  const int lane = threadIdx.x & 31;
+  const uint32_t n = *Q.count;
+  uint32_t samples = 0, checked = 0;
+  float err_sum = 0.0f, err_max = 0.0f;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(Q.count + 1, 32u);
+    base = __shfl_sync(kAll, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + uint32_t(lane);
+    if (i < n) {
+      const uint32_t entry = Q.items[i];
+      const uint32_t kind = entry >> 30, p = entry & 0x3fffffffu;
+      const int x = int(p % uint32_t(L.width)), y = int(p / uint32_t(L.width));
+      const size_t o = pix_offset(L, x, y) * L.channels;
+      const f3 ray = pixel_ray(L, A, x, y).ray;
+      f3 color = ld3(scene + o);
+      if (kind == kQueueSkyCheck) {
+        const f3 sky = sky_radiance(P, F, A.cam_alt, ray);
+        samples += uint32_t(P.sv_steps);
+        color = composite_sky_with(P, F, A, sky, ray, color, ld3(space + o), float(L.height));
+      } else {
+        float start, end;
+        const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, ray);
+        if (surface_interval(P, G, A.bottom, norm(ld3(pos + o)), start, end))
+          color = integrate_surface(P, F, G, ray, start, end, samples) +
+                  color * surface_segment_t(P, F, G, ray, start, end);
+      }
+      color = vmax(color, 0.0f);
+      if (kind != kQueueSurface) {
+        const float err = color_error(ld3(hdr + o), color, F.E);
+        ++checked;
+        err_sum += err;
+        err_max = mx(err_max, err);
+      }
+      hdr[o + 0] = color.x;
+      hdr[o + 1] = color.y;
+      hdr[o + 2] = color.z;
+    }
   }
   warp_count(samples, counter);
-  // error statistics of the re-integrated pixels: count, sum, max, gated surface pixels
-  if (stats != nullptr) {
-    const bool checked = err >= 0.0f;
-    const unsigned gated = __ballot_sync(kAll, surface && seg_ok && !use_ap);
-    float s = checked ? err : 0.0f, m = checked ? err : 0.0f;
+  if (Q.stats != nullptr) {
+    float c = float(checked);
 #pragma unroll
     for (int k = 16; k > 0; k >>= 1) {
-      s += __shfl_xor_sync(kAll, s, k);
-      m = mx(m, __shfl_xor_sync(kAll, m, k));
+      c += __shfl_xor_sync(kAll, c, k);
+      err_sum += __shfl_xor_sync(kAll, err_sum, k);
+      err_max = mx(err_max, __shfl_xor_sync(kAll, err_max, k));
     }
-    const unsigned n_checked = __popc(__ballot_sync(kAll, checked));
-    if ((threadIdx.x & 31) == 0) {
-      if (n_checked) {
-        atomicAdd(stats + 0, float(n_checked));
-        atomicAdd(stats + 1, s);
-        atomicMax(reinterpret_cast<int*>(stats + 2), __float_as_int(m));
-      }
-      if (gated) atomicAdd(stats + 3, float(__popc(gated)));
+    if (lane == 0 && c > 0.0f) {
+      atomicAdd(Q.stats + 0, c);
+      atomicAdd(Q.stats + 1, err_sum);
+      atomicMax(reinterpret_cast<int*>(Q.stats + 2), __float_as_int(err_max));  // non-negative floats
     }
   }
 }
@@ -327,17 +407,25 @@ cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind
   return cudaGetLastError();
 }
 
+size_t surrogate_smem_bytes(const SurrogateNets& nets) {
+  return size_t(nets.ap_bytes) + size_t(nets.sky_bytes) + 8 * sizeof(WarpSlot);
+}
+
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,
                                        const float4* tlut, const float4* mslut, const float4* svlut,
-                                       const SurrogateNets& nets, unsigned seed, float check_fraction, float* hdr,
-                                       float* stats, unsigned long long* counter, cudaStream_t s) {
-  const int smem = nets.ap_bytes + nets.sky_bytes;
-  cudaError_t e = cudaFuncSetAttribute(k_composite_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+                                       const SurrogateNets& nets, const SurrogateQueue& Q, float* hdr,
+                                       unsigned long long* counter, int sm_count, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(Q.count, 0, 2 * sizeof(uint32_t), s);
+  if (e != cudaSuccess) return e;
+  const int smem = int(surrogate_smem_bytes(nets));
+  e = cudaFuncSetAttribute(k_composite_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   const dim3 grid((L.width + 15) / 16, (L.height + 15) / 16);
-  k_composite_surrogate<<<grid, 256, smem, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, nets, seed,
-                                                check_fraction, hdr, stats, counter);
+  k_composite_surrogate<<<grid, 256, smem, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, nets, Q, hdr);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_surrogate_fallback<<<2 * sm_count, 256, 0, s>>>(P, L, A, scene, space, pos, tlut, mslut, Q, hdr, counter);
   return cudaGetLastError();
 }
 

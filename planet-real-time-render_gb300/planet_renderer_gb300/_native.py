@@ -141,6 +141,25 @@ class AtmBatchTuning(ctypes.Structure):
     ]
 
 
+class AtmSurrogate(ctypes.Structure):
+    _fields_ = [
+        ("aerial", ctypes.c_void_p),
+        ("sky", ctypes.c_void_p),
+        ("scale_height_range", ctypes.c_double * 4),
+        ("trained_planet_radius_m", ctypes.c_double),
+        ("trained_top_altitude_m", ctypes.c_double),
+        ("check_fraction", ctypes.c_double),
+        ("aerial_floor", ctypes.c_double),
+        ("sky_floor", ctypes.c_double),
+        ("aerial_per_opacity", ctypes.c_int32),
+        ("seed", ctypes.c_uint32),
+        ("stats", ctypes.c_void_p),
+    ]
+
+
+ATM_SURROGATE_SKY = 0
+ATM_SURROGATE_AERIAL = 1
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _D = ctypes.c_double
@@ -189,6 +208,13 @@ SIGNATURES = {
                                           ctypes.c_float, ctypes.c_float, _P, _P]),
     "atm_mlp_pack_bf16": (ctypes.c_int, [_P, _P]),
     "atm_mlp_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _I32, _P]),
+    "atm_surrogate_samples": (ctypes.c_int, [_P, _I32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double * 4, _P, _P,
+                                             _P]),
+    "atm_composite_surrogate": (
+        ctypes.c_int,
+        [_P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, c_double3, _D, c_double9,
+         _D, _D, _D, ctypes.POINTER(AtmSurrogate), _P],
+    ),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,

@@ -115,13 +115,19 @@ class Mlp:
         return self._loss
 
     # -- inference -------------------------------------------------------------------
+    def pack(self) -> None:
+        """Copy the current parameters into the BF16 tensor-core layout."""
+
+        if not self._packed:
+            _native.check(self._lib.atm_mlp_pack_bf16(self._handle, self._s()))
+            self._packed = True
+
     def forward(self, inputs: torch.Tensor, precision: str = "f32", out: torch.Tensor | None = None) -> torch.Tensor:
         x = self._check_io(inputs, self.n_in, "inputs")
         if out is None:
             out = torch.empty((x.shape[0], self.n_out), dtype=torch.float32, device=self.device)
-        if precision == "bf16" and not self._packed:
-            _native.check(self._lib.atm_mlp_pack_bf16(self._handle, self._s()))
-            self._packed = True
+        if precision == "bf16":
+            self.pack()
         code = {"f32": 0, "bf16": 1}[precision]
         _native.check(self._lib.atm_mlp_forward(self._handle, self._p(x), self._p(out), x.shape[0], code, self._s()))
         return out

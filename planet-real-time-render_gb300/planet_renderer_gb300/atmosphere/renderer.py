@@ -250,6 +250,31 @@ class AtmosphereRenderer:
             _stream_handle(self.device)))
 
     # ---- extensions ------------------------------------------------------------
+    def composite_surrogate(self, scene_hdr, space_hdr, surface_id, position_view, hdr, planet_radius_m: float,
+                            camera_radius_m: float, sun_local, solar_irradiance, sun_disk_radiance,
+                            sun_angular_radius_degrees: float, view_basis, tangent_half_fov: float,
+                            star_contrast_start: float, star_contrast_end: float, surrogate,
+                            stats: torch.Tensor | None = None, check_fraction: float = 0.01,
+                            seed: int = 0) -> None:
+        """COMPOSITE view with the learned surrogates (``surrogate``: a
+        :class:`~planet_renderer_gb300.atmosphere.surrogate.Surrogate`).  The
+        plain integrator re-integrates ``check_fraction`` of the MLP pixels;
+        ``stats`` (8 floats on the device, accumulated) receives their error
+        and the pixel counts of each path."""
+
+        img = self._image([scene_hdr, space_hdr, position_view, hdr], surface_id)
+        if stats is not None and (stats.device != self.device or stats.dtype != torch.float32 or stats.numel() < 8):
+            raise ValueError("stats must be a float32 tensor of 8 elements on the renderer's device")
+        sg = surrogate.native(check_fraction=check_fraction, seed=seed,
+                              stats=None if stats is None else stats.data_ptr())
+        _native.check(self._lib.atm_composite_surrogate(
+            self._handle, ctypes.c_void_p(scene_hdr.data_ptr()), ctypes.c_void_p(space_hdr.data_ptr()),
+            ctypes.c_void_p(surface_id.data_ptr()), ctypes.c_void_p(position_view.data_ptr()),
+            ctypes.c_void_p(hdr.data_ptr()), ctypes.byref(img), float(planet_radius_m), float(camera_radius_m),
+            _native.d3(sun_local), _native.d3(solar_irradiance), _native.d3(sun_disk_radiance),
+            float(sun_angular_radius_degrees), _native.d9(view_basis), float(tangent_half_fov),
+            float(star_contrast_start), float(star_contrast_end), ctypes.byref(sg), _stream_handle(self.device)))
+
     def build_lut(self, kind: str, *, planet_radius_m: float, camera_altitude_m: float = 0.0,
                   sun_zenith_cosine: float = 1.0, sun_local=(0.0, 1.0, 0.0), solar_irradiance=(4.0, 3.9, 3.7),
                   sun_angular_radius_degrees: float = 0.266, view_basis=((1, 0, 0), (0, 1, 0), (0, 0, 1)),

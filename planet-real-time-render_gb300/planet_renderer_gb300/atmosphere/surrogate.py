@@ -1,0 +1,306 @@
+"""Learned surrogates of the sky radiance and of the camera-to-surface
+in-scattering / transmittance (no counterpart in the reference).
+
+Training data come from the plain CUDA integrator itself
+(``atm_surrogate_samples``): features uniform over the input box, over a grid
+of parameter sets that differ in their Rayleigh and Mie scale heights (the
+networks' features 4 and 5).  Networks are trained by the package's own fused
+FP32 forward/backward kernels with Adam on standardised targets; the
+standardisation is then folded into the output layer and the weights are
+packed for the BF16 tensor-core composite (``atm_composite_surrogate``).
+
+Networks (feature layout in ``include/atm_capi.h``):
+  * sky:    6 -> 3 x 64 SiLU -> 3   sky radiance, ln(L / E + floor)
+  * aerial: 7 -> 4 x 64 SiLU -> 6   segment in-scattering (``TargetSpec``),
+                                     optical depth
+The surrogate composite takes the surface pixels' transmittance from the
+transmittance LUT, as the plain composite does; the aerial network's
+optical-depth outputs are trained and reported, not used in the frame.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import math
+import time
+from dataclasses import dataclass, field
+from pathlib import Path
+
+import numpy as np
+import torch
+
+from .. import _native
+from .batch import BatchedLutBuilder
+from .config import EARTH_RADIUS_M, earth_baseline
+from .mlp import Mlp, layer_shapes
+
+SKY = _native.ATM_SURROGATE_SKY
+AERIAL = _native.ATM_SURROGATE_AERIAL
+# Rayleigh scale height min, max; Mie scale height min, max (m)
+SCALE_HEIGHT_RANGE = (6000.0, 10000.0, 800.0, 1600.0)
+SHAPES = {SKY: (6, 3, 3), AERIAL: (7, 4, 6)}  # n_in, hidden layers, n_out
+FLOOR = 1.0e-7        # floor of the generator's targets ln(L / E + FLOOR)
+MAX_LENGTH_M = 2.0e6
+MAX_DEPTH = 30.0
+
+
+@dataclass(frozen=True)
+class TargetSpec:
+    """What a network's radiance outputs mean: ln(L / E + floor), or for the
+    aerial network with ``per_opacity`` ln(L / (E (1 - T)) + floor), T the
+    segment's LUT-ratio transmittance (the in-scattering per unit of
+    opacity: bounded and nearly independent of the segment's length, where
+    L itself spans many decades).  Outputs 3..5 of the aerial network stay
+    the optical depth."""
+
+    floor: float = 1.0e-4
+    per_opacity: bool = False
+
+
+DEFAULT_SPECS = {SKY: TargetSpec(1.0e-4, False), AERIAL: TargetSpec(1.0e-4, False)}
+
+
+def _generator_radiance(y: torch.Tensor) -> torch.Tensor:
+    return (torch.exp(y[:, :3]) - FLOOR).clamp_min(0.0)
+
+
+def to_targets(kind: int, y: torch.Tensor, spec: TargetSpec) -> torch.Tensor:
+    """Network targets from the generator's (ln(L/E + 1e-7)[, optical depth])."""
+
+    L = _generator_radiance(y)
+    if kind == AERIAL and spec.per_opacity:
+        L = L / (1.0 - torch.exp(-y[:, 3:6])).clamp_min(1.0e-6)
+    t = torch.log(L + spec.floor)
+    return t if kind == SKY else torch.cat([t, y[:, 3:6]], 1)
+
+
+def radiance_of(kind: int, out: torch.Tensor, spec: TargetSpec, transmittance=None) -> torch.Tensor:
+    """L / E of network outputs (``transmittance`` needed for per_opacity)."""
+
+    L = (torch.exp(out[:, :3]) - spec.floor).clamp_min(0.0)
+    if kind == AERIAL and spec.per_opacity:
+        L = L * (1.0 - transmittance)
+    return L
+
+
+def parameter_grid(base=None, rayleigh=(6000.0, 8000.0, 10000.0), mie=(800.0, 1200.0, 1600.0)):
+    """Parameter sets of the training data: ``base`` (Earth-like by default)
+    with every (Rayleigh, Mie) scale-height pair of the grid."""
+
+    base = base or earth_baseline()
+    return [dataclasses.replace(base, rayleigh_scale_height_m=float(hr), mie_scale_height_m=float(hm))
+            for hr in rayleigh for hm in mie]
+
+
+def scale_height_features(config, scale_height_range=SCALE_HEIGHT_RANGE):
+    lo_r, hi_r, lo_m, hi_m = scale_height_range
+    f = lambda h, lo, hi: 2.0 * (math.log(h) - math.log(lo)) / (math.log(hi) - math.log(lo)) - 1.0
+    return f(config.rayleigh_scale_height_m, lo_r, hi_r), f(config.mie_scale_height_m, lo_m, hi_m)
+
+
+class SampleSource:
+    """Training samples from the plain integrator over parameter sets of one
+    planet (their transmittance and multi-scattering LUTs are built once)."""
+
+    def __init__(self, configs, planet_radius_m: float = EARTH_RADIUS_M, solar_irradiance=(4.0, 3.9, 3.7),
+                 sun_angular_radius_degrees: float = 0.266, scale_height_range=SCALE_HEIGHT_RANGE, device=None):
+        self.configs = list(configs)
+        self.planet_radius_m = float(planet_radius_m)
+        self.top_altitude_m = float(self.configs[0].top_altitude_m)
+        self.scale_height_range = tuple(float(v) for v in scale_height_range)
+        self.builder = BatchedLutBuilder([(c, planet_radius_m) for c in self.configs], solar_irradiance,
+                                         sun_angular_radius_degrees, device=device)
+        self.device = self.builder.device
+
+    def samples(self, kind: int, n: int, seed: int):
+        n_in, _, n_out = SHAPES[kind]
+        x = torch.empty((n, n_in), dtype=torch.float32, device=self.device)
+        y = torch.empty((n, n_out), dtype=torch.float32, device=self.device)
+        rng = (ctypes.c_double * 4)(*self.scale_height_range)
+        _native.check(self.builder._lib.atm_surrogate_samples(
+            self.builder._handle, int(kind), int(n), int(seed) & (2**64 - 1), rng, ctypes.c_void_p(x.data_ptr()),
+            ctypes.c_void_p(y.data_ptr()), self.builder._stream()))
+        return x, y
+
+    def close(self):
+        self.builder.close()
+
+
+@dataclass
+class TrainReport:
+    kind: int
+    steps: int
+    batch: int
+    n_samples: int
+    seconds: float
+    loss: list = field(default_factory=list)         # (step, mean squared error, standardised)
+    held_out: dict = field(default_factory=dict)
+    spec: TargetSpec | None = None
+
+
+def _fold_standardisation(params: torch.Tensor, shapes, mean: torch.Tensor, std: torch.Tensor) -> torch.Tensor:
+    """Parameters whose output layer returns std * y + mean."""
+
+    p = params.clone()
+    off = 0
+    for i, (o, n_in) in enumerate(shapes):
+        w = p[off:off + o * n_in].view(o, n_in)
+        b = p[off + o * n_in:off + o * n_in + o]
+        if i == len(shapes) - 1:
+            w.mul_(std[:, None])
+            b.mul_(std).add_(mean)
+        off += o * n_in + o
+    return p
+
+
+def held_out_error(net: Mlp, kind: int, x: torch.Tensor, y: torch.Tensor, spec: TargetSpec,
+                   precision: str = "bf16") -> dict:
+    """Errors of a de-standardised network on held-out samples: radiance as
+    relative error where L > 1e-4 E; for the aerial network also the
+    composite-like error |dL + C dT| / (L + C T) with a lit surface of
+    radiance C = 0.02 E behind the segment, with the LUT-ratio T (as the
+    composite uses it), and the optical-depth output's absolute error."""
+
+    pred = net.forward(x, precision).double()
+    yd = y.double()
+    Lt = _generator_radiance(yd)
+    Tt = torch.exp(-yd[:, 3:6]) if kind == AERIAL else None
+    Lp = radiance_of(kind, pred, spec, Tt)
+    bright = Lt > 1e-4
+    rel = ((Lp - Lt).abs() / Lt.clamp_min(1e-30))[bright]
+    q = lambda v, p: float(torch.quantile(v[:1 << 20].float(), p)) if v.numel() else 0.0
+    out = {"radiance_rel_mean": float(rel.mean()) if rel.numel() else 0.0, "radiance_rel_p99": q(rel, 0.99)}
+    if kind == AERIAL:
+        C = 0.02
+        comp = ((Lp - Lt).abs() / (Lt + C * Tt)).max(1).values
+        out["composite_rel_mean"] = float(comp.mean())
+        out["composite_rel_p99"] = q(comp, 0.99)
+        dtau = (pred[:, 3:6].clamp_min(0) - yd[:, 3:6]).abs()
+        live = yd[:, 3:6] < 10.0
+        out["depth_abs_mean"] = float(dtau[live].mean())
+    return out
+
+
+def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 65536, epochs: int = 200,
+          lr: float = 2e-3, lr_final: float = 1e-5, seed: int = 1, held_out: int = 2**16,
+          spec: TargetSpec | None = None, log_every: int = 100) -> tuple[Mlp, TrainReport]:
+    """Train one surrogate network on ``n_samples`` integrator samples with
+    Adam (cosine learning-rate decay from ``lr`` to ``lr_final``).  Returns
+    the network (standardisation folded in, BF16 packed) and a report with
+    the loss history and held-out errors."""
+
+    spec = spec or DEFAULT_SPECS[kind]
+    n_in, n_hidden, n_out = SHAPES[kind]
+    x, y = source.samples(kind, n_samples, seed)
+    t = to_targets(kind, y, spec)
+    del y
+    mean, std = t.mean(0), t.std(0).clamp_min(1e-6)
+    ts = (t - mean) / std
+    del t
+    net = Mlp(n_in, n_hidden, n_out, seed=seed, device=source.device)
+    steps_per_epoch = max(n_samples // batch, 1)
+    steps = steps_per_epoch * epochs
+    gen = torch.Generator(device=source.device)
+    gen.manual_seed(seed)
+    report = TrainReport(kind, steps, batch, n_samples, 0.0)
+    torch.cuda.synchronize(source.device)
+    t0 = time.perf_counter()
+    step = 0
+    for epoch in range(epochs):
+        perm = torch.randperm(n_samples, device=source.device, generator=gen)
+        for k in range(steps_per_epoch):
+            idx = perm[k * batch:(k + 1) * batch]
+            frac = step / max(steps - 1, 1)
+            rate = lr_final + 0.5 * (lr - lr_final) * (1.0 + math.cos(math.pi * frac))
+            loss = net.train_step(x[idx], ts[idx], lr=rate)
+            if log_every and step % log_every == 0:
+                report.loss.append((step, float(loss) / (batch * n_out)))
+            step += 1
+    torch.cuda.synchronize(source.device)
+    report.seconds = time.perf_counter() - t0
+    folded = _fold_standardisation(net.params(), layer_shapes(n_in, n_hidden, n_out), mean, std)
+    net.set_params(folded)
+    net.pack()
+    xh, yh = source.samples(kind, held_out, seed + 7919)
+    report.held_out = {"bf16": held_out_error(net, kind, xh, yh, spec, "bf16"),
+                       "f32": held_out_error(net, kind, xh, yh, spec, "f32")}
+    report.spec = spec
+    return net, report
+
+
+class Surrogate:
+    """The two networks plus what atm_composite_surrogate needs to use them."""
+
+    def __init__(self, aerial: Mlp | None, sky: Mlp | None, planet_radius_m: float = EARTH_RADIUS_M,
+                 top_altitude_m: float = 100_000.0, scale_height_range=SCALE_HEIGHT_RANGE,
+                 aerial_spec: TargetSpec | None = None, sky_spec: TargetSpec | None = None):
+        self.aerial, self.sky = aerial, sky
+        self.planet_radius_m = float(planet_radius_m)
+        self.top_altitude_m = float(top_altitude_m)
+        self.scale_height_range = tuple(float(v) for v in scale_height_range)
+        self.aerial_spec = aerial_spec or DEFAULT_SPECS[AERIAL]
+        self.sky_spec = sky_spec or DEFAULT_SPECS[SKY]
+        for net in (aerial, sky):
+            if net is not None:
+                net.pack()
+
+    def native(self, check_fraction: float = 0.01, seed: int = 0, stats=None) -> _native.AtmSurrogate:
+        s = _native.AtmSurrogate()
+        s.aerial = self.aerial.handle.value if self.aerial is not None else None
+        s.sky = self.sky.handle.value if self.sky is not None else None
+        s.scale_height_range[:] = list(self.scale_height_range)
+        s.trained_planet_radius_m = self.planet_radius_m
+        s.trained_top_altitude_m = self.top_altitude_m
+        s.check_fraction = float(check_fraction)
+        s.aerial_floor = float(self.aerial_spec.floor)
+        s.sky_floor = float(self.sky_spec.floor)
+        s.aerial_per_opacity = 1 if self.aerial_spec.per_opacity else 0
+        s.seed = int(seed) & 0xFFFFFFFF
+        s.stats = stats
+        return s
+
+    def save(self, directory) -> None:
+        d = Path(directory)
+        d.mkdir(parents=True, exist_ok=True)
+        for name, net in (("aerial", self.aerial), ("sky", self.sky)):
+            if net is not None:
+                net.save(d / f"{name}.npz")
+        np.savez(d / "meta.npz", planet_radius_m=self.planet_radius_m, top_altitude_m=self.top_altitude_m,
+                 scale_height_range=np.array(self.scale_height_range),
+                 aerial_spec=np.array([self.aerial_spec.floor, float(self.aerial_spec.per_opacity)]),
+                 sky_spec=np.array([self.sky_spec.floor, float(self.sky_spec.per_opacity)]))
+
+    @classmethod
+    def load(cls, directory, device=None) -> "Surrogate":
+        d = Path(directory)
+        meta = np.load(d / "meta.npz")
+        nets = {name: (Mlp.load(d / f"{name}.npz", device=device) if (d / f"{name}.npz").exists() else None)
+                for name in ("aerial", "sky")}
+        spec = lambda a: TargetSpec(float(a[0]), bool(a[1]))
+        return cls(nets["aerial"], nets["sky"], float(meta["planet_radius_m"]), float(meta["top_altitude_m"]),
+                   tuple(float(v) for v in meta["scale_height_range"]), spec(meta["aerial_spec"]),
+                   spec(meta["sky_spec"]))
+
+
+def train_surrogate(configs=None, n_samples: int = 2**22, batch: int = 65536, epochs: int = 200, seed: int = 1,
+                    device=None, log_every: int = 100, specs=None):
+    """Both networks on the default grid; returns (Surrogate, {kind: report})."""
+
+    specs = {**DEFAULT_SPECS, **(specs or {})}
+    source = SampleSource(configs or parameter_grid(), device=device)
+    try:
+        aerial, ra = train(source, AERIAL, n_samples, batch, epochs, seed=seed, spec=specs[AERIAL],
+                           log_every=log_every)
+        sky, rs = train(source, SKY, n_samples, batch, epochs, seed=seed + 1, spec=specs[SKY], log_every=log_every)
+    finally:
+        source.close()
+    return Surrogate(aerial, sky, source.planet_radius_m, source.top_altitude_m, source.scale_height_range,
+                     specs[AERIAL], specs[SKY]), {AERIAL: ra, SKY: rs}
+
+
+def stats_summary(stats: torch.Tensor) -> dict:
+    s = [float(v) for v in stats.cpu()]
+    n = max(s[0], 1.0)
+    return {"checked": int(s[0]), "check_rel_mean": s[1] / n, "check_rel_max": s[2], "gated_surface": int(s[3]),
+            "mlp_surface": int(s[4]), "mlp_sky": int(s[5]), "lut_sky": int(s[6])}

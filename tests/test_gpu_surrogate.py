@@ -1,0 +1,278 @@
+"""Learned surrogates: training samples against the oracle, training by the
+package's kernels, the surrogate composite's queue and gates, its error
+against the FP64 oracle and what it gains over the aerial-perspective froxel
+volume (the method without it)."""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+E = (4.0, 3.9, 3.7)
+AR_DEG = 0.266
+
+
+@pytest.fixture(scope="module")
+def source():
+    from planet_renderer_gb300.atmosphere.surrogate import SampleSource, parameter_grid
+
+    s = SampleSource(parameter_grid(rayleigh=(6000.0, 10000.0), mie=(800.0, 1600.0)))
+    yield s
+    s.close()
+
+
+@pytest.fixture(scope="module")
+def trained(source):
+    """Both networks at a reduced training budget (seconds)."""
+
+    from planet_renderer_gb300.atmosphere.surrogate import AERIAL, SKY, Surrogate, train
+
+    aerial, ra = train(source, AERIAL, n_samples=2**20, batch=32768, epochs=24, seed=3, log_every=0)
+    sky, rs = train(source, SKY, n_samples=2**20, batch=32768, epochs=24, seed=4, log_every=0)
+    return Surrogate(aerial, sky, source.planet_radius_m, source.top_altitude_m, source.scale_height_range), ra, rs
+
+
+# ---- feature decoding (the generator's maps, numpy float64) ------------------------
+def _decode(x, top, R, scale_height_range, kind):
+    x = x.astype(np.float64)
+    h = top * ((x[:, 0] + 1.0) * 0.5) ** 2
+    rho = np.sqrt(h * (2 * R + h))
+    hz = math.pi - np.arccos(np.clip(rho / (R + h), 0.0, 1.0))
+    v = (x[:, 1] + 1.0) * 0.5
+    zen = np.where(v < 0.5, hz * (1 - (1 - 2 * v) ** 2), hz + (math.pi - hz) * (2 * v - 1) ** 2)
+    hc = -rho / (R + h)
+    u = (x[:, 2] + 1.0) * 0.5
+    mu_s = np.where(u < 0.5, hc - (hc + 1) * (1 - 2 * u) ** 2, hc + (1 - hc) * (2 * u - 1) ** 2)
+    mu_s = np.clip(mu_s, -1, 1)
+    cphi = x[:, 3]
+    ss, sphi = np.sqrt(np.maximum(1 - mu_s ** 2, 0)), np.sqrt(np.maximum(1 - cphi ** 2, 0))
+    ray = np.stack([np.sin(zen), np.cos(zen), np.zeros_like(zen)], 1)
+    sun = np.stack([ss * cphi, mu_s, ss * sphi], 1)
+    lo_r, hi_r, lo_m, hi_m = scale_height_range
+    hr = np.exp(math.log(lo_r) + (x[:, 4] + 1) * 0.5 * (math.log(hi_r) - math.log(lo_r)))
+    hm = np.exp(math.log(lo_m) + (x[:, 5] + 1) * 0.5 * (math.log(hi_m) - math.log(lo_m)))
+    length = 2.0e6 ** ((x[:, 6] + 1) * 0.5) if kind == 1 else None
+    return h, ray, sun, hr, hm, length
+
+
+def test_samples_are_deterministic_and_in_the_box(source):
+    from planet_renderer_gb300.atmosphere.surrogate import AERIAL, SKY
+
+    for kind in (SKY, AERIAL):
+        x1, y1 = source.samples(kind, 4096, 5)
+        x2, y2 = source.samples(kind, 8192, 5)
+        torch.cuda.synchronize()
+        assert torch.equal(x1, x2[:4096]) and torch.equal(y1, y2[:4096])
+        assert float(x1.abs().max()) <= 1.0 + 1e-6
+        assert bool(torch.isfinite(y1).all())
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_samples_match_the_oracle_integrator(source, kind):
+    """Targets of the GPU generator against the oracle's single-ray
+    restatement of the same integrals at the decoded geometry."""
+
+    from oracle.atm import Oracle
+    from planet_renderer_gb300.atmosphere.surrogate import FLOOR, MAX_DEPTH
+
+    x, y = source.samples(kind, 1536, 11)
+    x, y = x.cpu().numpy(), y.cpu().numpy()
+    h, ray, sun, hr, hm, length = _decode(x, source.top_altitude_m, source.planet_radius_m,
+                                          source.scale_height_range, kind)
+    # FP64: the reference's float32 segment weight rounds the in-scattering of
+    # thin high-altitude segments to zero, the kernels' series weight does not
+    o = Oracle("f64")
+    ar = math.radians(AR_DEG)
+    ref = np.zeros_like(y, dtype=np.float64)
+    for cfg in source.configs:
+        m = (np.abs(hr - cfg.rayleigh_scale_height_m) < 1.0) & (np.abs(hm - cfg.mie_scale_height_m) < 1.0)
+        if not m.any():
+            continue
+        tl = o.build_transmittance(cfg, source.planet_radius_m)
+        ms = o.build_multi_scattering(cfg, source.planet_radius_m, E, ar, tl)
+        if kind == 0:
+            L = o.sky_rays(cfg, source.planet_radius_m, h[m], ray[m], sun[m], E, ar, tl, ms)
+            ref[m] = np.log(L / np.array(E) + FLOOR)
+        else:
+            L, T = o.surface_rays(cfg, source.planet_radius_m, h[m], ray[m], length[m], sun[m], E, ar, tl, ms)
+            ref[m, :3] = np.log(L / np.array(E) + FLOOR)
+            ref[m, 3:] = np.minimum(-np.log(np.maximum(T.astype(np.float64), 1e-30)), MAX_DEPTH)
+    d = np.abs(y - ref)
+    # radiance targets: ln differences = relative differences; decoding the
+    # features back to geometry in float64 moves rays by ~1e-7, which only
+    # matters for the rare ray grazing the ground
+    assert np.median(d[:, :3]) < 1e-4, np.median(d[:, :3])
+    assert np.quantile(d[:, :3], 0.99) < 5e-3, np.quantile(d[:, :3], 0.99)
+    if kind == 1:
+        live = ref[:, 3:] < 10
+        assert np.quantile(d[:, 3:][live], 0.99) < 5e-3
+
+
+def test_training_learns_both_networks(trained):
+    """Held-out errors at the reduced test budget (the bench states those of
+    the full budget); BF16 inference stays close to the FP32 network."""
+
+    _, ra, rs = trained
+    for rep in (ra, rs):
+        b, f = rep.held_out["bf16"], rep.held_out["f32"]
+        assert b["radiance_rel_mean"] < 0.1, rep.held_out
+        assert abs(b["radiance_rel_mean"] - f["radiance_rel_mean"]) < 0.02, rep.held_out
+        assert rep.loss == [] or rep.loss[-1][1] < 0.2 * rep.loss[0][1]
+    assert ra.held_out["bf16"]["composite_rel_mean"] < 0.05, ra.held_out
+
+
+# ---- frames ---------------------------------------------------------------------------
+def _frame(width, height, altitude_m, zenith_deg, azimuth_deg, seed=7):
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer, scene
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.workloads import CameraView, EARTH_RADIUS_M
+    from planet_renderer_gb300.lighting import LightingState
+
+    v = CameraView(altitude_m, zenith_deg, azimuth_deg)
+    r = AtmosphereRenderer(width, height, earth_baseline())
+    gb = scene.synthesize_gbuffer(width, height, EARTH_RADIUS_M, v.altitude_m, v.basis, v.tangent_half_fov,
+                                  v.sun_local, E, seed=seed, device=r.device)
+    light = LightingState(v.sun_local, AR_DEG, E)
+    r.update(EARTH_RADIUS_M, v.camera_radius_m, v.sun_local.copy(), E, AR_DEG)
+    r.prepare_frame(gb["position_view"], gb["surface_id"], EARTH_RADIUS_M, v.camera_radius_m, v.sun_local, E, AR_DEG,
+                    v.basis, v.tangent_half_fov)
+    args = (EARTH_RADIUS_M, v.camera_radius_m, v.sun_local, E, light.sun_disk_radiance, AR_DEG, v.basis,
+            v.tangent_half_fov, 4.0, 12.0)
+    return r, gb, args, v
+
+
+def _plain(r, gb, args):
+    hdr = torch.zeros_like(gb["scene_hdr"])
+    r.composite(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"], hdr, *args)
+    return hdr
+
+
+def _surrogate(r, gb, args, sg, check_fraction=0.0, scene=None):
+    hdr = torch.zeros_like(gb["scene_hdr"])
+    stats = torch.zeros(8, dtype=torch.float32, device=r.device)
+    r.composite_surrogate(gb["scene_hdr"] if scene is None else scene, gb["space_hdr"], gb["surface_id"],
+                          gb["position_view"], hdr, *args, surrogate=sg, stats=stats, check_fraction=check_fraction,
+                          seed=9)
+    torch.cuda.synchronize()
+    return hdr, stats
+
+
+def test_without_networks_the_surrogate_composite_is_the_plain_one():
+    from planet_renderer_gb300.atmosphere.surrogate import Surrogate
+
+    r, gb, args, _ = _frame(320, 180, 2000.0, 40.0, 30.0)
+    plain = _plain(r, gb, args)
+    got, stats = _surrogate(r, gb, args, Surrogate(None, None))
+    # every surface pixel goes through the queue and the plain integrator
+    np.testing.assert_allclose(got.cpu().numpy(), plain.cpu().numpy(), rtol=2e-5, atol=1e-9)
+    n_surface = int((gb["surface_id"] >= 0).sum())
+    assert int(stats[3]) <= n_surface and int(stats[4]) == 0 and int(stats[5]) == 0
+    r.close()
+
+
+def test_checked_pixels_keep_the_plain_result(trained):
+    """check_fraction = 1 re-integrates every MLP pixel: the frame is the
+    plain frame (sky network off: sky pixels read the LUT as the plain
+    composite does), and every MLP surface pixel was counted and judged."""
+
+    from planet_renderer_gb300.atmosphere.surrogate import Surrogate, stats_summary
+
+    sg_full, _, _ = trained
+    sg = Surrogate(sg_full.aerial, None, sg_full.planet_radius_m, sg_full.top_altitude_m, sg_full.scale_height_range)
+    r, gb, args, _ = _frame(320, 180, 2000.0, 40.0, 30.0)
+    plain = _plain(r, gb, args)
+    got, stats = _surrogate(r, gb, args, sg, check_fraction=1.0)
+    np.testing.assert_allclose(got.cpu().numpy(), plain.cpu().numpy(), rtol=2e-5, atol=1e-9)
+    s = stats_summary(stats)
+    n_surface = int((gb["surface_id"] >= 0).sum())
+    assert s["checked"] == s["mlp_surface"] > 0
+    assert s["mlp_surface"] + s["gated_surface"] <= n_surface
+    assert 0.0 < s["check_rel_mean"] < 0.2
+    r.close()
+
+
+def _fp64_pixels(r, gb, args, v, pixels, diagnostic_view=0, scene=None):
+    """FP64 oracle composite at the given (x, y) pixels (own FP64 LUTs)."""
+
+    from oracle.atm import Oracle
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+
+    o = Oracle("f64")
+    cfg = earth_baseline()
+    R, cr, sun, E_, disk, ar_deg, basis, tanfov, s0, s1 = args
+    alt = cr - R
+    ar = math.radians(ar_deg)
+    tl = o.build_transmittance(cfg, R)
+    ms = o.build_multi_scattering(cfg, R, E_, ar, tl)
+    sv = o.build_sky_view(cfg, R, alt, float(sun[1]), E_, ar, tl, ms)
+    W, H = r.width, r.height
+    ap = np.zeros((cfg.aerial_lut_width, cfg.aerial_lut_height, cfg.aerial_lut_depth, 3))
+    if diagnostic_view == 8:  # the froxel view reads the FP64 aerial volume
+        ap = o.build_aerial(cfg, W, H, R, alt, sun, E_, ar, basis, tanfov, tl, ms)
+    f = {k: gb[k].cpu().numpy().astype(np.float64) for k in ("scene_hdr", "space_hdr", "position_view")}
+    if scene is not None:
+        f["scene_hdr"] = scene
+    plist = (pixels[:, 0].astype(np.int64) * H + pixels[:, 1]).astype(np.int32)
+    hdr, _ = o.composite(cfg, f["scene_hdr"], f["space_hdr"], gb["surface_id"].cpu().numpy(), f["position_view"], R,
+                         alt, alt, sun, E_, disk, ar, basis, tanfov, s0, s1, diagnostic_view, tl, ms, sv, ap,
+                         pixel_list=plist)
+    return hdr[pixels[:, 0], pixels[:, 1]]
+
+
+def _rel(got, ref, floor):
+    return np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor), axis=-1)
+
+
+@pytest.mark.parametrize("altitude,zenith", [(2000.0, 40.0), (50_000.0, 60.0)])
+def test_surrogate_frame_against_fp64(trained, altitude, zenith):
+    """Composite radiance of the surrogate frame against the FP64 oracle at
+    sampled surface pixels; the plain FP32 frame's own error is the yardstick.
+    (The bench states the error of the fully trained networks.)"""
+
+    sg, _, _ = trained
+    r, gb, args, v = _frame(320, 180, altitude, zenith, 30.0)
+    plain = _plain(r, gb, args).cpu().numpy()
+    got, _ = _surrogate(r, gb, args, sg)
+    got = got.cpu().numpy()
+    sid = gb["surface_id"].cpu().numpy()
+    rng = np.random.default_rng(1)
+    xs, ys = np.nonzero(sid >= 0)
+    pick = rng.choice(len(xs), size=min(400, len(xs)), replace=False)
+    pixels = np.stack([xs[pick], ys[pick]], 1)
+    ref = _fp64_pixels(r, gb, args, v, pixels)
+    floor = 1e-4 * np.abs(ref).max()
+    e_mlp = _rel(got[pixels[:, 0], pixels[:, 1]], ref, floor)
+    e_plain = _rel(plain[pixels[:, 0], pixels[:, 1]], ref, floor)
+    assert np.median(e_plain) < 1e-3
+    assert np.mean(e_mlp) < 3e-2, (np.mean(e_mlp), np.quantile(e_mlp, 0.99))
+    r.close()
+
+
+def test_mlp_gains_over_the_froxel_volume(trained):
+    """In-scattering of surface pixels (scene radiance zeroed) from the aerial
+    network against the FP64 limb integrator, and the same from the
+    aerial-perspective froxel volume (AERIAL_FROXEL_ONLY, the method without
+    a network at a comparable per-pixel cost): the network is closer."""
+
+    sg, _, _ = trained
+    r, gb, args, v = _frame(320, 180, 2000.0, 40.0, 30.0)
+    zero = torch.zeros_like(gb["scene_hdr"])
+    got, _ = _surrogate(r, gb, args, sg, scene=zero)
+    froxel = torch.zeros_like(gb["scene_hdr"])
+    r.composite(zero, gb["space_hdr"], gb["surface_id"], gb["position_view"], froxel, *args, 8)  # AERIAL_FROXEL_ONLY
+    sid = gb["surface_id"].cpu().numpy()
+    rng = np.random.default_rng(2)
+    xs, ys = np.nonzero(sid >= 0)
+    pick = rng.choice(len(xs), size=min(400, len(xs)), replace=False)
+    pixels = np.stack([xs[pick], ys[pick]], 1)
+    exact = _fp64_pixels(r, gb, args, v, pixels, diagnostic_view=5)  # AERIAL_SCATTERING: limb integrator
+    floor = 1e-3 * np.abs(exact).max()
+    e_mlp = _rel(got.cpu().numpy()[pixels[:, 0], pixels[:, 1]], exact, floor)
+    e_fx = _rel(froxel.cpu().numpy()[pixels[:, 0], pixels[:, 1]], exact, floor)
+    assert np.mean(e_mlp) < np.mean(e_fx), (np.mean(e_mlp), np.mean(e_fx))
+    r.close()
