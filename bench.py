@@ -57,6 +57,7 @@ COMPOSITE_FLOP_PER_SAMPLE = 406.16
 # DRAM bytes a composite pixel must move: position 12 + surface_id 4 +
 # scene 12 + space 12 read, hdr 12 written (LUTs stay in L2).
 COMPOSITE_BYTES_PER_PIXEL = 52
+MLP_CHECK_FRACTION = 0.01  # share of MLP pixels the plain path re-integrates
 SMS, FP32_LANES = 152, 128
 
 
@@ -408,6 +409,8 @@ def main() -> None:
     parser.add_argument("--no-cpu-baseline", action="store_true")
     parser.add_argument("--no-4k", action="store_true")
     parser.add_argument("--no-batch", action="store_true")
+    parser.add_argument("--no-mlp", action="store_true", help="skip the surrogate frame (training + timing)")
+    parser.add_argument("--mlp-epochs", type=int, default=200, help="surrogate training epochs (2^22 samples)")
     args = parser.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -576,19 +579,140 @@ def _batch(device, args) -> dict:
     return out
 
 
+def _chain_surrogate(r, v, gb, light, sg, stats):
+    """One frame of the surrogate chain: the plain chain with the composite
+    replaced by atm_composite_surrogate (1% of the MLP pixels re-integrated)."""
+
+    from planet_renderer_gb300.atmosphere.workloads import EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG
+
+    sun = v.sun_local
+    r.build_lut("sky_view", planet_radius_m=EARTH_RADIUS_M, camera_altitude_m=float(_f32(v.altitude_m)),
+                sun_zenith_cosine=float(_f32(sun[1])), solar_irradiance=SOLAR_IRRADIANCE,
+                sun_angular_radius_degrees=math.degrees(float(_f32(math.radians(SUN_ANGULAR_RADIUS_DEG)))))
+    r.prepare_frame(gb["position_view"], gb["surface_id"], EARTH_RADIUS_M, v.camera_radius_m, sun, SOLAR_IRRADIANCE,
+                    SUN_ANGULAR_RADIUS_DEG, v.basis, v.tangent_half_fov)
+    r.composite_surrogate(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"], gb["hdr"],
+                          *_composite_args(v, light), surrogate=sg, stats=stats, check_fraction=MLP_CHECK_FRACTION,
+                          seed=SEED)
+
+
+def _capture_fn(frames, device, fn):
+    import torch
+
+    side = torch.cuda.Stream(device)
+    side.wait_stream(torch.cuda.current_stream(device))
+    with torch.cuda.stream(side):
+        for f in frames:  # warm-up outside capture
+            fn(*f)
+    torch.cuda.current_stream(device).wait_stream(side)
+    torch.cuda.synchronize(device)
+    graphs = []
+    for f in frames:
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            fn(*f)
+        graphs.append(g)
+    torch.cuda.synchronize(device)
+    return graphs
+
+
+def _fp64_error(r, cfg, frames, images, n_pixels=1500):
+    """Relative error (max over RGB, floor 1e-4 of the sample's peak) of each
+    camera's image against the FP64 oracle composite at n_pixels random
+    pixels; the oracle builds its own FP64 LUTs."""
+
+    import numpy as np
+
+    from oracle.atm import Oracle
+    from planet_renderer_gb300.atmosphere.workloads import EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG
+
+    o = Oracle("f64")
+    ar = math.radians(SUN_ANGULAR_RADIUS_DEG)
+    tl = o.build_transmittance(cfg, EARTH_RADIUS_M)
+    ms = o.build_multi_scattering(cfg, EARTH_RADIUS_M, SOLAR_IRRADIANCE, ar, tl)
+    W, H = r.width, r.height
+    rng = np.random.default_rng(SEED)
+    per_cam, all_errs = [], {k: [] for k in images[0]}
+    for (v, gb, light), imgs in zip(frames, images):
+        alt = v.altitude_m
+        sv = o.build_sky_view(cfg, EARTH_RADIUS_M, alt, float(v.sun_local[1]), SOLAR_IRRADIANCE, ar, tl, ms)
+        ap = np.zeros((cfg.aerial_lut_width, cfg.aerial_lut_height, cfg.aerial_lut_depth, 3))
+        pix = np.stack([rng.integers(0, W, n_pixels), rng.integers(0, H, n_pixels)], 1)
+        full = {k: gb[k].cpu().numpy().astype(np.float64) for k in ("scene_hdr", "space_hdr", "position_view")}
+        sid = gb["surface_id"].cpu().numpy()
+        plist = (pix[:, 0].astype(np.int64) * H + pix[:, 1]).astype(np.int32)
+        hdr, _ = o.composite(cfg, full["scene_hdr"], full["space_hdr"], sid, full["position_view"], EARTH_RADIUS_M,
+                             alt, alt, v.sun_local, SOLAR_IRRADIANCE, light.sun_disk_radiance, ar, v.basis,
+                             v.tangent_half_fov, 4.0, 12.0, 0, tl, ms, sv, ap, pixel_list=plist)
+        ref = hdr[pix[:, 0], pix[:, 1]]
+        floor = 1e-4 * np.abs(ref).max()
+        cam = {"altitude_m": alt}
+        for name, img in imgs.items():
+            e = np.max(np.abs(img[pix[:, 0], pix[:, 1]] - ref) / np.maximum(np.abs(ref), floor), axis=1)
+            all_errs[name].append(e)
+            cam[name] = {"mean": float(e.mean()), "p99": float(np.quantile(e, 0.99))}
+        per_cam.append(cam)
+    total = {}
+    for name, es in all_errs.items():
+        e = np.concatenate(es)
+        total[name] = {"mean": float(e.mean()), "p99": float(np.quantile(e, 0.99)), "max": float(e.max())}
+    return {"pixels_per_camera": n_pixels, "all": total, "cameras": per_cam}
+
+
 def _frame_4k(device, args) -> dict:
-    """Plain chain at 3840x2160 for the same cameras: frame ms (graph replay)."""
+    """Plain chain and surrogate chain at 3840x2160 for the same cameras:
+    frame ms (graph replay), the surrogate's training, gate statistics and
+    both frames' error against the FP64 oracle."""
+
+    import time
 
     import torch
 
-    r, _, frames = _setup_chain(device, 3840, 2160)
+    from planet_renderer_gb300.atmosphere.surrogate import stats_summary, train_surrogate
+
+    r, cfg, frames = _setup_chain(device, 3840, 2160)
     graphs = _capture(r, frames, device)
     for _ in range(3):
         for g in graphs:
             g.replay()
     steps = max(args.steps // 10, 5)
-    ms = _timed_graph_region(graphs, steps, device)
-    out = {"plain_ms": ms / steps / 3.0, "mlp_ms": None, "steps": steps}
+    plain_ms = _timed_graph_region(graphs, steps, device) / steps / 3.0
+    plain_imgs = []
+    for v, gb, light in frames:
+        _chain(r, v, gb, light)
+        plain_imgs.append(gb["hdr"].cpu().numpy().astype("float64"))
+    del graphs
+    out = {"plain_ms": plain_ms, "mlp_ms": None, "steps": steps}
+    if args.no_mlp:
+        return out
+    t0 = time.perf_counter()
+    sg, reports = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device)
+    train_s = time.perf_counter() - t0
+    stats = torch.zeros(8, dtype=torch.float32, device=device)
+    fn = lambda v, gb, light: _chain_surrogate(r, v, gb, light, sg, stats)
+    graphs = _capture_fn(frames, device, fn)
+    for _ in range(3):
+        for g in graphs:
+            g.replay()
+    mlp_ms = _timed_graph_region(graphs, steps, device) / steps / 3.0
+    stats.zero_()
+    for g in graphs:
+        g.replay()
+    torch.cuda.synchronize(device)
+    gate = stats_summary(stats)
+    images = []
+    for (v, gb, light), plain in zip(frames, plain_imgs):
+        _chain_surrogate(r, v, gb, light, sg, None)
+        images.append({"plain": plain, "mlp": gb["hdr"].cpu().numpy().astype("float64")})
+    err = _fp64_error(r, cfg, frames, images)
+    out.update({
+        "mlp_ms": mlp_ms, "speedup": plain_ms / mlp_ms, "error_vs_fp64": err,
+        "gate": {**gate, "check_fraction": MLP_CHECK_FRACTION},
+        "training": {"seconds": train_s, "samples_per_network": 2**22, "batch": 16384, "epochs": args.mlp_epochs,
+                     "held_out": {("aerial" if k == 1 else "sky"): rep.held_out["bf16"] for k, rep in
+                                  reports.items()}},
+        "networks": "aerial 7->4x64->6, sky 6->3x64->3, SiLU, BF16 mma.sync m16n8k16 with FP32 accumulation",
+    })
     del graphs, r, frames
     torch.cuda.empty_cache()
     return out

@@ -269,12 +269,15 @@ int atm_mlp_get_params(const AtmMlp* mlp, float* dst_device, void* stream);
 int atm_mlp_set_params(AtmMlp* mlp, const float* src_device, void* stream);
 /* Gradient of the batch loss into grad_out (device, n_params floats, may be
  * null) and the summed squared error into loss_out (device float, may be
- * null); parameters unchanged. */
-int atm_mlp_gradient(AtmMlp* mlp, const float* inputs, const float* targets, int64_t n, float* grad_out,
-                     float* loss_out, void* stream);
-/* One Adam step on a batch (inputs n x n_in, targets n x n_out, device). */
-int atm_mlp_train_step(AtmMlp* mlp, const float* inputs, const float* targets, int64_t n, float lr, float beta1,
-                       float beta2, float eps, float* loss_out, void* stream);
+ * null); parameters unchanged.  The loss is the mean over samples and
+ * outputs of weight * (output - target)^2; weights (n x n_out, device) may be
+ * null for all ones. */
+int atm_mlp_gradient(AtmMlp* mlp, const float* inputs, const float* targets, const float* weights, int64_t n,
+                     float* grad_out, float* loss_out, void* stream);
+/* One Adam step on a batch (inputs n x n_in, targets and weights n x n_out,
+ * device; weights may be null). */
+int atm_mlp_train_step(AtmMlp* mlp, const float* inputs, const float* targets, const float* weights, int64_t n,
+                       float lr, float beta1, float beta2, float eps, float* loss_out, void* stream);
 /* Copy the current parameters into the BF16 tensor-core layout. */
 int atm_mlp_pack_bf16(AtmMlp* mlp, void* stream);
 /* outputs (n x n_out) = network(inputs); precision 0 = FP32 CUDA cores,
@@ -323,12 +326,17 @@ typedef struct AtmSurrogate {
   double trained_top_altitude_m;
   double check_fraction; /* share of MLP pixels re-integrated by the plain path */
   double aerial_floor;   /* the aerial network's radiance outputs are
-                            ln(L / E + aerial_floor) ...                       */
+                            ln(L / E + aerial_floor + aerial_floor_t T), T the
+                            segment's transmittance from the LUT ...          */
+  double aerial_floor_t;
   double sky_floor;      /* ... and the sky network's ln(L / E + sky_floor)    */
-  int32_t aerial_per_opacity; /* 1: the aerial output is the in-scattering per
-                            unit of opacity (1 - T), T the segment's
-                            transmittance from the transmittance LUT          */
+  double twilight_cosine; /* gate: |sun cosine| below this at a surface
+                            segment's start, middle or end -> plain path     */
+  double sky_twilight_cosine; /* gate: |sun cosine| at the camera below this ->
+                            sky pixels read the sky-view LUT (e.g. 0.1)       */
+  double limb_degrees;   /* gate: view ray within this of the limb (e.g. 0.5) */
   uint32_t seed;         /* picks the checked pixels                            */
+  uint32_t reserved;
   float* stats;          /* device float[8] accumulated into, or null: checked
                             pixels, sum and max of their relative error, gated
                             surface pixels, MLP surface pixels, MLP sky pixels,
@@ -340,10 +348,10 @@ typedef struct AtmSurrogate {
  * tensor cores, FP32 accumulation).  Surface pixels keep the plain path's
  * transmittance (the two-tap LUT ratio of :1603-1665); the network gives
  * their in-scattering.  The plain integrator remains the
- * per-pixel fallback where a gate trips (view ray within 0.5 deg of the
- * limb; for surface pixels the sun within 0.1 of the local horizon at the
+ * per-pixel fallback where a gate trips (view ray within limb_degrees of the
+ * limb; for surface pixels the sun cosine below twilight_cosine at the
  * segment's start, middle or end; for sky pixels the camera's sun cosine
- * below 0.1 or the camera above the shell), and re-integrates
+ * below sky_twilight_cosine or the camera above the shell), and re-integrates
  * check_fraction of the MLP pixels, whose error goes to stats; those pixels
  * keep the plain result.  Allocates the handle's fallback queue (4 bytes a
  * pixel) on first use; stream-ordered and capturable afterwards. */

@@ -32,13 +32,14 @@ def forward(params, shapes, x):
     return a
 
 
-def loss(params, shapes, x, t):
+def loss(params, shapes, x, t, weights=None):
     y = forward(params, shapes, x)
-    return float(np.mean((y - np.asarray(t, dtype=np.float64)) ** 2))
+    w = 1.0 if weights is None else np.asarray(weights, dtype=np.float64)
+    return float(np.mean(w * (y - np.asarray(t, dtype=np.float64)) ** 2))
 
 
-def gradient(params, shapes, x, t):
-    """d loss / d params, analytic, float64."""
+def gradient(params, shapes, x, t, weights=None):
+    """d loss / d params, analytic, float64; loss = mean(w (y - t)^2)."""
 
     p = np.asarray(params, dtype=np.float64)
     layers = _unpack(p, shapes)
@@ -48,7 +49,8 @@ def gradient(params, shapes, x, t):
         zs.append(z)
         acts.append(z if i == len(layers) - 1 else silu(z))
     y = acts[-1]
-    d = 2.0 * (y - np.asarray(t, dtype=np.float64)) / y.size
+    w = 1.0 if weights is None else np.asarray(weights, dtype=np.float64)
+    d = 2.0 * w * (y - np.asarray(t, dtype=np.float64)) / y.size
     grads = []
     for i in range(len(layers) - 1, -1, -1):
         W, _ = layers[i]
@@ -63,15 +65,15 @@ def gradient(params, shapes, x, t):
     return np.concatenate(flat)
 
 
-def finite_difference(params, shapes, x, t, indices, h=1e-6):
+def finite_difference(params, shapes, x, t, indices, h=1e-6, weights=None):
     p = np.asarray(params, dtype=np.float64).copy()
     out = []
     for i in indices:
         old = p[i]
         p[i] = old + h
-        up = loss(p, shapes, x, t)
+        up = loss(p, shapes, x, t, weights)
         p[i] = old - h
-        dn = loss(p, shapes, x, t)
+        dn = loss(p, shapes, x, t, weights)
         p[i] = old
         out.append((up - dn) / (2 * h))
     return np.array(out)

@@ -800,7 +800,8 @@ ATM_API int atm_mlp_reset_optimizer(AtmMlp* m, void* stream) {
 }
 
 namespace {
-int mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n, float* loss_out, cudaStream_t s) {
+int mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, const float* weights, int64_t n,
+                 float* loss_out, cudaStream_t s) {
   if (!m || !inputs || !targets || n < 1) return fail(ATM_E_INVALID, "invalid MLP gradient arguments");
   const size_t ctas = size_t(atm::mlp_train_ctas(n));
   const size_t need = ctas * size_t(m->shape.n_params);
@@ -818,7 +819,8 @@ int mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n
     ATM_CUDA(cudaMalloc(&m->loss_partial, ctas * sizeof(float)), "loss workspace");
     m->loss_floats = ctas;
   }
-  ATM_CUDA(atm::launch_mlp_grad(m->shape, m->params, inputs, targets, n, m->partial, m->loss_partial, m->grad, s),
+  ATM_CUDA(atm::launch_mlp_grad(m->shape, m->params, inputs, targets, weights, n, m->partial, m->loss_partial,
+                                m->grad, s),
            "MLP forward/backward");
   if (loss_out) {
     ATM_CUDA(atm::launch_reduce_partials(m->loss_partial, int(ctas), 1, loss_out, s), "loss reduction");
@@ -827,10 +829,10 @@ int mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n
 }
 }  // namespace
 
-ATM_API int atm_mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, int64_t n, float* grad_out,
-                             float* loss_out, void* stream) {
+ATM_API int atm_mlp_gradient(AtmMlp* m, const float* inputs, const float* targets, const float* weights, int64_t n,
+                             float* grad_out, float* loss_out, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  int rc = mlp_gradient(m, inputs, targets, n, loss_out, s);
+  int rc = mlp_gradient(m, inputs, targets, weights, n, loss_out, s);
   if (rc) return rc;
   if (grad_out)
     ATM_CUDA(cudaMemcpyAsync(grad_out, m->grad, size_t(m->shape.n_params) * sizeof(float), cudaMemcpyDeviceToDevice,
@@ -839,12 +841,12 @@ ATM_API int atm_mlp_gradient(AtmMlp* m, const float* inputs, const float* target
   return ATM_OK;
 }
 
-ATM_API int atm_mlp_train_step(AtmMlp* m, const float* inputs, const float* targets, int64_t n, float lr, float beta1,
-                               float beta2, float eps, float* loss_out, void* stream) {
+ATM_API int atm_mlp_train_step(AtmMlp* m, const float* inputs, const float* targets, const float* weights, int64_t n,
+                               float lr, float beta1, float beta2, float eps, float* loss_out, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (!(lr > 0.0f) || !(beta1 >= 0.0f && beta1 < 1.0f) || !(beta2 >= 0.0f && beta2 < 1.0f) || !(eps > 0.0f))
     return fail(ATM_E_INVALID, "invalid Adam hyper-parameters");
-  int rc = mlp_gradient(m, inputs, targets, n, loss_out, s);
+  int rc = mlp_gradient(m, inputs, targets, weights, n, loss_out, s);
   if (rc) return rc;
   m->step += 1;
   m->packed_current = false;
@@ -949,7 +951,8 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
   if (!valid_range(sg->scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
   if (!(sg->check_fraction >= 0.0 && sg->check_fraction <= 1.0))
     return fail(ATM_E_INVALID, "check_fraction must be in [0, 1]");
-  if (!(sg->aerial_floor > 0.0 && sg->aerial_floor < 1.0 && sg->sky_floor > 0.0 && sg->sky_floor < 1.0))
+  if (!(sg->aerial_floor > 0.0 && sg->aerial_floor < 1.0 && sg->sky_floor > 0.0 && sg->sky_floor < 1.0 &&
+        sg->aerial_floor_t >= 0.0 && sg->aerial_floor_t < 1.0))
     return fail(ATM_E_INVALID, "radiance floors must be in (0, 1)");
   if (sg->aerial || sg->sky) {
     if (std::fabs(sg->trained_planet_radius_m - planet_radius_m) > 1.0 ||
@@ -975,9 +978,15 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
   const double* r = sg->scale_height_range;
   nets.lhr_n = log_feature(h->params.rayleigh_scale_height_m, r[0], r[1]);
   nets.lhm_n = log_feature(h->params.mie_scale_height_m, r[2], r[3]);
+  if (!(sg->twilight_cosine >= 0.0 && sg->twilight_cosine <= 1.0 && sg->sky_twilight_cosine >= 0.0 &&
+        sg->sky_twilight_cosine <= 1.0 && sg->limb_degrees >= 0.0 && sg->limb_degrees <= 90.0))
+    return fail(ATM_E_INVALID, "gate thresholds out of range");
+  nets.twilight_cos = float(sg->twilight_cosine);
+  nets.sky_twilight_cos = float(sg->sky_twilight_cosine);
+  nets.limb_rad = float(sg->limb_degrees * (kPi / 180.0));
   nets.floor = float(sg->aerial_floor);
+  nets.floor_t = float(sg->aerial_floor_t);
   nets.sky_floor = float(sg->sky_floor);
-  nets.per_opacity = sg->aerial_per_opacity != 0;
   if (!h->queue) {
     const size_t cap = size_t(h->width) * size_t(h->height);
     ATM_CUDA(cudaMalloc(&h->queue, (cap + 2) * sizeof(uint32_t)), "fallback queue");

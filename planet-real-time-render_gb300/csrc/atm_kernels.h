@@ -70,8 +70,10 @@ MlpShape make_mlp_shape(int n_in, int n_hidden, int n_out);
 int mlp_train_ctas(long long n);
 size_t mlp_train_smem_bytes(const MlpShape& m);
 size_t mlp_bf16_bytes(const MlpShape& m);
+// weights: per (sample, output) factors of the squared error, or null
 cudaError_t launch_mlp_grad(const MlpShape& m, const float* params, const float* inputs, const float* targets,
-                            long long n, float* grad_partial, float* loss_partial, float* grad, cudaStream_t s);
+                            const float* weights, long long n, float* grad_partial, float* loss_partial, float* grad,
+                            cudaStream_t s);
 cudaError_t launch_reduce_partials(const float* partial, int rows, int cols, float* out, cudaStream_t s);
 cudaError_t launch_adam(float* params, const float* grad, float* m1, float* m2, int n, float lr, float b1, float b2,
                         float eps, long long step, cudaStream_t s);
@@ -100,8 +102,11 @@ struct SurrogateNets {
   const unsigned char* sky;  // packed BF16 sky network (6 -> 3x64 -> 3) or null
   int ap_bytes, sky_bytes;   // multiples of 16
   float lhr_n, lhm_n;        // the frame's normalised log scale heights
-  float floor, sky_floor;    // outputs are ln(L / E + floor)
-  int per_opacity;           // aerial output is the in-scattering per unit of (1 - T)
+  float floor, floor_t;      // aerial output: ln(L / E + floor + floor_t T)
+  float sky_floor;           // sky output: ln(L / E + sky_floor)
+  float twilight_cos;        // gate: |sun cosine| at a surface segment below this -> plain path
+  float sky_twilight_cos;    // gate: |sun cosine| at the camera below this -> sky-view LUT
+  float limb_rad;            // gate: view ray within this of the limb -> plain path
 };
 // Pixels the surrogate composite hands to the plain integrator: entry =
 // kind << 30 | (y * width + x).  count and next are reset by each frame.

@@ -101,7 +101,8 @@ __device__ void dense_forward(const float* __restrict__ in, int in_stride, int i
 // gradient of the batch loss (every parameter) and its squared-error sum.
 __global__ void __launch_bounds__(kThreads) k_mlp_grad(MlpShape m, const float* __restrict__ params,
                                                        const float* __restrict__ inputs,
-                                                       const float* __restrict__ targets, long long n,
+                                                       const float* __restrict__ targets,
+                                                       const float* __restrict__ weights, long long n,
                                                        float inv_count, float* __restrict__ grad_partial,
                                                        float* __restrict__ loss_partial) {
   extern __shared__ float sm[];
@@ -144,8 +145,9 @@ __global__ void __launch_bounds__(kThreads) k_mlp_grad(MlpShape m, const float* 
     float g = 0.0f;
     if (base + s < n) {
       const float d = sm[L.y + s * (m.n_out + 1) + o] - targets[(base + s) * m.n_out + o];
-      sq += d * d;
-      g = 2.0f * d * inv_count;
+      const float w = weights != nullptr ? weights[(base + s) * m.n_out + o] : 1.0f;
+      sq += w * d * d;
+      g = 2.0f * w * d * inv_count;
     }
     sm[L.y + s * (m.n_out + 1) + o] = g;
   }
@@ -267,20 +269,23 @@ size_t mlp_bf16_bytes(const MlpShape& m) {
 
 namespace {
 
+// Hidden layers are stored with W and b halved (exact in BF16), so their
+// accumulators hold z / 2 for the packed SiLU of mlp_tile_bf16.
 __global__ void k_pack_bf16(MlpShape m, const float* __restrict__ params, unsigned char* __restrict__ packed) {
   size_t off = 0;
   for (int l = 0; l < m.n_layers; ++l) {
     const int in = m.in_dim[l], out = m.out_dim[l];
     const int row = mlp_bf16_layer_row(in), op = mlp_bf16_out_pad(out);
+    const float scale = l + 1 < m.n_layers ? 0.5f : 1.0f;
     __nv_bfloat16* W = reinterpret_cast<__nv_bfloat16*>(packed + off);
     for (int i = threadIdx.x; i < op * row; i += blockDim.x) {
       const int j = i / row, k = i % row;
       const float v = (j < out && k < in) ? params[m.off_w[l] + j * in + k] : 0.0f;
-      W[i] = __float2bfloat16_rn(v);
+      W[i] = __float2bfloat16_rn(v * scale);
     }
     off += size_t(op) * row * 2;
     float* b = reinterpret_cast<float*>(packed + off);
-    for (int j = threadIdx.x; j < op; j += blockDim.x) b[j] = j < out ? params[m.off_b[l] + j] : 0.0f;
+    for (int j = threadIdx.x; j < op; j += blockDim.x) b[j] = j < out ? params[m.off_b[l] + j] * scale : 0.0f;
     off += size_t(op) * 4;
   }
 }
@@ -342,13 +347,14 @@ int mlp_train_ctas(long long n) { return int((n + kS - 1) / kS); }
 size_t mlp_train_smem_bytes(const MlpShape& m) { return size_t(train_smem(m).total) * sizeof(float); }
 
 cudaError_t launch_mlp_grad(const MlpShape& m, const float* params, const float* inputs, const float* targets,
-                            long long n, float* grad_partial, float* loss_partial, float* grad, cudaStream_t s) {
+                            const float* weights, long long n, float* grad_partial, float* loss_partial, float* grad,
+                            cudaStream_t s) {
   const size_t smem = mlp_train_smem_bytes(m);
   cudaError_t e = cudaFuncSetAttribute(k_mlp_grad, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) return e;
   const int ctas = mlp_train_ctas(n);
   const float inv = 1.0f / float(double(n) * m.n_out);
-  k_mlp_grad<<<ctas, kThreads, smem, s>>>(m, params, inputs, targets, n, inv, grad_partial, loss_partial);
+  k_mlp_grad<<<ctas, kThreads, smem, s>>>(m, params, inputs, targets, weights, n, inv, grad_partial, loss_partial);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_reduce_partials<<<(m.n_params + 255) / 256, 256, 0, s>>>(grad_partial, ctas, m.n_params, grad);

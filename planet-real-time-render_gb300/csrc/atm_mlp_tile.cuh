@@ -14,7 +14,8 @@ __host__ __device__ inline int mlp_bf16_out_pad(int out_dim) { return ((out_dim 
 
 // Packed weights: layer l as bf16 [out_pad][in_pad + 8] (in_pad a multiple
 // of 16, out_pad of 8, zero padded; the +8 bf16 row padding makes a warp's
-// fragment loads conflict-free) followed by fp32 biases [out_pad].
+// fragment loads conflict-free) followed by fp32 biases [out_pad].  Hidden
+// layers hold W / 2 and b / 2 (see silu_half_bf16x2); the output layer W, b.
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(
       "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
@@ -26,12 +27,19 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t*>(&v);
 }
-// SiLU via tanh: z * sigmoid(z) = 0.5 z (1 + tanh(z / 2)), one MUFU op.
-__device__ __forceinline__ float silu_fast(float z) {
-  float th;
-  const float hz = 0.5f * z;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(th) : "f"(hz));
-  return fmaf(hz, th, hz);
+// SiLU of two pre-activations given as halves h = z / 2 (the packed hidden
+// layers are halved): z sigmoid(z) = h (1 + tanh h) = h + h tanh(h) in FP32
+// (tanh.approx.f32, one MUFU op each), rounded once into the packed BF16
+// pair that feeds the next layer.  (A packed tanh.approx.bf16x2 / fma.bf16x2
+// form halves the MUFU work but costs the networks up to 7x their held-out
+// radiance error: the activations would be rounded three times.)
+__device__ __forceinline__ float silu_half(float h) {
+  float t;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(t) : "f"(h));
+  return fmaf(h, t, h);
+}
+__device__ __forceinline__ uint32_t silu_half_bf16x2(float h_lo, float h_hi) {
+  return pack_bf16(silu_half(h_lo), silu_half(h_hi));
 }
 
 
@@ -66,10 +74,10 @@ __device__ __forceinline__ void mlp_tile_bf16(const unsigned char* __restrict__ 
     }
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
-      a[ks][0] = pack_bf16(silu_fast(c[2 * ks][0]), silu_fast(c[2 * ks][1]));
-      a[ks][1] = pack_bf16(silu_fast(c[2 * ks][2]), silu_fast(c[2 * ks][3]));
-      a[ks][2] = pack_bf16(silu_fast(c[2 * ks + 1][0]), silu_fast(c[2 * ks + 1][1]));
-      a[ks][3] = pack_bf16(silu_fast(c[2 * ks + 1][2]), silu_fast(c[2 * ks + 1][3]));
+      a[ks][0] = silu_half_bf16x2(c[2 * ks][0], c[2 * ks][1]);
+      a[ks][1] = silu_half_bf16x2(c[2 * ks][2], c[2 * ks][3]);
+      a[ks][2] = silu_half_bf16x2(c[2 * ks + 1][0], c[2 * ks + 1][1]);
+      a[ks][3] = silu_half_bf16x2(c[2 * ks + 1][2], c[2 * ks + 1][3]);
     }
     w += size_t(kMlpH) * in0_row * 2 + kMlpH * 4;
   }
@@ -94,10 +102,10 @@ __device__ __forceinline__ void mlp_tile_bf16(const unsigned char* __restrict__ 
     }
 #pragma unroll
     for (int ks = 0; ks < 4; ++ks) {
-      a[ks][0] = pack_bf16(silu_fast(c[2 * ks][0]), silu_fast(c[2 * ks][1]));
-      a[ks][1] = pack_bf16(silu_fast(c[2 * ks][2]), silu_fast(c[2 * ks][3]));
-      a[ks][2] = pack_bf16(silu_fast(c[2 * ks + 1][0]), silu_fast(c[2 * ks + 1][1]));
-      a[ks][3] = pack_bf16(silu_fast(c[2 * ks + 1][2]), silu_fast(c[2 * ks + 1][3]));
+      a[ks][0] = silu_half_bf16x2(c[2 * ks][0], c[2 * ks][1]);
+      a[ks][1] = silu_half_bf16x2(c[2 * ks][2], c[2 * ks][3]);
+      a[ks][2] = silu_half_bf16x2(c[2 * ks + 1][0], c[2 * ks + 1][1]);
+      a[ks][3] = silu_half_bf16x2(c[2 * ks + 1][2], c[2 * ks + 1][3]);
     }
     w += size_t(kMlpH) * kRow * 2 + kMlpH * 4;
   }

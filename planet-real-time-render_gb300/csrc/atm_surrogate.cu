@@ -185,8 +185,9 @@ __device__ __forceinline__ float color_error(f3 got, f3 ref, f3 E) {
 }
 
 // Radiance of a network's log output ln(L / E + floor), per channel.
-__device__ __forceinline__ f3 net_radiance(const float (&y)[8], const float* E, float floor) {
-  return vmax(mk((__expf(y[0]) - floor) * E[0], (__expf(y[1]) - floor) * E[1], (__expf(y[2]) - floor) * E[2]), 0.0f);
+__device__ __forceinline__ f3 net_radiance(const float (&y)[8], const float* E, f3 floor) {
+  return vmax(mk((__expf(y[0]) - floor.x) * E[0], (__expf(y[1]) - floor.y) * E[1], (__expf(y[2]) - floor.z) * E[2]),
+              0.0f);
 }
 
 enum PixelKind : int { kNone = 0, kSurfMlp, kSurfPlain, kSurfEmpty, kSkyMlp, kSkyLut };
@@ -213,8 +214,8 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
   const size_t o = e * L.channels;
   const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
   const f3 ray = pixel_ray(L, A, cx, cy).ray;
-  const float kHalfDeg = 0.5f * 0.0174532925f;
-  const bool near_limb = fabsf(acosf(clampf(ray.y, -1.0f, 1.0f)) - sky_horizon_zenith(A.cam_alt, A.bottom)) < kHalfDeg;
+  const bool near_limb =
+      fabsf(acosf(clampf(ray.y, -1.0f, 1.0f)) - sky_horizon_zenith(A.cam_alt, A.bottom)) < nets.limb_rad;
 
   int kind = kNone;
   float fx[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -236,20 +237,20 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
         const f3 tv = ray - up * mu_v, ts = F.sun - up * mu_s;
         const float nv = norm(tv), ns = norm(ts);
         const float cphi = (nv > 1e-6f && ns > 1e-6f) ? dot(tv, ts) / (nv * ns) : 1.0f;
-        // twilight gate: the sun within 0.1 of the local horizon at the start, middle or end
+        // twilight gate: the sun cosine small at the start, middle or end
         float mu_min = fabsf(mu_s);
         for (int k = 1; k <= 2; ++k) {
           const float t = start + (end - start) * 0.5f * float(k);
           const f3 pt = mk(ray.x * t, o_y + ray.y * t, ray.z * t);
           mu_min = mn(mu_min, fabsf(dot(F.sun, pt) / mx(norm(pt), 1.0f)));
         }
-        kind = mu_min < 0.1f ? kSurfPlain : kSurfMlp;
+        kind = mu_min < nets.twilight_cos ? kSurfPlain : kSurfMlp;
         geometry_features(P, A.bottom, hs, mu_v, mu_s, cphi, fx);
         fx[4] = nets.lhr_n;
         fx[5] = nets.lhm_n;
         fx[6] = 2.0f * __logf(clampf(end - start, 1.0f, kSurrogateMaxLength)) / logf(kSurrogateMaxLength) - 1.0f;
       }
-    } else if (nets.sky != nullptr && A.cam_alt <= P.top && fabsf(F.sun.y) >= 0.1f && !near_limb) {
+    } else if (nets.sky != nullptr && A.cam_alt <= P.top && fabsf(F.sun.y) >= nets.sky_twilight_cos && !near_limb) {
       kind = kSkyMlp;
       const float vl = sqrtf(ray.x * ray.x + ray.z * ray.z), sl = sqrtf(F.sun.x * F.sun.x + F.sun.z * F.sun.z);
       const float cphi = (vl > 1e-6f && sl > 1e-6f) ? (ray.x * F.sun.x + ray.z * F.sun.z) / (vl * sl) : 1.0f;
@@ -281,17 +282,16 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
     f3 color = ld3(scene + o);
     if (kind == kSurfMlp) {
       // transmittance: the plain path's own two-tap LUT ratio (:1603-1665);
-      // in-scattering: the network, optionally per unit of (1 - T)
+      // in-scattering: the network, ln(L / E + floor + floor_t T)
       const f3 Tm = surface_segment_t(P, F, camera_ray_geom(P, A.bottom, A.cam_alt, ray), ray, start, end);
-      f3 Lm = net_radiance(yv, A.E, nets.floor);
-      if (nets.per_opacity) Lm = Lm * (splat(1.0f) - Tm);
+      const f3 Lm = net_radiance(yv, A.E, splat(nets.floor) + Tm * nets.floor_t);
       color = Lm + color * Tm;
       if (check_pixel(x, y, Q.seed, Q.check_fraction)) {
         queued = true;
         qkind = kQueueSurfaceCheck;
       }
     } else if (kind == kSkyMlp) {
-      const f3 sky = net_radiance(yv, A.E, nets.sky_floor);
+      const f3 sky = net_radiance(yv, A.E, splat(nets.sky_floor));
       color = composite_sky_with(P, F, A, sky, ray, color, ld3(space + o), float(L.height));
       if (check_pixel(x, y, Q.seed, Q.check_fraction)) {
         queued = true;

@@ -150,9 +150,13 @@ class AtmSurrogate(ctypes.Structure):
         ("trained_top_altitude_m", ctypes.c_double),
         ("check_fraction", ctypes.c_double),
         ("aerial_floor", ctypes.c_double),
+        ("aerial_floor_t", ctypes.c_double),
         ("sky_floor", ctypes.c_double),
-        ("aerial_per_opacity", ctypes.c_int32),
+        ("twilight_cosine", ctypes.c_double),
+        ("sky_twilight_cosine", ctypes.c_double),
+        ("limb_degrees", ctypes.c_double),
         ("seed", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
         ("stats", ctypes.c_void_p),
     ]
 
@@ -203,8 +207,8 @@ SIGNATURES = {
     "atm_mlp_reset_optimizer": (ctypes.c_int, [_P, _P]),
     "atm_mlp_get_params": (ctypes.c_int, [_P, _P, _P]),
     "atm_mlp_set_params": (ctypes.c_int, [_P, _P, _P]),
-    "atm_mlp_gradient": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P, _P, _P]),
-    "atm_mlp_train_step": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+    "atm_mlp_gradient": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, _P, _P, _P]),
+    "atm_mlp_train_step": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
                                           ctypes.c_float, ctypes.c_float, _P, _P]),
     "atm_mlp_pack_bf16": (ctypes.c_int, [_P, _P]),
     "atm_mlp_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _I32, _P]),

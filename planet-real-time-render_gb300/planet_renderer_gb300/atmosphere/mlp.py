@@ -93,22 +93,35 @@ class Mlp:
         return m
 
     # -- training ------------------------------------------------------------------
-    def gradient(self, inputs: torch.Tensor, targets: torch.Tensor):
-        """(gradient of the batch MSE, summed squared error); no update."""
+    def _weights(self, weights, n):
+        if weights is None:
+            return None
+        w = self._check_io(weights, self.n_out, "weights")
+        if w.shape[0] != n:
+            raise ValueError("weights must have one row per sample")
+        return w
+
+    def gradient(self, inputs: torch.Tensor, targets: torch.Tensor, weights: torch.Tensor | None = None):
+        """(gradient of the batch's mean weighted squared error, summed
+        weighted squared error); no update."""
 
         x = self._check_io(inputs, self.n_in, "inputs")
         y = self._check_io(targets, self.n_out, "targets")
+        w = self._weights(weights, x.shape[0])
         g = torch.empty(self.n_params, dtype=torch.float32, device=self.device)
-        _native.check(self._lib.atm_mlp_gradient(self._handle, self._p(x), self._p(y), x.shape[0], self._p(g),
+        _native.check(self._lib.atm_mlp_gradient(self._handle, self._p(x), self._p(y),
+                                                 None if w is None else self._p(w), x.shape[0], self._p(g),
                                                  self._p(self._loss), self._s()))
         return g, self._loss.clone()
 
-    def train_step(self, inputs, targets, lr=1e-3, betas=(0.9, 0.999), eps=1e-8) -> torch.Tensor:
-        """One Adam step; returns the batch's summed squared error (device)."""
+    def train_step(self, inputs, targets, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, weights=None) -> torch.Tensor:
+        """One Adam step; returns the batch's summed (weighted) squared error (device)."""
 
         x = self._check_io(inputs, self.n_in, "inputs")
         y = self._check_io(targets, self.n_out, "targets")
-        _native.check(self._lib.atm_mlp_train_step(self._handle, self._p(x), self._p(y), x.shape[0], float(lr),
+        w = self._weights(weights, x.shape[0])
+        _native.check(self._lib.atm_mlp_train_step(self._handle, self._p(x), self._p(y),
+                                                   None if w is None else self._p(w), x.shape[0], float(lr),
                                                    float(betas[0]), float(betas[1]), float(eps), self._p(self._loss),
                                                    self._s()))
         self._packed = False

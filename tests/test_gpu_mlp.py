@@ -15,8 +15,9 @@ def _net(n_in, n_hidden, n_out, seed=1):
     return Mlp(n_in, n_hidden, n_out, seed=seed)
 
 
-@pytest.mark.parametrize("shape", [(6, 3, 3), (7, 4, 6), (3, 1, 2)])
-def test_gradient_matches_fp64_oracle(shape):
+@pytest.mark.parametrize("shape,weighted", [((6, 3, 3), False), ((7, 4, 6), False), ((3, 1, 2), False),
+                                            ((7, 4, 6), True)])
+def test_gradient_matches_fp64_oracle(shape, weighted):
     import torch
 
     from oracle import mlp_fp64
@@ -28,14 +29,16 @@ def test_gradient_matches_fp64_oracle(shape):
     n = 1000  # several training CTAs and a ragged last tile
     x = rng.uniform(-1.0, 1.0, (n, n_in)).astype(np.float32)
     t = rng.normal(0.0, 1.0, (n, n_out)).astype(np.float32)
-    g, sq = net.gradient(torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda"))
+    w = rng.uniform(0.0, 2.0, (n, n_out)).astype(np.float32) if weighted else None
+    g, sq = net.gradient(torch.as_tensor(x, device="cuda"), torch.as_tensor(t, device="cuda"),
+                         None if w is None else torch.as_tensor(w, device="cuda"))
     params = net.params().cpu().numpy().astype(np.float64)
     shapes = layer_shapes(n_in, n_hidden, n_out)
-    ref = mlp_fp64.gradient(params, shapes, x, t)
+    ref = mlp_fp64.gradient(params, shapes, x, t, w)
     got = g.cpu().numpy().astype(np.float64)
     scale = np.abs(ref).max()
     assert np.max(np.abs(got - ref)) <= 1e-4 * scale, np.max(np.abs(got - ref)) / scale
-    ref_sq = np.sum((mlp_fp64.forward(params, shapes, x) - t) ** 2)
+    ref_sq = np.sum((1.0 if w is None else w) * (mlp_fp64.forward(params, shapes, x) - t) ** 2)
     assert abs(float(sq.item()) - ref_sq) <= 1e-4 * ref_sq
     net.close()
 

@@ -5,7 +5,11 @@ from __future__ import annotations
 import numpy as np
 
 
-def test_fp64_analytic_gradient_matches_finite_differences():
+import pytest
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_fp64_analytic_gradient_matches_finite_differences(weighted):
     from oracle import mlp_fp64
     from planet_renderer_gb300.atmosphere.mlp import layer_shapes
 
@@ -15,7 +19,8 @@ def test_fp64_analytic_gradient_matches_finite_differences():
     params = rng.normal(0.0, 0.3, n)
     x = rng.uniform(-1, 1, (40, 7))
     t = rng.normal(0.0, 1.0, (40, 6))
-    g = mlp_fp64.gradient(params, shapes, x, t)
+    w = rng.uniform(0.0, 2.0, (40, 6)) if weighted else None
+    g = mlp_fp64.gradient(params, shapes, x, t, w)
     idx = rng.choice(n, 60, replace=False)
-    fd = mlp_fp64.finite_difference(params, shapes, x, t, idx)
+    fd = mlp_fp64.finite_difference(params, shapes, x, t, idx, weights=w)
     np.testing.assert_allclose(g[idx], fd, rtol=1e-5, atol=1e-8)
