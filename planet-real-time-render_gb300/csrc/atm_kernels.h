@@ -123,7 +123,7 @@ struct SurrogateQueue {
 // pixels, gated sky pixels (sky-view LUT)
 constexpr int kSurrogateStats = 8;
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
-                               const float E[3], float ar, float* features, float* targets,
+                               float top_fraction, const float E[3], float ar, float* features, float* targets,
                                unsigned long long* counter, cudaStream_t s);
 size_t surrogate_smem_bytes(const SurrogateNets& nets);
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,

@@ -57,13 +57,22 @@ __device__ __forceinline__ uint32_t sky_view_texel(const DevParams& P, const Fra
   float zen = sky_v_to_zenith(vv, sky_horizon_zenith(sh, bottom));
   float vs, vc, saz, caz;
   sincosf(zen, &vs, &vc);
-  if (far_camera(P, bottom, sh) && vv >= 0.5f) {
-    // below the horizon seen from above the shell: the nadir angle
-    // pi - zen = (pi - hz)(1 - local^2) of the same mapping keeps the digits
-    // that zen itself, near pi, loses (pi - hz = acos(rho / r))
-    const float local = 2.0f * vv - 1.0f;
-    const float nadir = acosf(clampf(shell_rho(sh, bottom) / mx(bottom + sh, 1.0f), 0.0f, 1.0f)) *
-                        (1.0f - local * local);
+  if (far_camera(P, bottom, sh)) {
+    // seen from many planet radii the whole planet spans a few degrees
+    // around the nadir: the same mapping in nadir angles keeps the digits
+    // that zen itself, near pi, loses.  The horizon's nadir angle
+    // pi - hz = acos(rho / r) = asin(R / r): acos of rho / r ~ 1 amplifies one
+    // float ulp of its argument to ~2e-6 rad (and 1e-7 rad of direction
+    // moves a limb texel's radiance by 0.2%); asin of R / r is well conditioned
+    const float nh = asinf(clampf(__fdiv_rn(bottom, bottom + sh), 0.0f, 1.0f));
+    float nadir;
+    if (vv >= 0.5f) {
+      const float local = 2.0f * vv - 1.0f;
+      nadir = nh * (1.0f - local * local);  // pi - (hz + (pi - hz) local^2)
+    } else {
+      const float inv = 1.0f - 2.0f * vv;
+      nadir = nh + (kPiF - nh) * (inv * inv);  // pi - hz (1 - inv^2)
+    }
     sincosf(nadir, &vs, &vc);
     vc = -vc;
   }

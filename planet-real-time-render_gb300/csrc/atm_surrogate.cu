@@ -74,9 +74,12 @@ __device__ f3 sky_radiance(const DevParams& P, const Frame& F, float h, f3 ray) 
   return vmax(acc.L, 0.0f);
 }
 
+// top_fraction (aerial): share of samples whose segment starts at the shell
+// top (feature 0 = 1), where every segment seen from above the shell starts.
 __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __restrict__ sets, int n_sets, int kind,
-                                                     long long n, unsigned long long seed, f3 E, float ar,
-                                                     float* __restrict__ features, float* __restrict__ targets,
+                                                     long long n, unsigned long long seed, float top_fraction, f3 E,
+                                                     float ar, float* __restrict__ features,
+                                                     float* __restrict__ targets,
                                                      unsigned long long* __restrict__ counter) {
   const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
   uint32_t samples = 0;
@@ -86,6 +89,7 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
     const float R = S.bottom;
     float x[8];
     for (int k = 0; k < 4; ++k) x[k] = 2.0f * uniform01(seed, i, k + 1) - 1.0f;
+    if (kind == 1 && uniform01(seed, i, 6) < top_fraction) x[0] = 1.0f;
     // invert the feature maps
     const float h = P.top * 0.25f * (x[0] + 1.0f) * (x[0] + 1.0f);
     const float zen = sky_v_to_zenith(0.5f * (x[1] + 1.0f), sky_horizon_zenith(h, R));
@@ -399,10 +403,10 @@ __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
 }  // namespace
 
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
-                               const float E[3], float ar, float* features, float* targets,
+                               float top_fraction, const float E[3], float ar, float* features, float* targets,
                                unsigned long long* counter, cudaStream_t s) {
   const f3 e3 = {E[0], E[1], E[2]};
-  k_gen_samples<<<unsigned((n + 127) / 128), 128, 0, s>>>(sets, n_sets, kind, n, seed, e3, ar,
+  k_gen_samples<<<unsigned((n + 127) / 128), 128, 0, s>>>(sets, n_sets, kind, n, seed, top_fraction, e3, ar,
                                                          features, targets, counter);
   return cudaGetLastError();
 }

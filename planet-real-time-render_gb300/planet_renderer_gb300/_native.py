@@ -212,8 +212,8 @@ SIGNATURES = {
                                           ctypes.c_float, ctypes.c_float, _P, _P]),
     "atm_mlp_pack_bf16": (ctypes.c_int, [_P, _P]),
     "atm_mlp_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _I32, _P]),
-    "atm_surrogate_samples": (ctypes.c_int, [_P, _I32, ctypes.c_int64, ctypes.c_uint64, ctypes.c_double * 4, _P, _P,
-                                             _P]),
+    "atm_surrogate_samples": (ctypes.c_int, [_P, _I32, ctypes.c_int64, ctypes.c_uint64, _D, ctypes.c_double * 4, _P,
+                                             _P, _P]),
     "atm_composite_surrogate": (
         ctypes.c_int,
         [_P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, c_double3, _D, c_double9,
