@@ -310,12 +310,20 @@ int atm_mlp_forward(const AtmMlp* mlp, const float* inputs, float* outputs, int6
  * of a batch (their transmittance and multi-scattering LUTs; the sets must
  * share the planet radius and the shell top).  Features are uniform over the
  * box above, drawn per sample index from `seed` (sample i does not depend on
- * n), the parameter set uniform among the batch's; for the aerial kind a
- * share shell_top_fraction of the samples starts at the shell top (feature 0
- * = 1), where every segment seen from a camera above the shell starts.
- * scale_height_range: H_R min, max, H_M min, max in metres.  features: n x 6
- * (sky) or n x 7 (aerial) floats, targets n x 3 or n x 6, device. */
-int atm_surrogate_samples(AtmBatch* batch, int32_t kind, int64_t n, uint64_t seed, double shell_top_fraction,
+ * n), the parameter set uniform among the batch's.  scale_height_range:
+ * H_R min, max, H_M min, max in metres.  features: n x 6 (sky) or n x 7
+ * (aerial) floats, targets n x 3 or n x 6, device.  options (aerial kind,
+ * may be null for uniform sampling) concentrate samples where surface pixels
+ * need them. */
+typedef struct AtmSampleOptions {
+  double shell_top_fraction; /* share of segments starting at the shell top (feature 0 = 1),
+                                where every segment seen from above the shell starts   */
+  double surface_fraction;   /* share of segments ending at an altitude uniform in
+                                [surface_min_m, surface_max_m] (where the ray reaches it) */
+  double surface_min_m;
+  double surface_max_m;
+} AtmSampleOptions;
+int atm_surrogate_samples(AtmBatch* batch, int32_t kind, int64_t n, uint64_t seed, const AtmSampleOptions* options,
                           const double scale_height_range[4], float* features, float* targets, void* stream);
 
 /* Networks and error check of atm_composite_surrogate. */

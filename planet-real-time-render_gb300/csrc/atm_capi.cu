@@ -892,14 +892,22 @@ bool mlp_is(const AtmMlp* m, int n_in, int n_hidden, int n_out) {
 }
 }  // namespace
 
-ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t seed, double shell_top_fraction,
-                                  const double scale_height_range[4], float* features, float* targets,
-                                  void* stream) {
+ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t seed,
+                                  const AtmSampleOptions* options, const double scale_height_range[4], float* features,
+                                  float* targets, void* stream) {
   if (!b || !features || !targets || n < 1) return fail(ATM_E_INVALID, "invalid surrogate sample arguments");
   if (kind != ATM_SURROGATE_SKY && kind != ATM_SURROGATE_AERIAL) return fail(ATM_E_INVALID, "unknown kind %d", kind);
   if (!valid_range(scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
-  if (!(shell_top_fraction >= 0.0 && shell_top_fraction <= 1.0))
-    return fail(ATM_E_INVALID, "shell_top_fraction must be in [0, 1]");
+  atm::SampleShaping shaping{0.0f, 0.0f, 0.0f, 0.0f};
+  if (options) {
+    const AtmSampleOptions& o = *options;
+    if (!(o.shell_top_fraction >= 0.0 && o.shell_top_fraction <= 1.0 && o.surface_fraction >= 0.0 &&
+          o.surface_fraction <= 1.0 && std::isfinite(o.surface_min_m) && std::isfinite(o.surface_max_m) &&
+          o.surface_min_m <= o.surface_max_m))
+      return fail(ATM_E_INVALID, "sample options out of range");
+    shaping = {float(o.shell_top_fraction), float(o.surface_fraction), float(o.surface_min_m),
+               float(o.surface_max_m)};
+  }
   const int n_sets = int(b->params.size());
   for (int i = 1; i < n_sets; ++i)
     if (b->radius[i] != b->radius[0] || b->params[i].top_altitude_m != b->params[0].top_altitude_m)
@@ -924,8 +932,8 @@ ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t
            "sample set upload");
   float ef[3];
   to_f32(b->E, ef, 3);
-  ATM_CUDA(atm::launch_gen_samples(b->d_sets, n_sets, kind, n, seed, float(shell_top_fraction), ef,
-                                   float(b->ar_rad), features, targets, b->d_samples, s),
+  ATM_CUDA(atm::launch_gen_samples(b->d_sets, n_sets, kind, n, seed, shaping, ef, float(b->ar_rad), features,
+                                   targets, b->d_samples, s),
            "surrogate samples");
   // the table is read by the launch: keep the host copy alive until it ran
   ATM_CUDA(cudaStreamSynchronize(s), "surrogate samples");

@@ -122,9 +122,14 @@ struct SurrogateQueue {
 // gated surface pixels (plain integrator), MLP surface pixels, MLP sky
 // pixels, gated sky pixels (sky-view LUT)
 constexpr int kSurrogateStats = 8;
+struct SampleShaping {
+  float top_fraction;      // share of aerial segments starting at the shell top
+  float surface_fraction;  // share ending at an altitude in [surface_min, surface_max]
+  float surface_min, surface_max;
+};
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
-                               float top_fraction, const float E[3], float ar, float* features, float* targets,
-                               unsigned long long* counter, cudaStream_t s);
+                               const SampleShaping& shaping, const float E[3], float ar, float* features,
+                               float* targets, unsigned long long* counter, cudaStream_t s);
 size_t surrogate_smem_bytes(const SurrogateNets& nets);
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,

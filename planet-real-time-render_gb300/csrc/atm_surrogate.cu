@@ -74,11 +74,13 @@ __device__ f3 sky_radiance(const DevParams& P, const Frame& F, float h, f3 ray) 
   return vmax(acc.L, 0.0f);
 }
 
-// top_fraction (aerial): share of samples whose segment starts at the shell
-// top (feature 0 = 1), where every segment seen from above the shell starts.
+// Aerial samples may be shaped toward camera-to-surface segments: a share
+// starts at the shell top (feature 0 = 1; every segment seen from above the
+// shell starts there) and a share ends at a surface altitude, where the ray
+// reaches it (the segment's length then follows from the geometry).
 __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __restrict__ sets, int n_sets, int kind,
-                                                     long long n, unsigned long long seed, float top_fraction, f3 E,
-                                                     float ar, float* __restrict__ features,
+                                                     long long n, unsigned long long seed, SampleShaping shaping,
+                                                     f3 E, float ar, float* __restrict__ features,
                                                      float* __restrict__ targets,
                                                      unsigned long long* __restrict__ counter) {
   const long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x;
@@ -89,7 +91,7 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
     const float R = S.bottom;
     float x[8];
     for (int k = 0; k < 4; ++k) x[k] = 2.0f * uniform01(seed, i, k + 1) - 1.0f;
-    if (kind == 1 && uniform01(seed, i, 6) < top_fraction) x[0] = 1.0f;
+    if (kind == 1 && uniform01(seed, i, 6) < shaping.top_fraction) x[0] = 1.0f;
     // invert the feature maps
     const float h = P.top * 0.25f * (x[0] + 1.0f) * (x[0] + 1.0f);
     const float zen = sky_v_to_zenith(0.5f * (x[1] + 1.0f), sky_horizon_zenith(h, R));
@@ -114,8 +116,19 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
       targets[i * 3 + 2] = logf(L.z + kSurrogateFloor);
     } else {  // aerial: + log length -> log(L/E + floor), optical depth
       const float u = uniform01(seed, i, 5);
-      const float len = expf(u * logf(kSurrogateMaxLength));
+      float len = expf(u * logf(kSurrogateMaxLength));
       x[6] = 2.0f * u - 1.0f;
+      if (uniform01(seed, i, 7) < shaping.surface_fraction) {
+        const float he = shaping.surface_min + (shaping.surface_max - shaping.surface_min) * uniform01(seed, i, 8);
+        float nr, fr;
+        bool hit;
+        shell_roots(h, mu_v, he, R, nr, fr, hit);
+        const float t = nr > 0.0f ? nr : fr;
+        if (hit && t >= 1.0f && t <= kSurrogateMaxLength) {
+          len = t;
+          x[6] = 2.0f * logf(len) / logf(kSurrogateMaxLength) - 1.0f;
+        }
+      }
       f3 L = splat(0.0f), T = splat(1.0f);
       float start, end;
       const RayGeom G = ray_geom(P, R, h, mu_v, sv);
@@ -403,11 +416,11 @@ __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
 }  // namespace
 
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
-                               float top_fraction, const float E[3], float ar, float* features, float* targets,
-                               unsigned long long* counter, cudaStream_t s) {
+                               const SampleShaping& shaping, const float E[3], float ar, float* features,
+                               float* targets, unsigned long long* counter, cudaStream_t s) {
   const f3 e3 = {E[0], E[1], E[2]};
-  k_gen_samples<<<unsigned((n + 127) / 128), 128, 0, s>>>(sets, n_sets, kind, n, seed, top_fraction, e3, ar,
-                                                         features, targets, counter);
+  k_gen_samples<<<unsigned((n + 127) / 128), 128, 0, s>>>(sets, n_sets, kind, n, seed, shaping, e3, ar, features,
+                                                         targets, counter);
   return cudaGetLastError();
 }
 

@@ -141,6 +141,15 @@ class AtmBatchTuning(ctypes.Structure):
     ]
 
 
+class AtmSampleOptions(ctypes.Structure):
+    _fields_ = [
+        ("shell_top_fraction", ctypes.c_double),
+        ("surface_fraction", ctypes.c_double),
+        ("surface_min_m", ctypes.c_double),
+        ("surface_max_m", ctypes.c_double),
+    ]
+
+
 class AtmSurrogate(ctypes.Structure):
     _fields_ = [
         ("aerial", ctypes.c_void_p),
@@ -212,8 +221,8 @@ SIGNATURES = {
                                           ctypes.c_float, ctypes.c_float, _P, _P]),
     "atm_mlp_pack_bf16": (ctypes.c_int, [_P, _P]),
     "atm_mlp_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _I32, _P]),
-    "atm_surrogate_samples": (ctypes.c_int, [_P, _I32, ctypes.c_int64, ctypes.c_uint64, _D, ctypes.c_double * 4, _P,
-                                             _P, _P]),
+    "atm_surrogate_samples": (ctypes.c_int, [_P, _I32, ctypes.c_int64, ctypes.c_uint64,
+                                             ctypes.POINTER(AtmSampleOptions), ctypes.c_double * 4, _P, _P, _P]),
     "atm_composite_surrogate": (
         ctypes.c_int,
         [_P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, c_double3, _D, c_double9,

@@ -43,6 +43,7 @@ SHAPES = {SKY: (6, 3, 3), AERIAL: (7, 4, 6)}  # n_in, hidden layers, n_out
 FLOOR = 1.0e-7        # floor of the generator's targets ln(L / E + FLOOR)
 MAX_LENGTH_M = 2.0e6
 MAX_DEPTH = 30.0
+SURFACE_RANGE_M = (-5000.0, 10000.0)  # surface altitudes of shaped aerial samples
 
 
 @dataclass(frozen=True)
@@ -63,16 +64,19 @@ class TargetSpec:
     # 0 = unweighted.
     surface_radiance: float = 0.0
     depth_weight: float = 1.0
-    # aerial: share of training samples starting at the shell top (feature
-    # 0 = 1), where every segment seen from a camera above the shell starts
+    # aerial sample shaping: share of training segments starting at the shell
+    # top (feature 0 = 1), where every segment seen from a camera above the
+    # shell starts, and share ending at a surface altitude (SURFACE_RANGE_M),
+    # where every surface pixel's segment ends
     shell_top_fraction: float = 0.0
+    surface_fraction: float = 0.0
 
 
 # Aerial defaults from 4K frames against FP64 (three cameras, 2 km - 2000 km):
 # the frame-sensitivity weights cut the 50 km and 2000 km cameras' errors
 # 2-3x (held-out averages over the uniform box hide this), and a quarter of
 # the samples at the shell top serves the cameras above the shell.
-DEFAULT_SPECS = {SKY: TargetSpec(1.0e-4), AERIAL: TargetSpec(1.0e-4, 0.0, 0.02, 0.1, 0.25)}
+DEFAULT_SPECS = {SKY: TargetSpec(1.0e-4), AERIAL: TargetSpec(1.0e-4, 0.0, 0.02, 0.1, 0.25, 0.6)}
 
 
 def loss_weights(kind: int, y: torch.Tensor, spec: TargetSpec):
@@ -136,16 +140,21 @@ class SampleSource:
                                          sun_angular_radius_degrees, device=device)
         self.device = self.builder.device
 
-    def samples(self, kind: int, n: int, seed: int, shell_top_fraction: float = 0.0):
-        """(features, targets) of n samples; ``shell_top_fraction`` of the
-        aerial samples start at the shell top (feature 0 = 1)."""
+    def samples(self, kind: int, n: int, seed: int, shell_top_fraction: float = 0.0, surface_fraction: float = 0.0,
+                surface_range_m=SURFACE_RANGE_M):
+        """(features, targets) of n samples.  Aerial samples: a share
+        ``shell_top_fraction`` starts at the shell top (feature 0 = 1) and a
+        share ``surface_fraction`` ends at an altitude uniform in
+        ``surface_range_m``; the rest is uniform over the input box."""
 
         n_in, _, n_out = SHAPES[kind]
         x = torch.empty((n, n_in), dtype=torch.float32, device=self.device)
         y = torch.empty((n, n_out), dtype=torch.float32, device=self.device)
         rng = (ctypes.c_double * 4)(*self.scale_height_range)
+        opts = _native.AtmSampleOptions(float(shell_top_fraction), float(surface_fraction), float(surface_range_m[0]),
+                                        float(surface_range_m[1]))
         _native.check(self.builder._lib.atm_surrogate_samples(
-            self.builder._handle, int(kind), int(n), int(seed) & (2**64 - 1), float(shell_top_fraction), rng,
+            self.builder._handle, int(kind), int(n), int(seed) & (2**64 - 1), ctypes.byref(opts), rng,
             ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), self.builder._stream()))
         return x, y
 
@@ -218,7 +227,7 @@ def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 
 
     spec = spec or DEFAULT_SPECS[kind]
     n_in, n_hidden, n_out = SHAPES[kind]
-    x, y = source.samples(kind, n_samples, seed, spec.shell_top_fraction)
+    x, y = source.samples(kind, n_samples, seed, spec.shell_top_fraction, spec.surface_fraction)
     t = to_targets(kind, y, spec)
     w = loss_weights(kind, y, spec)
     del y
@@ -252,6 +261,9 @@ def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 
     xh, yh = source.samples(kind, held_out, seed + 7919)
     report.held_out = {"bf16": held_out_error(net, kind, xh, yh, spec, "bf16"),
                        "f32": held_out_error(net, kind, xh, yh, spec, "f32")}
+    if kind == AERIAL and spec.surface_fraction > 0.0:  # segments ending at a surface
+        xs, ys = source.samples(kind, held_out, seed + 7921, spec.shell_top_fraction, 1.0)
+        report.held_out["bf16_surface"] = held_out_error(net, kind, xs, ys, spec, "bf16")
     report.spec = spec
     return net, report
 
