@@ -147,14 +147,14 @@ def _setup_chain(device, width, height):
 
 
 def _chain(r, v, gb, light):
-    """One frame of the plain chain for camera view v (explicit SV rebuild)."""
+    """One frame of the plain chain for camera view v: update (the sky-view
+    LUT rebuilds, its key changes with every camera) -> prepare_frame ->
+    composite, as the reference's frame scheduler calls them."""
 
     from planet_renderer_gb300.atmosphere.workloads import EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG
 
     sun = v.sun_local
-    r.build_lut("sky_view", planet_radius_m=EARTH_RADIUS_M, camera_altitude_m=float(_f32(v.altitude_m)),
-                sun_zenith_cosine=float(_f32(sun[1])), solar_irradiance=SOLAR_IRRADIANCE,
-                sun_angular_radius_degrees=math.degrees(float(_f32(math.radians(SUN_ANGULAR_RADIUS_DEG)))))
+    r.update(EARTH_RADIUS_M, v.camera_radius_m, sun, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG)
     r.prepare_frame(gb["position_view"], gb["surface_id"], EARTH_RADIUS_M, v.camera_radius_m, sun, SOLAR_IRRADIANCE,
                     SUN_ANGULAR_RADIUS_DEG, v.basis, v.tangent_half_fov)
     r.composite(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"], gb["hdr"], EARTH_RADIUS_M,
@@ -410,7 +410,7 @@ def main() -> None:
     parser.add_argument("--no-4k", action="store_true")
     parser.add_argument("--no-batch", action="store_true")
     parser.add_argument("--no-mlp", action="store_true", help="skip the surrogate frame (training + timing)")
-    parser.add_argument("--mlp-epochs", type=int, default=200, help="surrogate training epochs (2^22 samples)")
+    parser.add_argument("--mlp-epochs", type=int, default=400, help="surrogate training epochs (2^22 samples)")
     args = parser.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -586,9 +586,7 @@ def _chain_surrogate(r, v, gb, light, sg, stats):
     from planet_renderer_gb300.atmosphere.workloads import EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG
 
     sun = v.sun_local
-    r.build_lut("sky_view", planet_radius_m=EARTH_RADIUS_M, camera_altitude_m=float(_f32(v.altitude_m)),
-                sun_zenith_cosine=float(_f32(sun[1])), solar_irradiance=SOLAR_IRRADIANCE,
-                sun_angular_radius_degrees=math.degrees(float(_f32(math.radians(SUN_ANGULAR_RADIUS_DEG)))))
+    r.update(EARTH_RADIUS_M, v.camera_radius_m, sun, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG)
     r.prepare_frame(gb["position_view"], gb["surface_id"], EARTH_RADIUS_M, v.camera_radius_m, sun, SOLAR_IRRADIANCE,
                     SUN_ANGULAR_RADIUS_DEG, v.basis, v.tangent_half_fov)
     r.composite_surrogate(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"], gb["hdr"],
@@ -687,6 +685,7 @@ def _frame_4k(device, args) -> dict:
         return out
     t0 = time.perf_counter()
     sg, reports = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device)
+    torch.cuda.synchronize(device)
     train_s = time.perf_counter() - t0
     stats = torch.zeros(8, dtype=torch.float32, device=device)
     fn = lambda v, gb, light: _chain_surrogate(r, v, gb, light, sg, stats)
@@ -709,9 +708,10 @@ def _frame_4k(device, args) -> dict:
         "mlp_ms": mlp_ms, "speedup": plain_ms / mlp_ms, "error_vs_fp64": err,
         "gate": {**gate, "check_fraction": MLP_CHECK_FRACTION},
         "training": {"seconds": train_s, "samples_per_network": 2**22, "batch": 16384, "epochs": args.mlp_epochs,
-                     "held_out": {("aerial" if k == 1 else "sky"): rep.held_out["bf16"] for k, rep in
-                                  reports.items()}},
-        "networks": "aerial 7->4x64->6, sky 6->3x64->3, SiLU, BF16 mma.sync m16n8k16 with FP32 accumulation",
+                     "steps_per_network": reports["sky"].steps,
+                     "held_out": {name: rep.held_out for name, rep in reports.items()}},
+        "networks": "aerial 7->4x64->6 (one for cameras inside the shell, one above it), sky 6->3x64->3; SiLU; "
+                    "BF16 mma.sync m16n8k16 with FP32 accumulation",
     })
     del graphs, r, frames
     torch.cuda.empty_cache()

@@ -281,7 +281,10 @@ int atm_mlp_train_step(AtmMlp* mlp, const float* inputs, const float* targets, c
 /* Copy the current parameters into the BF16 tensor-core layout. */
 int atm_mlp_pack_bf16(AtmMlp* mlp, void* stream);
 /* outputs (n x n_out) = network(inputs); precision 0 = FP32 CUDA cores,
- * 1 = BF16 tensor cores with FP32 accumulation (after atm_mlp_pack_bf16). */
+ * 1 = BF16 tensor cores (mma.sync) with FP32 accumulation, 2 = BF16 on the
+ * 5th-generation tensor cores (tcgen05.mma, accumulators in tensor memory);
+ * 1 and 2 after atm_mlp_pack_bf16.  Precision 2 synchronises `stream` and
+ * returns ATM_E_TIMEOUT if an MMA did not complete in time. */
 int atm_mlp_forward(const AtmMlp* mlp, const float* inputs, float* outputs, int64_t n, int32_t precision,
                     void* stream);
 
@@ -331,6 +334,9 @@ typedef struct AtmSurrogate {
   const AtmMlp* aerial;  /* 7 -> 4 x 64 -> 6, packed (atm_mlp_pack_bf16), or null:
                             plain integrator for every surface pixel            */
   const AtmMlp* sky;     /* 6 -> 3 x 64 -> 3, packed, or null: sky-view LUT    */
+  const AtmMlp* aerial_above_shell; /* 7 -> 4 x 64 -> 6 used instead of aerial
+                            when the camera is above the shell (every segment
+                            then starts at the shell top), or null            */
   double scale_height_range[4];   /* of features 4, 5 (as in training)          */
   double trained_planet_radius_m; /* the networks' planet; the frame must match */
   double trained_top_altitude_m;
@@ -350,12 +356,14 @@ typedef struct AtmSurrogate {
   float* stats;          /* device float[8] accumulated into, or null: checked
                             pixels, sum and max of their relative error, gated
                             surface pixels, MLP surface pixels, MLP sky pixels,
-                            sky-view-LUT sky pixels, 0                          */
+                            sky-view-LUT sky pixels, blocks whose tensor-core
+                            MMA did not complete in time (0)                    */
 } AtmSurrogate;
 
 /* COMPOSITE view of atm_composite with the per-pixel limb integrator replaced
- * by the aerial network and the sky-view lookup by the sky network (BF16
- * tensor cores, FP32 accumulation).  Surface pixels keep the plain path's
+ * by the aerial network and the sky-view lookup by the sky network (BF16 on
+ * the 5th-generation tensor cores, tcgen05.mma, FP32 accumulators in tensor
+ * memory).  Surface pixels keep the plain path's
  * transmittance (the two-tap LUT ratio of :1603-1665); the network gives
  * their in-scattering.  The plain integrator remains the
  * per-pixel fallback where a gate trips (view ray within limb_degrees of the

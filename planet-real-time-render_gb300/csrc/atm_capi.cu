@@ -711,7 +711,9 @@ struct AtmMlp {
   float* loss_partial = nullptr;
   size_t loss_floats = 0;
   void* packed = nullptr;
-  bool packed_current = false;  // packed holds the current parameters
+  void* packed_tc = nullptr;    // tcgen05 layout (atm_mlp_tc.cuh)
+  int* d_error = nullptr;       // set by a tcgen05 kernel whose MMA timed out
+  bool packed_current = false;  // packed / packed_tc hold the current parameters
   long long step = 0;
   int sm_count = 0;
 };
@@ -720,7 +722,7 @@ ATM_API int atm_mlp_destroy(AtmMlp* m) {
   if (!m) return ATM_OK;
   for (void* p : {static_cast<void*>(m->params), static_cast<void*>(m->grad), static_cast<void*>(m->m1),
                   static_cast<void*>(m->m2), static_cast<void*>(m->partial), static_cast<void*>(m->loss_partial),
-                  m->packed})
+                  m->packed, m->packed_tc, static_cast<void*>(m->d_error)})
     if (p) cudaFree(p);
   delete m;
   return ATM_OK;
@@ -755,6 +757,9 @@ ATM_API int atm_mlp_create(int32_t n_in, int32_t n_hidden_layers, int32_t n_out,
   for (float** p : {&m->params, &m->grad, &m->m1, &m->m2})
     if (e == cudaSuccess) e = cudaMalloc(p, np * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&m->packed, atm::mlp_bf16_bytes(m->shape));
+  if (e == cudaSuccess) e = cudaMalloc(&m->packed_tc, atm::mlp_tc_bytes(m->shape));
+  if (e == cudaSuccess) e = cudaMalloc(&m->d_error, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(m->d_error, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMemcpy(m->params, host.data(), np * sizeof(float), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(m->m1, 0, np * sizeof(float));
   if (e == cudaSuccess) e = cudaMemset(m->m2, 0, np * sizeof(float));
@@ -859,6 +864,8 @@ ATM_API int atm_mlp_pack_bf16(AtmMlp* m, void* stream) {
   if (!m) return fail(ATM_E_INVALID, "null AtmMlp");
   ATM_CUDA(atm::launch_mlp_pack_bf16(m->shape, m->params, m->packed, static_cast<cudaStream_t>(stream)),
            "BF16 packing");
+  ATM_CUDA(atm::launch_mlp_pack_tc(m->shape, m->params, m->packed_tc, static_cast<cudaStream_t>(stream)),
+           "BF16 packing (tcgen05 layout)");
   m->packed_current = true;
   return ATM_OK;
 }
@@ -872,8 +879,17 @@ ATM_API int atm_mlp_forward(const AtmMlp* m, const float* inputs, float* outputs
   else if (precision == 1)
     ATM_CUDA(atm::launch_mlp_forward_bf16(m->shape, m->packed, inputs, outputs, n, m->sm_count, s),
              "MLP forward (BF16 tensor cores)");
-  else
-    return fail(ATM_E_INVALID, "precision must be 0 (FP32) or 1 (BF16)");
+  else if (precision == 2) {
+    if (!m->packed_current) return fail(ATM_E_STATE, "network not packed (atm_mlp_pack_bf16)");
+    ATM_CUDA(cudaMemsetAsync(m->d_error, 0, sizeof(int), s), "MLP forward (tcgen05)");
+    ATM_CUDA(atm::launch_mlp_forward_tc(m->shape, m->packed_tc, inputs, outputs, n, m->d_error, m->sm_count, s),
+             "MLP forward (tcgen05)");
+    int err = 0;
+    ATM_CUDA(cudaMemcpyAsync(&err, m->d_error, sizeof(int), cudaMemcpyDeviceToHost, s), "MLP forward (tcgen05)");
+    ATM_CUDA(cudaStreamSynchronize(s), "MLP forward (tcgen05)");
+    if (err) return fail(ATM_E_TIMEOUT, "tcgen05 MMA did not complete in time");
+  } else
+    return fail(ATM_E_INVALID, "precision must be 0 (FP32), 1 (BF16 mma.sync) or 2 (BF16 tcgen05)");
   return ATM_OK;
 }
 
@@ -964,25 +980,28 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
   if (!(sg->aerial_floor > 0.0 && sg->aerial_floor < 1.0 && sg->sky_floor > 0.0 && sg->sky_floor < 1.0 &&
         sg->aerial_floor_t >= 0.0 && sg->aerial_floor_t < 1.0))
     return fail(ATM_E_INVALID, "radiance floors must be in (0, 1)");
-  if (sg->aerial || sg->sky) {
+  if (sg->aerial || sg->sky || sg->aerial_above_shell) {
     if (std::fabs(sg->trained_planet_radius_m - planet_radius_m) > 1.0 ||
         std::fabs(sg->trained_top_altitude_m - h->params.top_altitude_m) > 1.0)
       return fail(ATM_E_INVALID, "the networks were trained for another planet radius or shell top");
   }
   atm::SurrogateNets nets{};
-  if (sg->aerial) {
-    if (!mlp_is(sg->aerial, atm::kSurrogateApIn, atm::kSurrogateApHidden, atm::kSurrogateApOut))
+  // the camera above the shell: every segment starts at the shell top
+  const bool above = camera_radius_m - planet_radius_m > h->params.top_altitude_m;
+  const AtmMlp* aerial = above && sg->aerial_above_shell ? sg->aerial_above_shell : sg->aerial;
+  if (aerial) {
+    if (!mlp_is(aerial, atm::kSurrogateApIn, atm::kSurrogateApHidden, atm::kSurrogateApOut))
       return fail(ATM_E_INVALID, "aerial network must be 7 -> 4 x 64 -> 6");
-    if (!sg->aerial->packed_current) return fail(ATM_E_STATE, "aerial network not packed (atm_mlp_pack_bf16)");
-    nets.ap = static_cast<const unsigned char*>(sg->aerial->packed);
-    nets.ap_bytes = int(atm::mlp_bf16_bytes(sg->aerial->shape));
+    if (!aerial->packed_current) return fail(ATM_E_STATE, "aerial network not packed (atm_mlp_pack_bf16)");
+    nets.ap = static_cast<const unsigned char*>(aerial->packed_tc);
+    nets.ap_bytes = int(atm::mlp_tc_bytes(aerial->shape));
   }
   if (sg->sky) {
     if (!mlp_is(sg->sky, atm::kSurrogateSkyIn, atm::kSurrogateSkyHidden, atm::kSurrogateSkyOut))
       return fail(ATM_E_INVALID, "sky network must be 6 -> 3 x 64 -> 3");
     if (!sg->sky->packed_current) return fail(ATM_E_STATE, "sky network not packed (atm_mlp_pack_bf16)");
-    nets.sky = static_cast<const unsigned char*>(sg->sky->packed);
-    nets.sky_bytes = int(atm::mlp_bf16_bytes(sg->sky->shape));
+    nets.sky = static_cast<const unsigned char*>(sg->sky->packed_tc);
+    nets.sky_bytes = int(atm::mlp_tc_bytes(sg->sky->shape));
   }
   if (nets.ap_bytes % 16 || nets.sky_bytes % 16) return fail(ATM_E_STATE, "packed network size not a multiple of 16");
   const double* r = sg->scale_height_range;

@@ -80,6 +80,11 @@ cudaError_t launch_adam(float* params, const float* grad, float* m1, float* m2, 
 cudaError_t launch_mlp_forward_f32(const MlpShape& m, const float* params, const float* inputs, float* outputs,
                                    long long n, cudaStream_t s);
 cudaError_t launch_mlp_pack_bf16(const MlpShape& m, const float* params, void* packed, cudaStream_t s);
+// tcgen05 path: packed layout of atm_mlp_tc.cuh; *error set if an MMA timed out
+size_t mlp_tc_bytes(const MlpShape& m);
+cudaError_t launch_mlp_pack_tc(const MlpShape& m, const float* params, void* packed, cudaStream_t s);
+cudaError_t launch_mlp_forward_tc(const MlpShape& m, const void* packed, const float* inputs, float* outputs,
+                                  long long n, int* error, int sm_count, cudaStream_t s);
 cudaError_t launch_mlp_forward_bf16(const MlpShape& m, const void* packed, const float* inputs, float* outputs,
                                     long long n, int sm_count, cudaStream_t s);
 
@@ -120,7 +125,8 @@ struct SurrogateQueue {
 };
 // stats: checked pixels, sum of their relative errors, max relative error,
 // gated surface pixels (plain integrator), MLP surface pixels, MLP sky
-// pixels, gated sky pixels (sky-view LUT)
+// pixels, gated sky pixels (sky-view LUT), blocks whose tensor-core MMA timed
+// out (0 unless the hardware misbehaves)
 constexpr int kSurrogateStats = 8;
 struct SampleShaping {
   float top_fraction;      // share of aerial segments starting at the shell top

@@ -14,6 +14,7 @@
 #include <cstdint>
 
 #include "atm_kernels.h"
+#include "atm_mlp_tc.cuh"
 #include "atm_mlp_tile.cuh"
 
 namespace atm {
@@ -290,6 +291,69 @@ __global__ void k_pack_bf16(MlpShape m, const float* __restrict__ params, unsign
   }
 }
 
+// tcgen05 layout of a network (atm_mlp_tc.cuh): weights as K-major core
+// matrices, hidden layers halved.
+__global__ void k_pack_tc(MlpShape m, const float* __restrict__ params, unsigned char* __restrict__ packed) {
+  int off = 0;
+  for (int l = 0; l < m.n_layers; ++l) {
+    const int in = m.in_dim[l], out = m.out_dim[l];
+    const int kp = tc_k_pad(in), np = tc_n_pad(out);
+    const float scale = l + 1 < m.n_layers ? 0.5f : 1.0f;
+    for (int i = threadIdx.x; i < kp * np; i += blockDim.x) {
+      const int n = i / kp, k = i % kp;
+      const float v = (n < out && k < in) ? params[m.off_w[l] + n * in + k] * scale : 0.0f;
+      *reinterpret_cast<__nv_bfloat16*>(packed + off + tc_w_offset(n, k, np)) = __float2bfloat16_rn(v);
+    }
+    float* b = reinterpret_cast<float*>(packed + off + kp * np * 2);
+    for (int j = threadIdx.x; j < np; j += blockDim.x) b[j] = j < out ? params[m.off_b[l] + j] * scale : 0.0f;
+    off += tc_layer_bytes(in, out);
+  }
+}
+
+// Forward of n samples on the tcgen05 path: one tile of 128 samples per
+// block at a time (grid-stride); TMEM: accumulators at column 0, activations
+// at column 128 of a 256-column allocation.  *error is set when an MMA did
+// not complete in time.
+template <int kHidden>
+__global__ void __launch_bounds__(128) k_mlp_forward_tc(MlpShape m, const unsigned char* __restrict__ packed,
+                                                        int packed_bytes, const float* __restrict__ inputs,
+                                                        float* __restrict__ outputs, long long n,
+                                                        int* __restrict__ error) {
+  extern __shared__ __align__(128) unsigned char smw[];
+  __shared__ __align__(8) uint64_t s_mbar;
+  __shared__ uint32_t s_tmem;
+  for (int i = threadIdx.x * 16; i < packed_bytes; i += blockDim.x * 16)
+    *reinterpret_cast<uint4*>(smw + i) = *reinterpret_cast<const uint4*>(packed + i);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor-core reads
+  if (threadIdx.x < 32) tc::alloc(&s_tmem, 256);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&s_mbar, 1);
+    tc::mbar_init_fence();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  TcTile T{s_tmem, s_tmem + 128, &s_mbar, 0u, 0, int(threadIdx.x)};
+  bool ok = true;
+  for (long long base = blockIdx.x * 128LL; base < n; base += gridDim.x * 128LL) {
+    const long long r = base + threadIdx.x;
+    float x[8] = {0, 0, 0, 0, 0, 0, 0, 0}, y[8];
+    if (r < n)
+      for (int k = 0; k < m.n_in; ++k) x[k] = inputs[r * m.n_in + k];
+    ok = mlp_tile_tc<kHidden>(smw, m.n_in, T, x, y) && ok;
+    if (r < n)
+      for (int k = 0; k < m.n_out; ++k) outputs[r * m.n_out + k] = y[k];
+  }
+  if (!ok) atomicExch(error, 1);
+  // before the tensor memory is freed, no MMA of this CTA may be in flight:
+  // after a timed-out wait, wait once more (bounded) for the last commit
+  tc::fence_before_sync();
+  if (__syncthreads_or(!ok)) tc::mbar_wait(&s_mbar, T.phase ^ 1u, kTcWaitTries);
+  __syncthreads();
+  tc::fence_after_sync();
+  if (threadIdx.x < 32) tc::dealloc(s_tmem, 256);
+}
+
 template <int kHidden>
 __global__ void __launch_bounds__(128) k_mlp_forward_bf16(MlpShape m, const unsigned char* __restrict__ packed,
                                                           int packed_bytes, const float* __restrict__ inputs,
@@ -377,6 +441,42 @@ cudaError_t launch_adam(float* params, const float* grad, float* m1, float* m2, 
 cudaError_t launch_mlp_forward_f32(const MlpShape& m, const float* params, const float* inputs, float* outputs,
                                    long long n, cudaStream_t s) {
   k_mlp_forward_f32<<<unsigned((n + 127) / 128), 128, 0, s>>>(m, params, inputs, outputs, n);
+  return cudaGetLastError();
+}
+
+size_t mlp_tc_bytes(const MlpShape& m) {
+  size_t b = 0;
+  for (int l = 0; l < m.n_layers; ++l) b += size_t(tc_layer_bytes(m.in_dim[l], m.out_dim[l]));
+  return b;
+}
+
+cudaError_t launch_mlp_pack_tc(const MlpShape& m, const float* params, void* packed, cudaStream_t s) {
+  k_pack_tc<<<1, 256, 0, s>>>(m, params, static_cast<unsigned char*>(packed));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mlp_forward_tc(const MlpShape& m, const void* packed, const float* inputs, float* outputs,
+                                  long long n, int* error, int sm_count, cudaStream_t s) {
+  const int bytes = int(mlp_tc_bytes(m));
+  const unsigned blocks = unsigned(std::min<long long>((n + 127) / 128, 2LL * sm_count));
+  const auto* p = static_cast<const unsigned char*>(packed);
+  cudaError_t e = cudaSuccess;
+  switch (m.n_layers - 1) {
+    case 1: e = cudaFuncSetAttribute(k_mlp_forward_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e == cudaSuccess) k_mlp_forward_tc<1><<<blocks, 128, bytes, s>>>(m, p, bytes, inputs, outputs, n, error);
+      break;
+    case 2: e = cudaFuncSetAttribute(k_mlp_forward_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e == cudaSuccess) k_mlp_forward_tc<2><<<blocks, 128, bytes, s>>>(m, p, bytes, inputs, outputs, n, error);
+      break;
+    case 3: e = cudaFuncSetAttribute(k_mlp_forward_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e == cudaSuccess) k_mlp_forward_tc<3><<<blocks, 128, bytes, s>>>(m, p, bytes, inputs, outputs, n, error);
+      break;
+    case 4: e = cudaFuncSetAttribute(k_mlp_forward_tc<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      if (e == cudaSuccess) k_mlp_forward_tc<4><<<blocks, 128, bytes, s>>>(m, p, bytes, inputs, outputs, n, error);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  if (e != cudaSuccess) return e;
   return cudaGetLastError();
 }
 

@@ -25,7 +25,7 @@
 #include "atm_device.cuh"
 #include "atm_frame_paths.cuh"
 #include "atm_kernels.h"
-#include "atm_mlp_tile.cuh"
+#include "atm_mlp_tc.cuh"
 
 namespace atm {
 
@@ -148,45 +148,6 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
   warp_count(samples, counter);
 }
 
-// ---- network evaluation for a warp's 32 pixels -----------------------------
-// Features go through shared memory into the mma A-fragment layout and the
-// outputs back to one row per lane.
-struct alignas(16) WarpSlot {
-  uint32_t in[32][4];  // 8 BF16 features per pixel
-  float out[32][8];    // outputs (the first n_out used)
-};
-
-// All 32 lanes call.  x: this lane's 8 features; y: its 8 outputs.
-template <int kHidden>
-__device__ __forceinline__ void warp_mlp(const unsigned char* __restrict__ w, int in0_row, WarpSlot& s,
-                                         const float (&x)[8], float (&y)[8]) {
-  const int lane = threadIdx.x & 31;
-  const int g = lane >> 2, q = lane & 3;
-  __syncwarp();  // an earlier use of the slot is complete
-  *reinterpret_cast<uint4*>(s.in[lane]) =
-      make_uint4(pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]));
-  __syncwarp();
-#pragma unroll 1
-  for (int tile = 0; tile < 2; ++tile) {
-    const uint32_t frag[4] = {s.in[tile * 16 + g][q], s.in[tile * 16 + g + 8][q], 0u, 0u};
-    float t[4];
-    mlp_tile_bf16<kHidden>(w, frag, in0_row, t);
-    *reinterpret_cast<float2*>(&s.out[tile * 16 + g][2 * q]) = make_float2(t[0], t[1]);
-    *reinterpret_cast<float2*>(&s.out[tile * 16 + g + 8][2 * q]) = make_float2(t[2], t[3]);
-  }
-  __syncwarp();
-  const float4 a = *reinterpret_cast<const float4*>(&s.out[lane][0]);
-  const float4 b = *reinterpret_cast<const float4*>(&s.out[lane][4]);
-  y[0] = a.x;
-  y[1] = a.y;
-  y[2] = a.z;
-  y[3] = a.w;
-  y[4] = b.x;
-  y[5] = b.y;
-  y[6] = b.z;
-  y[7] = b.w;
-}
-
 __device__ __forceinline__ bool check_pixel(int x, int y, unsigned seed, float fraction) {
   unsigned h = (unsigned(x) * 0x8DA6B343u) ^ (unsigned(y) * 0xD8163841u) ^ (seed * 0x9E3779B1u);
   h ^= h >> 15;
@@ -209,20 +170,36 @@ __device__ __forceinline__ f3 net_radiance(const float (&y)[8], const float* E, 
 
 enum PixelKind : int { kNone = 0, kSurfMlp, kSurfPlain, kSurfEmpty, kSkyMlp, kSkyLut };
 
+// 256 threads = two tiles of 128 pixels (warps 0-3, 4-7); a pixel is one
+// tensor-memory lane of its tile.  Tensor memory (256 columns): tile t holds
+// its accumulators at column 128 t and its activations at 128 t + 64.
+constexpr uint32_t kSurrogateTmemCols = 256;
+
 __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
     DevParams P, ImageLayout L, CompositeScalars A, const float* __restrict__ scene, const float* __restrict__ space,
     const int32_t* __restrict__ sid, const float* __restrict__ pos, const float4* __restrict__ tlut,
     const float4* __restrict__ mslut, const float4* __restrict__ svlut, SurrogateNets nets, SurrogateQueue Q,
     float* __restrict__ hdr) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  // the aerial network, the sky network, then one slot per warp
+  extern __shared__ __align__(128) unsigned char smem[];  // the aerial network, then the sky network
+  __shared__ __align__(8) uint64_t s_mbar[2];
+  __shared__ uint32_t s_tmem;
   const int wbytes = nets.ap_bytes + nets.sky_bytes;
   for (int i = threadIdx.x * 16; i < wbytes; i += blockDim.x * 16) {
     const unsigned char* src = i < nets.ap_bytes ? nets.ap + i : nets.sky + (i - nets.ap_bytes);
     *reinterpret_cast<uint4*>(smem + i) = __ldg(reinterpret_cast<const uint4*>(src));
   }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor-core reads
+  if (threadIdx.x < 32) tc::alloc(&s_tmem, kSurrogateTmemCols);
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&s_mbar[0], 1);
+    tc::mbar_init(&s_mbar[1], 1);
+    tc::mbar_init_fence();
+  }
+  tc::fence_before_sync();
   __syncthreads();
-  WarpSlot& slot = reinterpret_cast<WarpSlot*>(smem + wbytes)[threadIdx.x >> 5];
+  tc::fence_after_sync();
+  const int tile = threadIdx.x >> 7;
+  TcTile T{s_tmem + 128u * tile, s_tmem + 128u * tile + 64u, &s_mbar[tile], 0u, tile, int(threadIdx.x & 127)};
 
   int x, y;
   const bool inside = tile_pixel(L, x, y);
@@ -279,19 +256,29 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
     }
   }
 
+  // the networks on the tensor cores, each run by the whole block when any
+  // of its pixels needs it (block-uniform: every barrier stays convergent)
   float yv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  if (__any_sync(kAll, kind == kSurfMlp)) {
+  bool tc_ok = true;
+  if (__syncthreads_or(kind == kSurfMlp)) {
     float t[8];
-    warp_mlp<kSurrogateApHidden>(smem, mlp_bf16_layer_row(kSurrogateApIn), slot, fx, t);
+    tc_ok = mlp_tile_tc<kSurrogateApHidden>(smem, kSurrogateApIn, T, fx, t) && tc_ok;
     if (kind == kSurfMlp)
       for (int k = 0; k < 8; ++k) yv[k] = t[k];
   }
-  if (__any_sync(kAll, kind == kSkyMlp)) {
+  if (__syncthreads_or(kind == kSkyMlp)) {
     float t[8];
-    warp_mlp<kSurrogateSkyHidden>(smem + nets.ap_bytes, mlp_bf16_layer_row(kSurrogateSkyIn), slot, fx, t);
+    tc_ok = mlp_tile_tc<kSurrogateSkyHidden>(smem + nets.ap_bytes, kSurrogateSkyIn, T, fx, t) && tc_ok;
     if (kind == kSkyMlp)
       for (int k = 0; k < 8; ++k) yv[k] = t[k];
   }
+  // tensor memory is freed once no MMA is in flight (after a timed-out
+  // wait: one more bounded wait for the last commit of the tile)
+  tc::fence_before_sync();
+  if (__syncthreads_or(!tc_ok)) tc::mbar_wait(T.mbar, T.phase ^ 1u, kTcWaitTries);
+  __syncthreads();
+  tc::fence_after_sync();
+  if (threadIdx.x < 32) tc::dealloc(s_tmem, kSurrogateTmemCols);
 
   bool queued = false;
   uint32_t qkind = kQueueSurface;
@@ -337,6 +324,7 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
       Q.items[base + __popc(qm & ((1u << lane) - 1u))] = (qkind << 30) | uint32_t(cy * L.width + cx);
   }
   if (Q.stats != nullptr) {
+    if (!tc_ok && threadIdx.x == 0) atomicAdd(Q.stats + 7, 1.0f);  // tensor-core timeouts
     const unsigned gs = __ballot_sync(kAll, kind == kSurfPlain), ms = __ballot_sync(kAll, kind == kSurfMlp);
     const unsigned mk_ = __ballot_sync(kAll, kind == kSkyMlp), ls = __ballot_sync(kAll, kind == kSkyLut);
     if (lane == 0) {
@@ -424,9 +412,7 @@ cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind
   return cudaGetLastError();
 }
 
-size_t surrogate_smem_bytes(const SurrogateNets& nets) {
-  return size_t(nets.ap_bytes) + size_t(nets.sky_bytes) + 8 * sizeof(WarpSlot);
-}
+size_t surrogate_smem_bytes(const SurrogateNets& nets) { return size_t(nets.ap_bytes) + size_t(nets.sky_bytes); }
 
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,

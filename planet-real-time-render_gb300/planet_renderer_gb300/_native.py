@@ -154,6 +154,7 @@ class AtmSurrogate(ctypes.Structure):
     _fields_ = [
         ("aerial", ctypes.c_void_p),
         ("sky", ctypes.c_void_p),
+        ("aerial_above_shell", ctypes.c_void_p),
         ("scale_height_range", ctypes.c_double * 4),
         ("trained_planet_radius_m", ctypes.c_double),
         ("trained_top_altitude_m", ctypes.c_double),

@@ -139,9 +139,9 @@ class Mlp:
         x = self._check_io(inputs, self.n_in, "inputs")
         if out is None:
             out = torch.empty((x.shape[0], self.n_out), dtype=torch.float32, device=self.device)
-        if precision == "bf16":
+        if precision in ("bf16", "bf16_tc"):
             self.pack()
-        code = {"f32": 0, "bf16": 1}[precision]
+        code = {"f32": 0, "bf16": 1, "bf16_tc": 2}[precision]
         _native.check(self._lib.atm_mlp_forward(self._handle, self._p(x), self._p(out), x.shape[0], code, self._s()))
         return out
 

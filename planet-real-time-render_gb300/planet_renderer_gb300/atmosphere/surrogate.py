@@ -77,6 +77,12 @@ class TargetSpec:
 # 2-3x (held-out averages over the uniform box hide this), and a quarter of
 # the samples at the shell top serves the cameras above the shell.
 DEFAULT_SPECS = {SKY: TargetSpec(1.0e-4), AERIAL: TargetSpec(1.0e-4, 0.0, 0.02, 0.1, 0.25, 0.6)}
+# The pair of aerial networks used by train_surrogate: one for cameras inside
+# the shell (its segments start anywhere below the top) and one for cameras
+# above it (every segment starts at the shell top); the composite picks per
+# frame.  The radiance floor must be the same for both.
+AERIAL_INSIDE_SPEC = TargetSpec(1.0e-4, 0.0, 0.02, 0.1, 0.0, 0.6)
+AERIAL_ABOVE_SPEC = TargetSpec(1.0e-4, 0.0, 0.0, 1.0, 1.0, 0.6)
 
 
 def loss_weights(kind: int, y: torch.Tensor, spec: TargetSpec):
@@ -258,10 +264,12 @@ def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 
     folded = _fold_standardisation(net.params(), layer_shapes(n_in, n_hidden, n_out), mean, std)
     net.set_params(folded)
     net.pack()
-    xh, yh = source.samples(kind, held_out, seed + 7919)
+    # held-out: the input box (segments starting at the shell top where the
+    # network serves only those), and segments ending at a surface
+    xh, yh = source.samples(kind, held_out, seed + 7919, 1.0 if spec.shell_top_fraction >= 1.0 else 0.0)
     report.held_out = {"bf16": held_out_error(net, kind, xh, yh, spec, "bf16"),
                        "f32": held_out_error(net, kind, xh, yh, spec, "f32")}
-    if kind == AERIAL and spec.surface_fraction > 0.0:  # segments ending at a surface
+    if kind == AERIAL and spec.surface_fraction > 0.0:  # segments ending at a surface, as the frame's
         xs, ys = source.samples(kind, held_out, seed + 7921, spec.shell_top_fraction, 1.0)
         report.held_out["bf16_surface"] = held_out_error(net, kind, xs, ys, spec, "bf16")
     report.spec = spec
@@ -269,18 +277,22 @@ def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 
 
 
 class Surrogate:
-    """The two networks plus what atm_composite_surrogate needs to use them."""
+    """The networks plus what atm_composite_surrogate needs to use them:
+    ``aerial`` (or, for frames whose camera is above the shell,
+    ``aerial_above_shell`` when given) for surface pixels, ``sky`` for sky
+    pixels; any may be None (plain path)."""
 
     def __init__(self, aerial: Mlp | None, sky: Mlp | None, planet_radius_m: float = EARTH_RADIUS_M,
                  top_altitude_m: float = 100_000.0, scale_height_range=SCALE_HEIGHT_RANGE,
-                 aerial_spec: TargetSpec | None = None, sky_spec: TargetSpec | None = None):
-        self.aerial, self.sky = aerial, sky
+                 aerial_spec: TargetSpec | None = None, sky_spec: TargetSpec | None = None,
+                 aerial_above_shell: Mlp | None = None):
+        self.aerial, self.sky, self.aerial_above_shell = aerial, sky, aerial_above_shell
         self.planet_radius_m = float(planet_radius_m)
         self.top_altitude_m = float(top_altitude_m)
         self.scale_height_range = tuple(float(v) for v in scale_height_range)
         self.aerial_spec = aerial_spec or DEFAULT_SPECS[AERIAL]
         self.sky_spec = sky_spec or DEFAULT_SPECS[SKY]
-        for net in (aerial, sky):
+        for net in (aerial, sky, aerial_above_shell):
             if net is not None:
                 net.pack()
 
@@ -297,6 +309,7 @@ class Surrogate:
         s = _native.AtmSurrogate()
         s.aerial = self.aerial.handle.value if self.aerial is not None else None
         s.sky = self.sky.handle.value if self.sky is not None else None
+        s.aerial_above_shell = self.aerial_above_shell.handle.value if self.aerial_above_shell is not None else None
         s.scale_height_range[:] = list(self.scale_height_range)
         s.trained_planet_radius_m = self.planet_radius_m
         s.trained_top_altitude_m = self.top_altitude_m
@@ -314,7 +327,7 @@ class Surrogate:
     def save(self, directory) -> None:
         d = Path(directory)
         d.mkdir(parents=True, exist_ok=True)
-        for name, net in (("aerial", self.aerial), ("sky", self.sky)):
+        for name, net in (("aerial", self.aerial), ("sky", self.sky), ("aerial_above_shell", self.aerial_above_shell)):
             if net is not None:
                 net.save(d / f"{name}.npz")
         np.savez(d / "meta.npz", planet_radius_m=self.planet_radius_m, top_altitude_m=self.top_altitude_m,
@@ -327,31 +340,39 @@ class Surrogate:
         d = Path(directory)
         meta = np.load(d / "meta.npz")
         nets = {name: (Mlp.load(d / f"{name}.npz", device=device) if (d / f"{name}.npz").exists() else None)
-                for name in ("aerial", "sky")}
+                for name in ("aerial", "sky", "aerial_above_shell")}
         spec = lambda a: TargetSpec(float(a[0]), float(a[1]))
         return cls(nets["aerial"], nets["sky"], float(meta["planet_radius_m"]), float(meta["top_altitude_m"]),
                    tuple(float(v) for v in meta["scale_height_range"]), spec(meta["aerial_spec"]),
-                   spec(meta["sky_spec"]))
+                   spec(meta["sky_spec"]), nets["aerial_above_shell"])
 
 
-def train_surrogate(configs=None, n_samples: int = 2**22, batch: int = 65536, epochs: int = 200, seed: int = 1,
-                    device=None, log_every: int = 100, specs=None):
-    """Both networks on the default grid; returns (Surrogate, {kind: report})."""
+def train_surrogate(configs=None, n_samples: int = 2**22, batch: int = 16384, epochs: int = 400, seed: int = 1,
+                    lr: float = 4e-3, device=None, log_every: int = 100, above_shell: bool = True):
+    """The networks on the default grid: the aerial pair (inside / above the
+    shell; one aerial network for both when ``above_shell`` is False) and the
+    sky network.  Returns (Surrogate, {name: report})."""
 
-    specs = {**DEFAULT_SPECS, **(specs or {})}
     source = SampleSource(configs or parameter_grid(), device=device)
+    reports = {}
     try:
-        aerial, ra = train(source, AERIAL, n_samples, batch, epochs, seed=seed, spec=specs[AERIAL],
-                           log_every=log_every)
-        sky, rs = train(source, SKY, n_samples, batch, epochs, seed=seed + 1, spec=specs[SKY], log_every=log_every)
+        inside_spec = AERIAL_INSIDE_SPEC if above_shell else DEFAULT_SPECS[AERIAL]
+        aerial, reports["aerial"] = train(source, AERIAL, n_samples, batch, epochs, lr=lr, seed=seed,
+                                          spec=inside_spec, log_every=log_every)
+        above = None
+        if above_shell:
+            above, reports["aerial_above_shell"] = train(source, AERIAL, n_samples, batch, epochs, lr=lr,
+                                                         seed=seed + 2, spec=AERIAL_ABOVE_SPEC, log_every=log_every)
+        sky, reports["sky"] = train(source, SKY, n_samples, batch, epochs, lr=lr, seed=seed + 1,
+                                    spec=DEFAULT_SPECS[SKY], log_every=log_every)
     finally:
         source.close()
     return Surrogate(aerial, sky, source.planet_radius_m, source.top_altitude_m, source.scale_height_range,
-                     specs[AERIAL], specs[SKY]), {AERIAL: ra, SKY: rs}
+                     inside_spec, DEFAULT_SPECS[SKY], above), reports
 
 
 def stats_summary(stats: torch.Tensor) -> dict:
     s = [float(v) for v in stats.cpu()]
     n = max(s[0], 1.0)
     return {"checked": int(s[0]), "check_rel_mean": s[1] / n, "check_rel_max": s[2], "gated_surface": int(s[3]),
-            "mlp_surface": int(s[4]), "mlp_sky": int(s[5]), "lut_sky": int(s[6])}
+            "mlp_surface": int(s[4]), "mlp_sky": int(s[5]), "lut_sky": int(s[6]), "tensor_core_timeouts": int(s[7])}

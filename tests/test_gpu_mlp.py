@@ -83,3 +83,26 @@ def test_training_reduces_loss_and_checkpoint_round_trip(tmp_path):
     assert torch.equal(again.forward(x[:100]), net.forward(x[:100]))
     net.close()
     again.close()
+
+
+@pytest.mark.parametrize("shape", [(7, 4, 6), (6, 3, 3)])
+def test_forward_tcgen05_matches_mma_sync(shape):
+    """The tcgen05 forward (accumulators in tensor memory) against the
+    mma.sync forward of the same BF16 weights and the FP64 network."""
+
+    import torch
+
+    from oracle import mlp_fp64
+    from planet_renderer_gb300.atmosphere.mlp import layer_shapes
+
+    net = _net(*shape, seed=3)
+    rng = np.random.default_rng(11)
+    x = rng.uniform(-1.0, 1.0, (1000, shape[0])).astype(np.float32)  # ragged last tile of 128
+    xt = torch.as_tensor(x, device="cuda")
+    mma = net.forward(xt, "bf16").cpu().numpy()
+    tc = net.forward(xt, "bf16_tc").cpu().numpy()
+    ref = mlp_fp64.forward(net.params().cpu().numpy(), layer_shapes(*shape), x)
+    scale = np.sqrt(np.mean(ref ** 2))
+    assert np.sqrt(np.mean((tc - mma) ** 2)) <= 2e-3 * scale, np.sqrt(np.mean((tc - mma) ** 2)) / scale
+    assert np.sqrt(np.mean((tc - ref) ** 2)) <= 2e-2 * scale
+    net.close()
