@@ -13,13 +13,16 @@ __device__ __forceinline__ size_t pix_offset(const ImageLayout& L, int x, int y)
   return size_t(int64_t(x) * L.sx + int64_t(y) * L.sy);
 }
 
-// Pixel of thread: blocks of 16x16 pixels, each warp an 8x4 sub-tile.
-__device__ __forceinline__ bool tile_pixel(const ImageLayout& L, int& x, int& y) {
+// Pixel of thread in the 16x16 pixel block (bx, by): each warp an 8x4 sub-tile.
+__device__ __forceinline__ bool tile_pixel_at(const ImageLayout& L, int bx, int by, int& x, int& y) {
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;  // 0..7
-  x = blockIdx.x * 16 + (w & 1) * 8 + (lane & 7);
-  y = blockIdx.y * 16 + (w >> 1) * 4 + (lane >> 3);
+  x = bx * 16 + (w & 1) * 8 + (lane & 7);
+  y = by * 16 + (w >> 1) * 4 + (lane >> 3);
   return x < L.width && y < L.height;
+}
+__device__ __forceinline__ bool tile_pixel(const ImageLayout& L, int& x, int& y) {
+  return tile_pixel_at(L, blockIdx.x, blockIdx.y, x, y);
 }
 
 // Pixel of a thread for memory-bound per-pixel kernels: consecutive threads
