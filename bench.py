@@ -710,7 +710,7 @@ def _frame_4k(device, args) -> dict:
         "training": {"seconds": train_s, "samples_per_network": 2**22, "batch": 16384, "epochs": args.mlp_epochs,
                      "steps_per_network": reports["sky"].steps,
                      "held_out": {name: rep.held_out for name, rep in reports.items()}},
-        "networks": "aerial 7->4x64->6 (one for cameras inside the shell, one above it), sky 6->3x64->3; SiLU; "
+        "networks": "aerial 11->4x64->6 (one for cameras inside the shell, one above it), sky 10->3x64->3; SiLU; "
                     "BF16 mma.sync m16n8k16 with FP32 accumulation",
     })
     del graphs, r, frames

@@ -255,7 +255,8 @@ int atm_batch_static_lut(const AtmBatch* batch, int32_t param_set, int32_t kind,
 
 /* ---- MLP surrogates --------------------------------------------------------
  * No counterpart in the reference (its atmosphere has no learned part): small
- * networks n_in -> [64 SiLU] x n_hidden -> n_out standing in for the sky-view
+ * networks n_in -> [64 SiLU] x n_hidden -> n_out (n_in <= 16, n_out <= 8, 1-4
+ * hidden layers) standing in for the sky-view
  * and aerial-perspective integrals.  Parameters live on the device as one
  * float array (per layer W (out x in, row-major) then b).  Training: fused
  * FP32 forward + backward of the mean squared error over the batch, Adam. */
@@ -301,6 +302,13 @@ int atm_mlp_forward(const AtmMlp* mlp, const float* inputs, float* outputs, int6
  *         2 (ln H - ln H_min) / (ln H_max - ln H_min) - 1
  *   6     aerial only: segment length, 2 ln(clamp(len, 1 m, 2000 km)) /
  *         ln(2000 km) - 1
+ *   7, 8  aerial only: sun cosine (as 2) and altitude (as 0, clamped to
+ *         [0, top]) at the segment's end
+ *   9, 10 aerial only: the same at the segment's middle
+ *   6, 7  sky only: sun cosine and altitude (as 7, 8) where the sky-view march
+ *         ends (the shell top or the ground)
+ *   8, 9  sky only: the same at the march's lowest point (the closest
+ *         approach to the planet's centre, clamped to the march)
  * Targets: sky (ATM_SURROGATE_SKY) ln(L / E + 1e-7) per channel of the sky
  * radiance along the ray (the sky-view march, :1208-1302, from the ray's
  * altitude); aerial (ATM_SURROGATE_AERIAL) the same for the in-scattering of
@@ -314,7 +322,7 @@ int atm_mlp_forward(const AtmMlp* mlp, const float* inputs, float* outputs, int6
  * share the planet radius and the shell top).  Features are uniform over the
  * box above, drawn per sample index from `seed` (sample i does not depend on
  * n), the parameter set uniform among the batch's.  scale_height_range:
- * H_R min, max, H_M min, max in metres.  features: n x 6 (sky) or n x 7
+ * H_R min, max, H_M min, max in metres.  features: n x 10 (sky) or n x 11
  * (aerial) floats, targets n x 3 or n x 6, device.  options (aerial kind,
  * may be null for uniform sampling) concentrate samples where surface pixels
  * need them. */
@@ -331,10 +339,10 @@ int atm_surrogate_samples(AtmBatch* batch, int32_t kind, int64_t n, uint64_t see
 
 /* Networks and error check of atm_composite_surrogate. */
 typedef struct AtmSurrogate {
-  const AtmMlp* aerial;  /* 7 -> 4 x 64 -> 6, packed (atm_mlp_pack_bf16), or null:
+  const AtmMlp* aerial;  /* 11 -> 4 x 64 -> 6, packed (atm_mlp_pack_bf16), or null:
                             plain integrator for every surface pixel            */
-  const AtmMlp* sky;     /* 6 -> 3 x 64 -> 3, packed, or null: sky-view LUT    */
-  const AtmMlp* aerial_above_shell; /* 7 -> 4 x 64 -> 6 used instead of aerial
+  const AtmMlp* sky;     /* 10 -> 3 x 64 -> 3, packed, or null: sky-view LUT    */
+  const AtmMlp* aerial_above_shell; /* 11 -> 4 x 64 -> 6 used instead of aerial
                             when the camera is above the shell (every segment
                             then starts at the shell top), or null            */
   double scale_height_range[4];   /* of features 4, 5 (as in training)          */

@@ -731,7 +731,7 @@ ATM_API int atm_mlp_destroy(AtmMlp* m) {
 ATM_API int atm_mlp_create(int32_t n_in, int32_t n_hidden_layers, int32_t n_out, uint64_t seed, AtmMlp** out) {
   if (!out) return fail(ATM_E_INVALID, "null output");
   *out = nullptr;
-  if (n_in < 1 || n_in > 8 || n_out < 1 || n_out > 8 || n_hidden_layers < 1 || n_hidden_layers > 4)
+  if (n_in < 1 || n_in > 16 || n_out < 1 || n_out > 8 || n_hidden_layers < 1 || n_hidden_layers > 4)
     return fail(ATM_E_INVALID, "MLP shape must have 1..8 inputs, 1..8 outputs and 1..4 hidden layers of 64");
   AtmMlp* m = new (std::nothrow) AtmMlp();
   if (!m) return fail(ATM_E_NOMEM, "host allocation failed");
@@ -991,14 +991,14 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
   const AtmMlp* aerial = above && sg->aerial_above_shell ? sg->aerial_above_shell : sg->aerial;
   if (aerial) {
     if (!mlp_is(aerial, atm::kSurrogateApIn, atm::kSurrogateApHidden, atm::kSurrogateApOut))
-      return fail(ATM_E_INVALID, "aerial network must be 7 -> 4 x 64 -> 6");
+      return fail(ATM_E_INVALID, "aerial network must be 11 -> 4 x 64 -> 6");
     if (!aerial->packed_current) return fail(ATM_E_STATE, "aerial network not packed (atm_mlp_pack_bf16)");
     nets.ap = static_cast<const unsigned char*>(aerial->packed_tc);
     nets.ap_bytes = int(atm::mlp_tc_bytes(aerial->shape));
   }
   if (sg->sky) {
     if (!mlp_is(sg->sky, atm::kSurrogateSkyIn, atm::kSurrogateSkyHidden, atm::kSurrogateSkyOut))
-      return fail(ATM_E_INVALID, "sky network must be 6 -> 3 x 64 -> 3");
+      return fail(ATM_E_INVALID, "sky network must be 10 -> 3 x 64 -> 3");
     if (!sg->sky->packed_current) return fail(ATM_E_STATE, "sky network not packed (atm_mlp_pack_bf16)");
     nets.sky = static_cast<const unsigned char*>(sg->sky->packed_tc);
     nets.sky_bytes = int(atm::mlp_tc_bytes(sg->sky->shape));

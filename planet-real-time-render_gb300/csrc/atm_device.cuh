@@ -225,6 +225,13 @@ __device__ __forceinline__ void aerial_prefix(const DevParams& P, float h, float
 }
 
 // ---- per-ray geometry ---------------------------------------------------------
+// a + b = s + err exactly (Knuth's two-sum; no contraction applies to it).
+__device__ __forceinline__ float two_sum(float a, float b, float& err) {
+  const float s = a + b;
+  const float bb = s - a;
+  err = (a - (s - bb)) + (b - bb);
+  return s;
+}
 // r(t)^2 - R^2 along a camera ray, t the distance from the camera at
 // (0, R + h0, 0), is the quadratic q(u) = (q0 + q1 u) + u^2, u = t - t0.
 // Cameras within half a planet radius of the ground use the reference's own
@@ -235,8 +242,12 @@ __device__ __forceinline__ void aerial_prefix(const DevParams& P, float h, float
 // 1800 km: 10 m altitude errors against a 300 m Mie scale height, the
 // reference's own float result then off by tens of percent).  Such rays
 // pivot at the closest approach t_c = -(R + h0) cos v, where q0 = r_c^2 - R^2
-// and the shell discriminants are formed in FP64 from the ray's sine, once
-// per ray.
+// and the shell discriminants are differences of squares formed once per ray
+// from the ray's sine in compensated float (r_c = (R + h0) sin v as an
+// unevaluated sum hi + lo: Knuth's two-sum and the FMA two-product), which
+// keeps r_c^2 - R^2 and (R + top)^2 - r_c^2 to a few float ulps of themselves
+// at every grazing angle without FP64 (a small fraction of the FP32 rate on
+// this part).
 struct RayGeom {
   float h0, cosv;    // camera altitude, view cosine
   float t0, q0, q1;  // pivot and coefficients of q
@@ -263,14 +274,20 @@ __device__ __forceinline__ RayGeom ray_geom(const DevParams& P, float bottom, fl
     G.tc = -orad * cosv;
     G.disc_top = G.disc_ground = 0.0f;
   } else {
-    const double b = bottom, o = double(bottom) + double(a), top = P.top;
-    const double rc = o * double(sinv);
-    const double K = (rc - b) * (rc + b);
-    G.t0 = G.tc = float(-o * double(cosv));
-    G.q0 = float(K);
+    float o_lo, bt_lo;
+    const float o = two_sum(bottom, a, o_lo);         // R + h0 = o + o_lo
+    const float rc = o * sinv;                         // r_c = rc + rc_lo
+    const float rc_lo = fmaf(o, sinv, -rc) + o_lo * sinv;
+    const float bt = two_sum(bottom, P.top, bt_lo);    // R + top = bt + bt_lo
+    // R - r_c and (R + top) - r_c: the leading differences are exact where
+    // they cancel (Sterbenz), the low parts then carry the digits
+    const float dg = (bottom - rc) - rc_lo;
+    const float dt = ((bt - rc) + bt_lo) - rc_lo;
+    G.disc_ground = dg * (bottom + rc);
+    G.disc_top = dt * (bt + rc);
+    G.t0 = G.tc = -fmaf(o, cosv, o_lo * cosv);
+    G.q0 = -G.disc_ground;
     G.q1 = 0.0f;
-    G.disc_top = float(top * (2.0 * b + top) - K);
-    G.disc_ground = float(-K);
   }
   return G;
 }
@@ -627,11 +644,15 @@ __device__ __forceinline__ RaySource make_ray_source(const DevParams& P, const F
   R.q1 = G.q1;
   R.r_sun = dot(ray, F.sun);
   const float o_y = F.bottom + mx(G.h0, 0.0f);
-  if (G.far)
-    R.s0 = float(double(o_y) * double(F.sun.y) + double(G.t0) * (double(ray.x) * F.sun.x + double(ray.y) * F.sun.y +
-                                                                  double(ray.z) * F.sun.z));
-  else
+  if (G.far) {
+    // p(t0) . sun with the closest-approach point formed first (one rounding
+    // per component, each ~r_c): o_y sun.y + t0 ray . sun cancels ~r_cam
+    // down to ~r_c
+    const f3 c = mk(G.t0 * ray.x, fmaf(G.t0, ray.y, o_y), G.t0 * ray.z);
+    R.s0 = dot(c, F.sun);
+  } else {
     R.s0 = o_y * F.sun.y;
+  }
   const float cr = clampf(R.r_sun, -1.0f, 1.0f);
   R.ER = F.E * arr3(P.beta_r) * rayleigh_phase(P, cr);
   R.EM = F.E * arr3(P.beta_ms) * mie_phase(P, cr);

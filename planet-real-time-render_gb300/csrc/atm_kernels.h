@@ -93,8 +93,8 @@ cudaError_t launch_mlp_forward_bf16(const MlpShape& m, const void* packed, const
 constexpr float kSurrogateFloor = 1.0e-7f;
 constexpr float kSurrogateMaxLength = 2.0e6f;
 constexpr float kSurrogateMaxDepth = 30.0f;
-constexpr int kSurrogateApIn = 7, kSurrogateApOut = 6, kSurrogateApHidden = 4;
-constexpr int kSurrogateSkyIn = 6, kSurrogateSkyOut = 3, kSurrogateSkyHidden = 3;
+constexpr int kSurrogateApIn = 11, kSurrogateApOut = 6, kSurrogateApHidden = 4;
+constexpr int kSurrogateSkyIn = 10, kSurrogateSkyOut = 3, kSurrogateSkyHidden = 3;
 struct SurrogateSetDev {
   DevParams P;
   const float4* tlut;
@@ -103,8 +103,8 @@ struct SurrogateSetDev {
   float lhr_n, lhm_n;  // normalised log scale heights (features 4, 5)
 };
 struct SurrogateNets {
-  const unsigned char* ap;   // packed BF16 aerial network (7 -> 4x64 -> 6) or null
-  const unsigned char* sky;  // packed BF16 sky network (6 -> 3x64 -> 3) or null
+  const unsigned char* ap;   // packed BF16 aerial network (11 -> 4x64 -> 6) or null
+  const unsigned char* sky;  // packed BF16 sky network (10 -> 3x64 -> 3) or null
   int ap_bytes, sky_bytes;   // multiples of 16
   float lhr_n, lhm_n;        // the frame's normalised log scale heights
   float floor, floor_t;      // aerial output: ln(L / E + floor + floor_t T)

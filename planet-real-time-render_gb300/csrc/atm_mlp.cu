@@ -2,7 +2,7 @@
 // on CUDA cores, Adam, an FP32 reference forward and a BF16 tensor-core
 // forward (mma.sync m16n8k16, FP32 accumulate).
 //
-// Network: n_in -> [64 SiLU] x n_hidden -> n_out (n_in, n_out <= 8,
+// Network: n_in -> [64 SiLU] x n_hidden -> n_out (n_in <= 16, n_out <= 8,
 // n_hidden 1..4).  Parameters are one float array: for each layer l, W_l
 // (out x in, row-major) then b_l.  The training objective is the mean
 // squared error over all outputs of the batch.
@@ -337,7 +337,7 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(MlpShape m, const unsign
   bool ok = true;
   for (long long base = blockIdx.x * 128LL; base < n; base += gridDim.x * 128LL) {
     const long long r = base + threadIdx.x;
-    float x[8] = {0, 0, 0, 0, 0, 0, 0, 0}, y[8];
+    float x[16] = {}, y[8];
     if (r < n)
       for (int k = 0; k < m.n_in; ++k) x[k] = inputs[r * m.n_in + k];
     ok = mlp_tile_tc<kHidden>(smw, m.n_in, T, x, y) && ok;

@@ -44,21 +44,22 @@ struct TcTile {
   int row;           // this thread's row 0..127
 };
 
-// Runs the network (n_in <= 8 inputs, kHidden layers of 64, n_out <= 8) for
+// Runs the network (n_in <= 16 inputs, kHidden layers of 64, n_out <= 8) for
 // the tile's 128 rows; every thread of the tile calls with its row's inputs
-// and receives its row's outputs.  w: generic pointer to the packed network
+// (unused ones zero) and receives its row's outputs.  w: generic pointer to the packed network
 // in shared memory.  Returns false if an MMA did not complete in time (the
 // outputs are then not valid).
 template <int kHidden>
-__device__ __forceinline__ bool mlp_tile_tc(const unsigned char* w, int n_in, TcTile& T, const float (&x)[8],
+__device__ __forceinline__ bool mlp_tile_tc(const unsigned char* w, int n_in, TcTile& T, const float (&x)[16],
                                             float (&y)[8]) {
   const uint32_t lane_off = uint32_t(T.row & ~31) << 16;  // the warp's quarter of the lanes
   const bool issuer = T.row == 0;
   bool ok = true;
-  // inputs -> A columns 0..7 (K = 16: 8 inputs, then zeros)
+  // inputs -> A columns 0..7 (K = 16, BF16 pairs)
   {
-    uint32_t v[8] = {pack_bf16(x[0], x[1]), pack_bf16(x[2], x[3]), pack_bf16(x[4], x[5]), pack_bf16(x[6], x[7]),
-                     0u, 0u, 0u, 0u};
+    uint32_t v[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = pack_bf16(x[2 * i], x[2 * i + 1]);
     tc::st8(T.tmem_a + lane_off, v);
     tc::wait_st();
   }

@@ -43,6 +43,42 @@ __device__ __forceinline__ void geometry_features(const DevParams& P, float bott
   x[3] = clampf(cos_dphi, -1.0f, 1.0f);
 }
 
+// Sun (multi-scattering u mapping) and altitude features, x[0] and x[1], of
+// the point at distance t along a ray leaving (0, o_y, 0) (G: its geometry).
+// Where a segment's light comes from depends on where it ends and how low it
+// dips as much as on where it starts: with these points given, the networks'
+// held-out errors drop by about a quarter (sky) to a third (camera-to-surface
+// segments).  Returns the point's sun cosine.
+__device__ __forceinline__ float point_features(const DevParams& P, float bottom, const RayGeom& G, f3 ray, float o_y,
+                                                f3 sun, float t, float* x) {
+  const f3 pt = mk(ray.x * t, o_y + ray.y * t, ray.z * t);
+  const float mu = clampf(dot(sun, pt) / mx(norm(pt), 1.0f), -1.0f, 1.0f);
+  const float h = altitude_at(G, t, bottom);
+  x[0] = 2.0f * sun_cosine_to_u(mu, horizon_cosine(h, bottom)) - 1.0f;
+  x[1] = 2.0f * sqrtf(clampf(h * P.inv_top, 0.0f, 1.0f)) - 1.0f;
+  return mu;
+}
+// Aerial x[7..10]: the segment's end, then its middle.  Returns the smaller
+// |sun cosine| of the two (the twilight gate).
+__device__ __forceinline__ float segment_features(const DevParams& P, float bottom, const RayGeom& G, f3 ray,
+                                                  float o_y, f3 sun, float start, float end, float* x) {
+  const float a = point_features(P, bottom, G, ray, o_y, sun, end, x + 7);
+  const float b = point_features(P, bottom, G, ray, o_y, sun, 0.5f * (start + end), x + 9);
+  return mn(fabsf(a), fabsf(b));
+}
+// Sky x[6..9]: the end of the ray's march (the shell top or the ground),
+// then its lowest point (the closest approach, clamped to the march).
+__device__ __forceinline__ void sky_ray_features(const DevParams& P, float bottom, float h, f3 ray, f3 sun, float* x) {
+  const RayGeom G = camera_ray_geom(P, bottom, h, ray);
+  float start, end;
+  bool valid, ground;
+  segment_of(P, G, bottom, start, end, valid, ground);
+  if (!valid) start = end = 0.0f;
+  const float o_y = bottom + mx(h, 0.0f);
+  point_features(P, bottom, G, ray, o_y, sun, end, x + 6);
+  point_features(P, bottom, G, ray, o_y, sun, clampf(G.tc, start, end), x + 8);
+}
+
 // Counter-based uniform in [0, 1): 64-bit mix of (seed, index, lane).
 __device__ __forceinline__ float uniform01(unsigned long long seed, unsigned long long i, unsigned k) {
   unsigned long long z = seed + 0x9E3779B97F4A7C15ull * (i * 16 + k + 1);
@@ -89,7 +125,7 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
     const SurrogateSetDev& S = sets[min(int(uniform01(seed, i, 0) * n_sets), n_sets - 1)];
     const DevParams& P = S.P;
     const float R = S.bottom;
-    float x[8];
+    float x[16];
     for (int k = 0; k < 4; ++k) x[k] = 2.0f * uniform01(seed, i, k + 1) - 1.0f;
     if (kind == 1 && uniform01(seed, i, 6) < shaping.top_fraction) x[0] = 1.0f;
     // invert the feature maps
@@ -107,10 +143,11 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
     x[5] = S.lhm_n;
     const Frame F = make_frame(P, S.tlut, S.mslut, R, ar, sun, E);
     const f3 inv_e = mk(1.0f / E.x, 1.0f / E.y, 1.0f / E.z);
-    if (kind == 0) {  // sky: 6 features -> log(L/E + floor)
+    if (kind == 0) {  // sky: 10 features -> log(L/E + floor)
       const f3 L = sky_radiance(P, F, h, ray) * inv_e;
       samples = uint32_t(P.sv_steps);
-      for (int k = 0; k < 6; ++k) features[i * 6 + k] = x[k];
+      sky_ray_features(P, R, h, ray, sun, x);
+      for (int k = 0; k < kSurrogateSkyIn; ++k) features[i * kSurrogateSkyIn + k] = x[k];
       targets[i * 3 + 0] = logf(L.x + kSurrogateFloor);
       targets[i * 3 + 1] = logf(L.y + kSurrogateFloor);
       targets[i * 3 + 2] = logf(L.z + kSurrogateFloor);
@@ -135,8 +172,11 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
       if (surface_interval(P, G, R, len, start, end)) {
         L = integrate_surface(P, F, G, ray, start, end, samples) * inv_e;
         T = surface_segment_t(P, F, G, ray, start, end);
+      } else {
+        start = end = 0.0f;
       }
-      for (int k = 0; k < 7; ++k) features[i * 7 + k] = x[k];
+      segment_features(P, R, G, ray, R + h, sun, start, end, x);
+      for (int k = 0; k < kSurrogateApIn; ++k) features[i * kSurrogateApIn + k] = x[k];
       targets[i * 6 + 0] = logf(L.x + kSurrogateFloor);
       targets[i * 6 + 1] = logf(L.y + kSurrogateFloor);
       targets[i * 6 + 2] = logf(L.z + kSurrogateFloor);
@@ -212,7 +252,7 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
       fabsf(acosf(clampf(ray.y, -1.0f, 1.0f)) - sky_horizon_zenith(A.cam_alt, A.bottom)) < nets.limb_rad;
 
   int kind = kNone;
-  float fx[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  float fx[16] = {};
   float start = 0.0f, end = 0.0f;
   if (inside) {
     if (sid[e] >= 0) {
@@ -231,18 +271,13 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
         const f3 tv = ray - up * mu_v, ts = F.sun - up * mu_s;
         const float nv = norm(tv), ns = norm(ts);
         const float cphi = (nv > 1e-6f && ns > 1e-6f) ? dot(tv, ts) / (nv * ns) : 1.0f;
-        // twilight gate: the sun cosine small at the start, middle or end
-        float mu_min = fabsf(mu_s);
-        for (int k = 1; k <= 2; ++k) {
-          const float t = start + (end - start) * 0.5f * float(k);
-          const f3 pt = mk(ray.x * t, o_y + ray.y * t, ray.z * t);
-          mu_min = mn(mu_min, fabsf(dot(F.sun, pt) / mx(norm(pt), 1.0f)));
-        }
-        kind = mu_min < nets.twilight_cos ? kSurfPlain : kSurfMlp;
         geometry_features(P, A.bottom, hs, mu_v, mu_s, cphi, fx);
         fx[4] = nets.lhr_n;
         fx[5] = nets.lhm_n;
         fx[6] = 2.0f * __logf(clampf(end - start, 1.0f, kSurrogateMaxLength)) / logf(kSurrogateMaxLength) - 1.0f;
+        // twilight gate: the sun cosine small at the start, middle or end
+        const float mu_min = mn(fabsf(mu_s), segment_features(P, A.bottom, G, ray, o_y, F.sun, start, end, fx));
+        kind = mu_min < nets.twilight_cos ? kSurfPlain : kSurfMlp;
       }
     } else if (nets.sky != nullptr && A.cam_alt <= P.top && fabsf(F.sun.y) >= nets.sky_twilight_cos && !near_limb) {
       kind = kSkyMlp;
@@ -251,6 +286,7 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
       geometry_features(P, A.bottom, A.cam_alt, ray.y, F.sun.y, cphi, fx);
       fx[4] = nets.lhr_n;
       fx[5] = nets.lhm_n;
+      sky_ray_features(P, A.bottom, A.cam_alt, ray, F.sun, fx);
     } else {
       kind = kSkyLut;
     }

@@ -10,8 +10,8 @@ standardisation is then folded into the output layer and the weights are
 packed for the BF16 tensor-core composite (``atm_composite_surrogate``).
 
 Networks (feature layout in ``include/atm_capi.h``):
-  * sky:    6 -> 3 x 64 SiLU -> 3   sky radiance, ln(L / E + floor)
-  * aerial: 7 -> 4 x 64 SiLU -> 6   segment in-scattering (``TargetSpec``),
+  * sky:    10 -> 3 x 64 SiLU -> 3  sky radiance, ln(L / E + floor)
+  * aerial: 11 -> 4 x 64 SiLU -> 6  segment in-scattering (``TargetSpec``),
                                      optical depth
 The surrogate composite takes the surface pixels' transmittance from the
 transmittance LUT, as the plain composite does; the aerial network's
@@ -39,7 +39,7 @@ SKY = _native.ATM_SURROGATE_SKY
 AERIAL = _native.ATM_SURROGATE_AERIAL
 # Rayleigh scale height min, max; Mie scale height min, max (m)
 SCALE_HEIGHT_RANGE = (6000.0, 10000.0, 800.0, 1600.0)
-SHAPES = {SKY: (6, 3, 3), AERIAL: (7, 4, 6)}  # n_in, hidden layers, n_out
+SHAPES = {SKY: (10, 3, 3), AERIAL: (11, 4, 6)}  # n_in, hidden layers, n_out
 FLOOR = 1.0e-7        # floor of the generator's targets ln(L / E + FLOOR)
 MAX_LENGTH_M = 2.0e6
 MAX_DEPTH = 30.0

@@ -15,8 +15,8 @@ def _net(n_in, n_hidden, n_out, seed=1):
     return Mlp(n_in, n_hidden, n_out, seed=seed)
 
 
-@pytest.mark.parametrize("shape,weighted", [((6, 3, 3), False), ((7, 4, 6), False), ((3, 1, 2), False),
-                                            ((7, 4, 6), True)])
+@pytest.mark.parametrize("shape,weighted", [((6, 3, 3), False), ((11, 4, 6), False), ((3, 1, 2), False),
+                                            ((11, 4, 6), True), ((16, 2, 8), False)])
 def test_gradient_matches_fp64_oracle(shape, weighted):
     import torch
 
@@ -49,13 +49,13 @@ def test_forward_fp32_and_bf16():
     from oracle import mlp_fp64
     from planet_renderer_gb300.atmosphere.mlp import layer_shapes
 
-    net = _net(7, 4, 6)
+    net = _net(11, 4, 6)
     rng = np.random.default_rng(9)
-    x = rng.uniform(-1.0, 1.0, (4099, 7)).astype(np.float32)
+    x = rng.uniform(-1.0, 1.0, (4099, 11)).astype(np.float32)
     xt = torch.as_tensor(x, device="cuda")
     f32 = net.forward(xt, "f32").cpu().numpy()
     bf16 = net.forward(xt, "bf16").cpu().numpy()
-    ref = mlp_fp64.forward(net.params().cpu().numpy(), layer_shapes(7, 4, 6), x)
+    ref = mlp_fp64.forward(net.params().cpu().numpy(), layer_shapes(11, 4, 6), x)
     scale = np.abs(ref).max()
     assert np.max(np.abs(f32 - ref)) <= 1e-5 * scale
     # bf16 operands (8-bit mantissa), fp32 accumulation
@@ -85,7 +85,7 @@ def test_training_reduces_loss_and_checkpoint_round_trip(tmp_path):
     again.close()
 
 
-@pytest.mark.parametrize("shape", [(7, 4, 6), (6, 3, 3)])
+@pytest.mark.parametrize("shape", [(11, 4, 6), (6, 3, 3), (16, 2, 8)])
 def test_forward_tcgen05_matches_mma_sync(shape):
     """The tcgen05 forward (accumulators in tensor memory) against the
     mma.sync forward of the same BF16 weights and the FP64 network."""

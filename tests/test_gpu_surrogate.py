@@ -113,6 +113,63 @@ def test_samples_match_the_oracle_integrator(source, kind):
         assert np.quantile(d[:, 3:][live], 0.99) < 5e-3
 
 
+def _point_features_match(x, fs, fh, top, R, ray, sun, h, t):
+    """Features fs (sun cosine, u mapping) and fh (altitude) of the point at
+    distance t along each ray against float64 geometry."""
+
+    p = np.stack([ray[:, 0] * t, R + h + ray[:, 1] * t, ray[:, 2] * t], 1)
+    r = np.linalg.norm(p, axis=1)
+    he = np.clip(r - R, 0.0, top)
+    mu = np.sum(p * sun, axis=1) / r
+    got_h = top * ((x[:, fh].astype(np.float64) + 1.0) * 0.5) ** 2
+    assert np.max(np.abs(got_h - he) / (3.0 + 1e-4 * he)) <= 1.0
+    hc = -np.sqrt(got_h * (2 * R + got_h)) / (R + got_h)
+    u = (x[:, fs].astype(np.float64) + 1.0) * 0.5
+    got_mu = np.where(u < 0.5, hc - (hc + 1) * (1 - 2 * u) ** 2, hc + (1 - hc) * (2 * u - 1) ** 2)
+    assert np.max(np.abs(got_mu - np.clip(mu, -1, 1))) <= 2e-4
+
+
+def test_aerial_segment_end_features(source):
+    """Aerial features 7-10: sun cosine and altitude at the segment's end (the
+    shell-clipped length) and middle, against the decoded geometry."""
+
+    from planet_renderer_gb300.atmosphere.surrogate import AERIAL
+
+    x, _ = source.samples(AERIAL, 4096, 13, 0.25, 0.5)
+    x = x.cpu().numpy()
+    assert x.shape[1] == 11
+    top, R = source.top_altitude_m, source.planet_radius_m
+    h, ray, sun, _, _, length = _decode(x, top, R, source.scale_height_range, AERIAL)
+    b = (R + h) * ray[:, 1]
+    t_top = -b + np.sqrt(np.maximum(b * b - ((R + h) ** 2 - (R + top) ** 2), 0.0))
+    end = np.minimum(length, t_top)
+    _point_features_match(x, 7, 8, top, R, ray, sun, h, end)
+    _point_features_match(x, 9, 10, top, R, ray, sun, h, 0.5 * end)
+
+
+def test_sky_ray_end_features(source):
+    """Sky features 6-9: sun cosine and altitude where the march ends (top or
+    ground) and at its lowest point."""
+
+    from planet_renderer_gb300.atmosphere.surrogate import SKY
+
+    x, _ = source.samples(SKY, 4096, 17)
+    x = x.cpu().numpy()
+    assert x.shape[1] == 10
+    top, R = source.top_altitude_m, source.planet_radius_m
+    h, ray, sun, _, _, _ = _decode(x, top, R, source.scale_height_range, SKY)
+    b = (R + h) * ray[:, 1]
+    t_top = -b + np.sqrt(np.maximum(b * b - ((R + h) ** 2 - (R + top) ** 2), 0.0))
+    dg = b * b - ((R + h) ** 2 - R ** 2)
+    t_g = -b - np.sqrt(np.maximum(dg, 0.0))
+    # rays decoded within ~1e-7 rad of the horizon may hit or miss the ground
+    grazing = np.abs(dg) < 1e-6 * (R + h) ** 2
+    x, h, ray, sun, b, t_top, dg, t_g = (v[~grazing] for v in (x, h, ray, sun, b, t_top, dg, t_g))
+    end = np.where((dg >= 0) & (ray[:, 1] < 0) & (t_g > 0), t_g, t_top)
+    _point_features_match(x, 6, 7, top, R, ray, sun, h, end)
+    _point_features_match(x, 8, 9, top, R, ray, sun, h, np.clip(-b, 0.0, end))
+
+
 def test_training_learns_both_networks(trained):
     """Held-out errors at the reduced test budget (the bench states those of
     the full budget); BF16 inference stays close to the FP32 network."""
