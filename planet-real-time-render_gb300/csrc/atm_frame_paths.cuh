@@ -112,57 +112,75 @@ __device__ __forceinline__ RayGeom camera_ray_geom(const DevParams& P, float bot
   return ray_geom(P, bottom, h0, ray.y, sqrtf(ray.x * ray.x + ray.z * ray.z));
 }
 
+// Per-ray state of the limb integrator (_integrate_surface_scattering
+// :1667-1755): shadow-cylinder roots, the ray's source terms and the
+// distribution of its base intervals over [start, end].
+struct SurfaceMarch {
+  RaySource rs;
+  RayWarp rw;
+  float sr0, sr1;
+  bool sv0, sv1;
+};
+__device__ __forceinline__ SurfaceMarch make_surface_march(const DevParams& P, const Frame& F, const RayGeom& G, f3 ray,
+                                                           float start, float end) {
+  SurfaceMarch M;
+  if (G.far)
+    shadow_roots_far(G.h0, ray, F.sun, F.bottom, M.sr0, M.sr1, M.sv0, M.sv1);
+  else
+    shadow_roots(mk(0.0f, F.bottom + G.h0, 0.0f), ray, F.sun, F.bottom, M.sr0, M.sr1, M.sv0, M.sv1);
+  M.rs = make_ray_source(P, F, G, ray);
+  M.rw = make_warp(G.tc, start, end);
+  return M;
+}
+// One base interval [d0, d1] with its terminator refinement (:901-1031).
+__device__ __forceinline__ Seg surface_interval_seg(const DevParams& P, const Frame& F, const SurfaceMarch& M, float d0,
+                                                    float d1, uint32_t& samples) {
+  float vis;
+  Seg coarse = source_segment<true>(P, F, M.rs, d0, d1, vis);
+  ++samples;
+  // _terminator_refinement_weight :901-966; zero unless a shadow-cylinder
+  // root exists or the disk is partly hidden at the midpoint
+  float w = 0.0f;
+  if ((M.sv0 || M.sv1) || (vis > 0.0f && vis < 1.0f)) {
+    float mid = (d0 + d1) * 0.5f;
+    float iw = mx(d1 - d0, 1.0e-4f);
+    float closest_root = 1.0e30f;
+    if (M.sv0) closest_root = mn(closest_root, fabsf(mid - M.sr0));
+    if (M.sv1) closest_root = mn(closest_root, fabsf(mid - M.sr1));
+    float prox = __saturatef(2.0f - fdiv(closest_root, iw));
+    prox = prox * prox * (3.0f - 2.0f * prox);
+    w = mx(prox, 4.0f * vis * (1.0f - vis));
+  }
+  Seg interval = coarse;
+  if (w > 0.0f) {
+    // _integrate_adaptive_scattering_interval :998-1031
+    const int nsub = P.substeps;
+    Seg fine = {splat(0.0f), splat(1.0f)};
+    float c0 = d0 + (d1 - d0) * 0.0f;
+    for (int k = 0; k < nsub; ++k) {
+      float c1 = d0 + (d1 - d0) * (float(k + 1) / float(nsub));
+      float cvis;
+      fine = seg_then(fine, source_segment<true>(P, F, M.rs, c0, c1, cvis));
+      c0 = c1;
+    }
+    samples += nsub;
+    interval.L = coarse.L * (1.0f - w) + fine.L * w;
+    interval.T = coarse.T * (1.0f - w) + fine.T * w;
+  }
+  return interval;
+}
+
 // _integrate_surface_scattering :1667-1755 (with :901-1032).  `start`/`end`
 // are the shell-clipped interval; the caller has checked it is non-empty.
 __device__ __forceinline__ f3 integrate_surface(const DevParams& P, const Frame& F, const RayGeom& G, f3 ray,
                                                 float start, float end, uint32_t& samples) {
-  float sr0, sr1;
-  bool sv0, sv1;
-  if (G.far)
-    shadow_roots_far(G.h0, ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
-  else
-    shadow_roots(mk(0.0f, F.bottom + G.h0, 0.0f), ray, F.sun, F.bottom, sr0, sr1, sv0, sv1);
-  const RaySource rs = make_ray_source(P, F, G, ray);
-  const RayWarp rw = make_warp(G.tc, start, end);
-  const bool roots = sv0 || sv1;
+  const SurfaceMarch M = make_surface_march(P, F, G, ray, start, end);
   const int n = P.limb_steps;
-  const int nsub = P.substeps;
   Seg acc = {splat(0.0f), splat(1.0f)};
-  float d0 = warp_at(rw, 0.0f);
+  float d0 = warp_at(M.rw, 0.0f);
   for (int i = 0; i < n; ++i) {
-    float d1 = warp_at(rw, float(i + 1) / float(n));
-    float vis;
-    Seg coarse = source_segment<true>(P, F, rs, d0, d1, vis);
-    ++samples;
-    // _terminator_refinement_weight :901-966; zero unless a shadow-cylinder
-    // root exists or the disk is partly hidden at the midpoint
-    float w = 0.0f;
-    if (roots || (vis > 0.0f && vis < 1.0f)) {
-      float mid = (d0 + d1) * 0.5f;
-      float iw = mx(d1 - d0, 1.0e-4f);
-      float closest_root = 1.0e30f;
-      if (sv0) closest_root = mn(closest_root, fabsf(mid - sr0));
-      if (sv1) closest_root = mn(closest_root, fabsf(mid - sr1));
-      float prox = __saturatef(2.0f - fdiv(closest_root, iw));
-      prox = prox * prox * (3.0f - 2.0f * prox);
-      w = mx(prox, 4.0f * vis * (1.0f - vis));
-    }
-    Seg interval = coarse;
-    if (w > 0.0f) {
-      // _integrate_adaptive_scattering_interval :998-1031
-      Seg fine = {splat(0.0f), splat(1.0f)};
-      float c0 = d0 + (d1 - d0) * 0.0f;
-      for (int k = 0; k < nsub; ++k) {
-        float c1 = d0 + (d1 - d0) * (float(k + 1) / float(nsub));
-        float cvis;
-        fine = seg_then(fine, source_segment<true>(P, F, rs, c0, c1, cvis));
-        c0 = c1;
-      }
-      samples += nsub;
-      interval.L = coarse.L * (1.0f - w) + fine.L * w;
-      interval.T = coarse.T * (1.0f - w) + fine.T * w;
-    }
-    acc = seg_then(acc, interval);
+    float d1 = warp_at(M.rw, float(i + 1) / float(n));
+    acc = seg_then(acc, surface_interval_seg(P, F, M, d0, d1, samples));
     d0 = d1;
   }
   return vmax(acc.L, 0.0f);

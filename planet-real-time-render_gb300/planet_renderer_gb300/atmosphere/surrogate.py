@@ -72,17 +72,21 @@ class TargetSpec:
     surface_fraction: float = 0.0
 
 
-# Aerial defaults from 4K frames against FP64 (three cameras, 2 km - 2000 km):
+# Aerial defaults from frames against FP64 (three cameras, 2 km - 2000 km):
 # the frame-sensitivity weights cut the 50 km and 2000 km cameras' errors
 # 2-3x (held-out averages over the uniform box hide this), and a quarter of
-# the samples at the shell top serves the cameras above the shell.
-DEFAULT_SPECS = {SKY: TargetSpec(1.0e-4), AERIAL: TargetSpec(1.0e-4, 0.0, 0.02, 0.1, 0.25, 0.6)}
+# the samples at the shell top serves the cameras above the shell.  The
+# surface behind the segment is taken dim (C = 0.005 E, a low sun's lit
+# ground): with C = 0.02 E the weights neglect the in-scattering of low-sun
+# frames, whose surfaces are far dimmer (50 km camera at sun zenith 83 deg:
+# 2.0% mean frame error against 1.7% with 0.005; unweighted, 2.3%).
+DEFAULT_SPECS = {SKY: TargetSpec(1.0e-4), AERIAL: TargetSpec(1.0e-4, 0.0, 0.005, 0.1, 0.25, 0.6)}
 # The pair of aerial networks used by train_surrogate: one for cameras inside
 # the shell (its segments start anywhere below the top) and one for cameras
 # above it (every segment starts at the shell top); the composite picks per
 # frame.  The radiance floor must be the same for both.
-AERIAL_INSIDE_SPEC = TargetSpec(1.0e-4, 0.0, 0.02, 0.1, 0.0, 0.6)
-AERIAL_ABOVE_SPEC = TargetSpec(1.0e-4, 0.0, 0.0, 1.0, 1.0, 0.6)
+AERIAL_INSIDE_SPEC = TargetSpec(1.0e-4, 0.0, 0.005, 0.1, 0.0, 0.6)
+AERIAL_ABOVE_SPEC = TargetSpec(1.0e-4, 0.0, 0.002, 0.1, 1.0, 0.6)
 
 
 def loss_weights(kind: int, y: torch.Tensor, spec: TargetSpec):
