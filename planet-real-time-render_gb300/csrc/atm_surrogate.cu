@@ -46,9 +46,9 @@ __device__ __forceinline__ void geometry_features(const DevParams& P, float bott
 // Sun (multi-scattering u mapping) and altitude features, x[0] and x[1], of
 // the point at distance t along a ray leaving (0, o_y, 0) (G: its geometry).
 // Where a segment's light comes from depends on where it ends and how low it
-// dips as much as on where it starts: with these points given, the networks'
-// held-out errors drop by about a quarter (sky) to a third (camera-to-surface
-// segments).  Returns the point's sun cosine.
+// dips as much as on where it starts: with these points given, the sky
+// network's held-out error drops by a quarter and the aerial network's on
+// camera-to-surface segments to a third.  Returns the point's sun cosine.
 __device__ __forceinline__ float point_features(const DevParams& P, float bottom, const RayGeom& G, f3 ray, float o_y,
                                                 f3 sun, float t, float* x) {
   const f3 pt = mk(ray.x * t, o_y + ray.y * t, ray.z * t);
