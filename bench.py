@@ -411,6 +411,7 @@ def main() -> None:
     parser.add_argument("--no-batch", action="store_true")
     parser.add_argument("--no-mlp", action="store_true", help="skip the surrogate frame (training + timing)")
     parser.add_argument("--mlp-epochs", type=int, default=400, help="surrogate training epochs (2^22 samples)")
+    parser.add_argument("--no-post", action="store_true", help="skip the 4K display post-process timing")
     args = parser.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -477,6 +478,7 @@ def main() -> None:
     if not args.no_4k:
         frame_4k = _frame_4k(device, args)
     batch = None if args.no_batch else _batch(device, args)
+    post = None if args.no_post else _postprocess_4k(device, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -499,6 +501,7 @@ def main() -> None:
             "frame_ms_1080p": ms_per_step / 3.0,
             "frame_ms_4k": frame_4k,
             "batch": batch,
+            "postprocess_4k": post,
             "samples_per_step": samples_per_step,
             "e2e": {"value": world * e2e_samples / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / e2e_steps,
@@ -529,6 +532,52 @@ def _composite_args(v, light):
 
     return (EARTH_RADIUS_M, v.camera_radius_m, v.sun_local, SOLAR_IRRADIANCE, light.sun_disk_radiance,
             SUN_ANGULAR_RADIUS_DEG, v.basis, v.tangent_half_fov, 4.0, 12.0)
+
+
+POST_BYTES_PER_PIXEL = 36  # float3 HDR read by the extract and by the resolve, float3 display written
+
+
+def _postprocess_4k(device, args) -> dict:
+    """The display post-process that follows the atmosphere stage
+    (PostProcessor, reference postprocess.py) on 3840x2160 HDR frames with
+    the default configuration (4 bloom passes) and tone mapping: device time
+    per frame with CUDA events, two HDR frames alternated."""
+
+    import torch
+
+    from planet_renderer_gb300.postprocess import PostprocessConfig, PostProcessor
+
+    width, height = 3840, 2160
+    g = torch.Generator(device=device).manual_seed(SEED)
+    hdrs = [torch.exp(torch.randn((width, height, 3), device=device, generator=g) * 1.5 - 1.0) for _ in range(2)]
+    display = torch.empty_like(hdrs[0])
+    config = PostprocessConfig()
+    pp = PostProcessor(width, height, config, device=device)
+    for i in range(args.warmup):
+        pp.process(hdrs[i % 2], display, 0.0, bloom=True, tone_map=True)
+    steps = max(args.steps // 4, 10)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    start.record()
+    for i in range(steps):
+        pp.process(hdrs[i % 2], display, 0.0, bloom=True, tone_map=True)
+    end.record()
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    peaks = _peaks()
+    gbs = width * height * POST_BYTES_PER_PIXEL / (ms / 1e3) / 1e9
+    out = {
+        "workload": "3840x2160 float3 HDR -> display: bloom extract at half resolution, 4 fused blur passes, "
+                    "resolve (exposure, bilinear bloom, ACES, sRGB); two HDR frames alternated (each frame's "
+                    "300 MB of traffic exceeds L2)",
+        "ms": ms, "steps": steps, "launches_per_frame": 2 + config.bloom_passes,
+        "algorithmic_bytes_per_pixel": POST_BYTES_PER_PIXEL, "achieved_gbs": gbs, "hbm_peak_gbs": peaks["hbm_gbs"],
+        "frac": gbs / peaks["hbm_gbs"],
+    }
+    pp.close()
+    del hdrs, display
+    torch.cuda.empty_cache()
+    return out
 
 
 def _batch(device, args) -> dict:

@@ -418,6 +418,39 @@ int atm_composite_noalloc(const AtmParams* params, const void* transmittance_lut
                           const double view_basis[9], double tangent_half_fov, double star_contrast_start,
                           double star_contrast_end, uint64_t* samples_out, void* stream);
 
+/* ---- display post-process -------------------------------------------------
+ * PostProcessor (src/planet_renderer/postprocess.py:75-207), the step after
+ * the atmosphere stage: bloom at half resolution (2x2 extract with the soft
+ * threshold and bright-pass cap, then separable 5-tap blur passes) and the
+ * display transform (exposure, bilinear bloom, ACES fit, sRGB).  The bloom
+ * planes are allocated at creation; atm_post_process is stream-ordered and
+ * capturable. */
+typedef struct AtmPostConfig { /* PostprocessConfig, postprocess.py:10-38 */
+  double exposure_ev;     /* finite, [-20, 20]; validated only: atm_post_process takes the EV */
+  double bloom_threshold; /* finite, >= 0 */
+  double bloom_knee;      /* finite, >= 0 */
+  double bloom_clamp;     /* finite, >= 0 */
+  double bloom_strength;  /* finite, >= 0 */
+  int32_t bloom_passes;   /* 0..8 */
+} AtmPostConfig;
+typedef struct AtmPost AtmPost;
+/* PostProcessor.__init__ (:78-86) with PostprocessConfig's validation
+ * (:21-38): ATM_E_INVALID with the reference's message on a bad field. */
+int atm_post_create(const AtmPostConfig* config, int32_t width, int32_t height, AtmPost** out);
+int atm_post_destroy(AtmPost* post);
+/* PostProcessor.process (:176-207): hdr -> display, both with `image`'s
+ * shape and strides (3 or 4 floats per pixel; display's first three are
+ * written, hdr is not modified).  Exposure 2^exposure_ev applies only when
+ * tone_map != 0; bloom runs when bloom != 0 and the configuration has
+ * passes and strength. */
+int atm_post_process(AtmPost* post, const float* hdr, float* display, const AtmImage* image, double exposure_ev,
+                     int32_t bloom, int32_t tone_map, void* stream);
+/* The half-resolution bloom plane of the last atm_post_process that ran
+ * bloom (dims: half width, half height), copied stream-ordered into
+ * dst_device (float4 [y][x], dims[0] * dims[1] texels; may be null to query
+ * dims), for inspection. */
+int atm_post_read_bloom(const AtmPost* post, int32_t dims[2], float* dst_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

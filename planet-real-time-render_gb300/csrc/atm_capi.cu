@@ -7,6 +7,7 @@
 // layer (which is a thin ctypes wrapper over these functions).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -732,7 +733,7 @@ ATM_API int atm_mlp_create(int32_t n_in, int32_t n_hidden_layers, int32_t n_out,
   if (!out) return fail(ATM_E_INVALID, "null output");
   *out = nullptr;
   if (n_in < 1 || n_in > 16 || n_out < 1 || n_out > 8 || n_hidden_layers < 1 || n_hidden_layers > 4)
-    return fail(ATM_E_INVALID, "MLP shape must have 1..8 inputs, 1..8 outputs and 1..4 hidden layers of 64");
+    return fail(ATM_E_INVALID, "MLP shape must have 1..16 inputs, 1..8 outputs and 1..4 hidden layers of 64");
   AtmMlp* m = new (std::nothrow) AtmMlp();
   if (!m) return fail(ATM_E_NOMEM, "host allocation failed");
   m->shape = atm::make_mlp_shape(n_in, n_hidden_layers, n_out);
@@ -1096,5 +1097,113 @@ ATM_API int atm_composite_noalloc(const AtmParams* params, const void* transmitt
                                          reinterpret_cast<unsigned long long*>(samples_out),
                                          static_cast<cudaStream_t>(stream)),
            "composite (no allocation)");
+  return ATM_OK;
+}
+
+// ---- display post-process ----------------------------------------------------
+struct AtmPost {
+  AtmPostConfig config{};
+  int32_t width = 0, height = 0;
+  atm::PostParams params{};
+  float4* bloom_a = nullptr;
+  float4* bloom_b = nullptr;
+  const float4* last_bloom = nullptr;
+};
+
+namespace {
+
+// PostprocessConfig.__post_init__ (postprocess.py:21-38), same messages.
+int check_post_config(const AtmPostConfig* c) {
+  if (!c) return fail(ATM_E_INVALID, "null AtmPostConfig");
+  if (!std::isfinite(c->exposure_ev) || !(c->exposure_ev >= -20.0 && c->exposure_ev <= 20.0))
+    return fail(ATM_E_INVALID, "postprocess.exposure_ev must be finite and in [-20, 20]");
+  const struct {
+    const char* name;
+    double value;
+  } fields[] = {{"bloom_threshold", c->bloom_threshold},
+                {"bloom_knee", c->bloom_knee},
+                {"bloom_clamp", c->bloom_clamp},
+                {"bloom_strength", c->bloom_strength}};
+  for (const auto& f : fields)
+    if (!std::isfinite(f.value) || f.value < 0.0)
+      return fail(ATM_E_INVALID, "postprocess.%s must be finite and non-negative", f.name);
+  if (c->bloom_passes < 0 || c->bloom_passes > 8) return fail(ATM_E_INVALID, "postprocess.bloom_passes must be in 0..8");
+  return ATM_OK;
+}
+
+}  // namespace
+
+ATM_API int atm_post_destroy(AtmPost* p) {
+  if (!p) return ATM_OK;
+  if (p->bloom_a) cudaFree(p->bloom_a);
+  if (p->bloom_b) cudaFree(p->bloom_b);
+  delete p;
+  return ATM_OK;
+}
+
+ATM_API int atm_post_create(const AtmPostConfig* config, int32_t width, int32_t height, AtmPost** out) {
+  if (!out) return fail(ATM_E_INVALID, "null output");
+  *out = nullptr;
+  int rc;
+  if ((rc = check_post_config(config))) return rc;
+  if (width < 1 || height < 1) return fail(ATM_E_INVALID, "post-process size must be at least 1x1");
+  AtmPost* p = new (std::nothrow) AtmPost();
+  if (!p) return fail(ATM_E_NOMEM, "host allocation failed");
+  p->config = *config;
+  p->width = width;
+  p->height = height;
+  atm::PostParams& Q = p->params;
+  Q.hw = std::max((width + 1) / 2, 1);  // PostProcessor.__init__ :81-82
+  Q.hh = std::max((height + 1) / 2, 1);
+  Q.threshold = float(config->bloom_threshold);
+  Q.knee = float(config->bloom_knee);
+  Q.two_knee = float(2.0 * config->bloom_knee);
+  Q.knee_div = float(std::max(4.0 * config->bloom_knee, 1.0e-6));
+  Q.clamp = float(config->bloom_clamp);
+  const size_t bytes = size_t(Q.hw) * size_t(Q.hh) * sizeof(float4);
+  cudaError_t e = cudaMalloc(&p->bloom_a, bytes);
+  if (e == cudaSuccess) e = cudaMalloc(&p->bloom_b, bytes);
+  if (e == cudaSuccess) e = cudaMemset(p->bloom_a, 0, bytes);
+  if (e != cudaSuccess) {
+    atm_post_destroy(p);
+    return cuda_fail(e, "post-process allocation");
+  }
+  p->last_bloom = p->bloom_a;
+  *out = p;
+  return ATM_OK;
+}
+
+ATM_API int atm_post_process(AtmPost* p, const float* hdr, float* display, const AtmImage* image, double exposure_ev,
+                             int32_t bloom, int32_t tone_map, void* stream) {
+  if (!p) return fail(ATM_E_INVALID, "null AtmPost");
+  if (!hdr || !display) return fail(ATM_E_INVALID, "null image pointer");
+  if (!image) return fail(ATM_E_INVALID, "null AtmImage");
+  if (image->width != p->width || image->height != p->height)
+    return fail(ATM_E_INVALID, "image is %dx%d but the post-process was created for %dx%d", image->width,
+                image->height, p->width, p->height);
+  if (image->channels != 3 && image->channels != 4) return fail(ATM_E_INVALID, "channels must be 3 or 4");
+  if (image->stride_x <= 0 || image->stride_y <= 0) return fail(ATM_E_INVALID, "image strides must be positive");
+  // PostProcessor.process :176-207: the multiplier and strength are f32 kernel arguments
+  const float exposure = tone_map ? float(std::pow(2.0, exposure_ev)) : 1.0f;
+  const bool use_bloom = bloom && p->config.bloom_passes > 0 && p->config.bloom_strength > 0.0;
+  const float4* result = nullptr;
+  ATM_CUDA(atm::launch_post(p->params, layout_of(image), hdr, display, p->bloom_a, p->bloom_b, exposure,
+                            float(p->config.bloom_strength), p->config.bloom_passes, use_bloom, tone_map != 0,
+                            &result, static_cast<cudaStream_t>(stream)),
+           "post-process");
+  if (use_bloom) p->last_bloom = result;
+  return ATM_OK;
+}
+
+ATM_API int atm_post_read_bloom(const AtmPost* p, int32_t dims[2], float* dst_device, void* stream) {
+  if (!p) return fail(ATM_E_INVALID, "null AtmPost");
+  if (dims) {
+    dims[0] = p->params.hw;
+    dims[1] = p->params.hh;
+  }
+  if (dst_device)
+    ATM_CUDA(cudaMemcpyAsync(dst_device, p->last_bloom, size_t(p->params.hw) * p->params.hh * sizeof(float4),
+                             cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)),
+             "bloom read");
   return ATM_OK;
 }

@@ -154,4 +154,19 @@ cudaError_t launch_composite_noalloc(const DevParams& P, const ImageLayout& L, c
                                      const float4* tlut, const float4* mslut, const float4* svlut, float* hdr,
                                      uint32_t* tile_scratch, unsigned long long* samples_out, cudaStream_t s);
 
+// Display post-process (atm_post.cu), float32 constants rounded on the host
+// the way the reference's Taichi trace rounds them.
+struct PostParams {
+  int hw, hh;             // bloom planes: max((W + 1) / 2, 1) x max((H + 1) / 2, 1), float4 [y][x]
+  float threshold, knee;  // f32(bloom_threshold), f32(bloom_knee)
+  float two_knee;         // f32(2 knee)
+  float knee_div;         // f32(max(4 knee, 1e-6))
+  float clamp;            // f32(bloom_clamp)
+};
+// Extract into bloom_a, `passes` blur passes ping-ponging between the planes
+// (*bloom_out: the plane holding the result), resolve into display.
+cudaError_t launch_post(const PostParams& Q, const ImageLayout& L, const float* hdr, float* display, float4* bloom_a,
+                        float4* bloom_b, float exposure, float strength, int passes, bool use_bloom, bool tone_map,
+                        const float4** bloom_out, cudaStream_t s);
+
 }  // namespace atm

@@ -174,6 +174,17 @@ class AtmSurrogate(ctypes.Structure):
 ATM_SURROGATE_SKY = 0
 ATM_SURROGATE_AERIAL = 1
 
+
+class AtmPostConfig(ctypes.Structure):
+    _fields_ = [
+        ("exposure_ev", ctypes.c_double),
+        ("bloom_threshold", ctypes.c_double),
+        ("bloom_knee", ctypes.c_double),
+        ("bloom_clamp", ctypes.c_double),
+        ("bloom_strength", ctypes.c_double),
+        ("bloom_passes", ctypes.c_int32),
+    ]
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _D = ctypes.c_double
@@ -229,6 +240,10 @@ SIGNATURES = {
         [_P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, c_double3, _D, c_double9,
          _D, _D, _D, ctypes.POINTER(AtmSurrogate), _P],
     ),
+    "atm_post_create": (ctypes.c_int, [ctypes.POINTER(AtmPostConfig), _I32, _I32, ctypes.POINTER(_P)]),
+    "atm_post_destroy": (ctypes.c_int, [_P]),
+    "atm_post_process": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(AtmImage), _D, _I32, _I32, _P]),
+    "atm_post_read_bloom": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P, _P]),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,

@@ -25,7 +25,10 @@ Scenarios:
       intervals): full LUTs, and a 1920x1080 frame sampled at selected pixels;
   earth_cameras
       the same LUTs re-keyed for cameras at 50 km and 2000 km with low suns
-      (twilight / terminator), composite sampled at selected pixels.
+      (twilight / terminator), composite sampled at selected pixels;
+  postprocess
+      the display post-process (src/planet_renderer/postprocess.py) on
+      seeded HDR images, eight configurations.
 
 The script reads the reference only when it runs; the tests read the .npz.
 """
@@ -251,6 +254,52 @@ def model_reference(reference: Path) -> dict:
     return out
 
 
+def postprocess_reference(reference: Path) -> dict:
+    """The reference's display post-process (src/planet_renderer/postprocess.py)
+    run unmodified on seeded HDR images: odd and even sizes, bloom on and
+    off, tone mapping on and off, 0-8 blur passes, thresholds and clamps that
+    make the soft knee and the bright-pass cap matter."""
+
+    shim.install()
+    sys.path.insert(0, str(reference / "src"))
+    from planet_renderer.postprocess import PostProcessor, PostprocessConfig  # type: ignore
+
+    rng = np.random.default_rng(4242)
+    cases = [
+        # (width, height, config kwargs, exposure_ev, bloom, tone_map)
+        (24, 16, {}, 0.0, True, True),
+        (23, 15, {"bloom_passes": 1}, 1.5, True, True),
+        (17, 9, {"bloom_threshold": 0.3, "bloom_knee": 0.2, "bloom_clamp": 2.0, "bloom_strength": 0.5,
+                 "bloom_passes": 8}, -2.0, True, True),
+        (24, 16, {}, 0.7, False, True),
+        (23, 15, {}, 3.0, True, False),
+        (9, 5, {"bloom_passes": 0}, 0.0, True, True),
+        (1, 1, {"bloom_passes": 2}, 0.0, True, True),
+        (16, 11, {"bloom_knee": 0.0, "bloom_strength": 0.25, "bloom_passes": 3}, -0.5, True, True),
+        (31, 7, {}, -6.0, True, True),  # dark: the sRGB linear segment
+    ]
+    out = {}
+    for k, (w, h, kw, ev, bloom, tone) in enumerate(cases):
+        # linear HDR: log-normal radiance with a few very bright texels (a sun disk)
+        hdr = np.exp(rng.normal(-1.0, 1.5, (w, h, 3))).astype(np.float32)
+        for _ in range(max(1, w * h // 60)):
+            hdr[rng.integers(0, w), rng.integers(0, h)] *= np.float32(rng.uniform(50.0, 5.0e4))
+        cfg = PostprocessConfig(**kw)
+        pp = PostProcessor(w, h, cfg)
+        src = shim.Vector.field(3, dtype=shim.f32, shape=(w, h))
+        src.from_numpy(hdr)
+        display = shim.Vector.field(3, dtype=shim.f32, shape=(w, h))
+        pp.process(src, display, ev, bloom=bloom, tone_map=tone)
+        assert np.array_equal(src.to_numpy(), hdr)  # the HDR source is never modified
+        out[f"case{k}_hdr"] = hdr
+        out[f"case{k}_display"] = display.to_numpy()
+        out[f"case{k}_args"] = np.array(json.dumps({"width": w, "height": h, "config": kw, "exposure_ev": ev,
+                                                    "bloom": bloom, "tone_map": tone}))
+    out["meta"] = np.array(json.dumps({"name": "postprocess", "cases": len(cases),
+                                       "generator": "reference postprocess.py through taichi_f32_shim"}))
+    return out
+
+
 def earth_config1_kwargs():
     return dict(
         mie_extinction_per_m=(3.996e-6 + 4.4e-6,) * 3,
@@ -293,6 +342,8 @@ def main() -> None:
         np.savez_compressed(HERE / f"tiny_orbit{suffix}.npz", **out)
     if want("model_reference") and args.precision == "f32":
         np.savez_compressed(HERE / "model_reference.npz", **model_reference(args.reference))
+    if want("postprocess") and args.precision == "f32":
+        np.savez_compressed(HERE / "postprocess.npz", **postprocess_reference(args.reference))
     renderer = None
     if args.precision == "f64":
         return

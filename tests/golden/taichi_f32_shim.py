@@ -264,6 +264,12 @@ abs = _unary(np.abs, _builtins.abs)  # noqa: A001 - mirrors ti.abs
 floor = _unary(np.floor, _pymath.floor)
 
 
+def pow(x, a):  # noqa: A001 - mirrors ti.pow
+    if _is_py(x) and _is_py(a):
+        return x ** a
+    return np.power(x, _FLOAT(a) if _is_py(a) else a)
+
+
 def atan2(y, x):
     if _is_py(y) and _is_py(x):
         return _pymath.atan2(y, x)
