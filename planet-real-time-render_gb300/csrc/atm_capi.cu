@@ -1108,6 +1108,7 @@ struct AtmPost {
   float4* bloom_a = nullptr;
   float4* bloom_b = nullptr;
   const float4* last_bloom = nullptr;
+  int last_x_fast = 1;  // orientation of last_bloom's storage
 };
 
 namespace {
@@ -1187,11 +1188,16 @@ ATM_API int atm_post_process(AtmPost* p, const float* hdr, float* display, const
   const float exposure = tone_map ? float(std::pow(2.0, exposure_ev)) : 1.0f;
   const bool use_bloom = bloom && p->config.bloom_passes > 0 && p->config.bloom_strength > 0.0;
   const float4* result = nullptr;
-  ATM_CUDA(atm::launch_post(p->params, layout_of(image), hdr, display, p->bloom_a, p->bloom_b, exposure,
+  atm::PostParams Q = p->params;
+  Q.x_fast = atm::image_x_fast(layout_of(image)) ? 1 : 0;
+  ATM_CUDA(atm::launch_post(Q, layout_of(image), hdr, display, p->bloom_a, p->bloom_b, exposure,
                             float(p->config.bloom_strength), p->config.bloom_passes, use_bloom, tone_map != 0,
                             &result, static_cast<cudaStream_t>(stream)),
            "post-process");
-  if (use_bloom) p->last_bloom = result;
+  if (use_bloom) {
+    p->last_bloom = result;
+    p->last_x_fast = Q.x_fast;
+  }
   return ATM_OK;
 }
 
@@ -1201,9 +1207,12 @@ ATM_API int atm_post_read_bloom(const AtmPost* p, int32_t dims[2], float* dst_de
     dims[0] = p->params.hw;
     dims[1] = p->params.hh;
   }
-  if (dst_device)
-    ATM_CUDA(cudaMemcpyAsync(dst_device, p->last_bloom, size_t(p->params.hw) * p->params.hh * sizeof(float4),
-                             cudaMemcpyDeviceToDevice, static_cast<cudaStream_t>(stream)),
+  if (dst_device) {
+    atm::PostParams Q = p->params;
+    Q.x_fast = p->last_x_fast;
+    ATM_CUDA(atm::launch_post_read_bloom(Q, p->last_bloom, reinterpret_cast<float4*>(dst_device),
+                                         static_cast<cudaStream_t>(stream)),
              "bloom read");
+  }
   return ATM_OK;
 }

@@ -157,7 +157,8 @@ cudaError_t launch_composite_noalloc(const DevParams& P, const ImageLayout& L, c
 // Display post-process (atm_post.cu), float32 constants rounded on the host
 // the way the reference's Taichi trace rounds them.
 struct PostParams {
-  int hw, hh;             // bloom planes: max((W + 1) / 2, 1) x max((H + 1) / 2, 1), float4 [y][x]
+  int hw, hh;             // bloom planes: max((W + 1) / 2, 1) x max((H + 1) / 2, 1) float4 texels
+  int x_fast;             // image and bloom planes with x the contiguous axis ([y][x]); else [x][y]
   float threshold, knee;  // f32(bloom_threshold), f32(bloom_knee)
   float two_knee;         // f32(2 knee)
   float knee_div;         // f32(max(4 knee, 1e-6))
@@ -168,5 +169,9 @@ struct PostParams {
 cudaError_t launch_post(const PostParams& Q, const ImageLayout& L, const float* hdr, float* display, float4* bloom_a,
                         float4* bloom_b, float exposure, float strength, int passes, bool use_bloom, bool tone_map,
                         const float4** bloom_out, cudaStream_t s);
+// Whether x is the image's contiguous axis (the orientation of its bloom planes).
+bool image_x_fast(const ImageLayout& L);
+// A bloom plane of orientation Q.x_fast copied into dst as float4 [y][x].
+cudaError_t launch_post_read_bloom(const PostParams& Q, const float4* bloom, float4* dst, cudaStream_t s);
 
 }  // namespace atm

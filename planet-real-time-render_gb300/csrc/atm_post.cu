@@ -6,12 +6,15 @@
 //
 // Memory-bound work: HDR is read twice (extract, resolve) and the display
 // written once; the half-resolution bloom planes (float4, W/2 x H/2) stay in
-// L2 between the kernels.  Each blur pass is one kernel: a 32 x 8 tile of
+// L2 between the kernels.  A bloom plane is stored with the image's
+// contiguous axis fastest, so the extract's HDR reads and writes and the
+// resolve's bloom taps are coalesced in either image layout.  Each blur pass
+// is one kernel (the reference's two kernels per pass): a 32 x 8 tile of
 // output texels loads its 36 x 12 neighbourhood once into shared memory and
-// runs the horizontal and then the vertical taps from there (the reference's
-// two kernels per pass).  Edge rules are the reference's clamped indices;
-// the clamp is applied where the tile is loaded, which gives every tap the
-// texel the reference reads.
+// runs the x taps and then the y taps from there, along whichever storage
+// axis each lies.  Edge rules are the reference's clamped indices; the clamp
+// is applied where the tile is loaded, which gives every tap the texel the
+// reference reads.
 //
 // Arithmetic is IEEE float32 in the reference's operation order with no
 // contraction (__fmul_rn / __fadd_rn): every result is the reference's
@@ -69,12 +72,19 @@ __device__ __forceinline__ float4 soft_threshold(float4 v, const PostParams& Q) 
   return scale4(r, fminf_(1.0f, __fdiv_rn(Q.clamp, fmaxf_(peak, 1.0e-6f))));
 }
 
-// _extract, postprocess.py:110-119: one thread per half-resolution texel.
+// Storage index of bloom texel (x, y): [y][x] when x is the fast axis, else [x][y].
+__device__ __forceinline__ size_t bloom_index(const PostParams& Q, int x, int y) {
+  return Q.x_fast ? size_t(y) * Q.hw + x : size_t(x) * Q.hh + y;
+}
+
+// _extract, postprocess.py:110-119: one thread per half-resolution texel, in
+// storage order.
 __global__ void __launch_bounds__(256) k_post_extract(PostParams Q, ImageLayout L, const float* __restrict__ hdr,
                                                       float scale, float4* __restrict__ bloom) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= Q.hw * Q.hh) return;
-  const int x = i % Q.hw, y = i / Q.hw;
+  const int x = Q.x_fast ? i % Q.hw : i / Q.hh;
+  const int y = Q.x_fast ? i / Q.hw : i % Q.hh;
   float4 v = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll
   for (int ox = 0; ox < 2; ++ox)
@@ -84,33 +94,57 @@ __global__ void __launch_bounds__(256) k_post_extract(PostParams Q, ImageLayout 
   bloom[i] = soft_threshold(scale4(v, scale), Q);
 }
 
-// One blur pass (_blur_horizontal then _blur_vertical, :121-139) fused.
-constexpr int kTileX = 32, kTileY = 8, kHalo = 2;
-constexpr int kInX = kTileX + 2 * kHalo, kInY = kTileY + 2 * kHalo;
+// One blur pass (_blur_horizontal then _blur_vertical, :121-139) fused.  The
+// tile is kTileS rows of the slow storage axis by kTileF texels of the fast
+// one; kXFast: x (the first pass) runs along the fast axis.
+constexpr int kTileF = 32, kTileS = 8, kHalo = 2;
+constexpr int kInF = kTileF + 2 * kHalo, kInS = kTileS + 2 * kHalo;
 
-__global__ void __launch_bounds__(kTileX * kTileY) k_post_blur(PostParams Q, const float4* __restrict__ src,
+template <bool kXFast>
+__global__ void __launch_bounds__(kTileF * kTileS) k_post_blur(PostParams Q, const float4* __restrict__ src,
                                                                float4* __restrict__ dst) {
-  __shared__ float4 s_in[kInY][kInX];
-  __shared__ float4 s_h[kInY][kTileX];
+  __shared__ float4 s_in[kInS][kInF];
+  __shared__ float4 s_mid[kInS][kInF];  // after the x taps
   const int t = threadIdx.x;
-  const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY;
-  for (int k = t; k < kInY * kInX; k += kTileX * kTileY) {
-    const int r = k / kInX, c = k % kInX;
-    const int gx = min(max(x0 - kHalo + c, 0), Q.hw - 1);
-    const int gy = min(max(y0 - kHalo + r, 0), Q.hh - 1);
-    s_in[r][c] = src[size_t(gy) * Q.hw + gx];
+  const int nf = kXFast ? Q.hw : Q.hh, ns = kXFast ? Q.hh : Q.hw;  // fast / slow extents
+  const int f0 = blockIdx.x * kTileF, s0 = blockIdx.y * kTileS;
+  for (int k = t; k < kInS * kInF; k += kTileF * kTileS) {
+    const int r = k / kInF, c = k % kInF;
+    const int gf = min(max(f0 - kHalo + c, 0), nf - 1);
+    const int gs = min(max(s0 - kHalo + r, 0), ns - 1);
+    s_in[r][c] = src[size_t(gs) * nf + gf];
   }
   __syncthreads();
-  // horizontal taps for the tile's columns on all kInY (clamped) rows
-  for (int k = t; k < kInY * kTileX; k += kTileX * kTileY) {
-    const int r = k / kTileX, c = k % kTileX + kHalo;
-    s_h[r][c - kHalo] = taps5(s_in[r][c], s_in[r][c - 1], s_in[r][c + 1], s_in[r][c - 2], s_in[r][c + 2]);
+  if (kXFast) {
+    // x taps along the fast axis on every (clamped) slow row, then y taps along the slow axis
+    for (int k = t; k < kInS * kTileF; k += kTileF * kTileS) {
+      const int r = k / kTileF, c = k % kTileF + kHalo;
+      s_mid[r][c] = taps5(s_in[r][c], s_in[r][c - 1], s_in[r][c + 1], s_in[r][c - 2], s_in[r][c + 2]);
+    }
+  } else {
+    // x taps along the slow axis on every (clamped) fast column, then y taps along the fast axis
+    for (int k = t; k < kTileS * kInF; k += kTileF * kTileS) {
+      const int r = k / kInF + kHalo, c = k % kInF;
+      s_mid[r][c] = taps5(s_in[r][c], s_in[r - 1][c], s_in[r + 1][c], s_in[r - 2][c], s_in[r + 2][c]);
+    }
   }
   __syncthreads();
-  const int c = t % kTileX, r = t / kTileX + kHalo;
-  const int x = x0 + c, y = y0 + r - kHalo;
-  if (x < Q.hw && y < Q.hh)
-    dst[size_t(y) * Q.hw + x] = taps5(s_h[r][c], s_h[r - 1][c], s_h[r + 1][c], s_h[r - 2][c], s_h[r + 2][c]);
+  const int c = t % kTileF + kHalo, r = t / kTileF + kHalo;
+  const int f = f0 + c - kHalo, sl = s0 + r - kHalo;
+  if (f < nf && sl < ns) {
+    const float4 out = kXFast ? taps5(s_mid[r][c], s_mid[r - 1][c], s_mid[r + 1][c], s_mid[r - 2][c], s_mid[r + 2][c])
+                              : taps5(s_mid[r][c], s_mid[r][c - 1], s_mid[r][c + 1], s_mid[r][c - 2], s_mid[r][c + 2]);
+    dst[size_t(sl) * nf + f] = out;
+  }
+}
+
+// Storage [x][y] -> [y][x] (the bloom plane's read-back).
+__global__ void __launch_bounds__(256) k_post_transpose(const float4* __restrict__ src, float4* __restrict__ dst,
+                                                        int hw, int hh) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= hw * hh) return;
+  const int x = i % hw, y = i / hw;
+  dst[i] = src[size_t(x) * hh + y];
 }
 
 // _sample_bloom, postprocess.py:141-153.
@@ -123,8 +157,8 @@ __device__ __forceinline__ float4 sample_bloom(const float4* __restrict__ bloom,
   const int x1 = min(x0 + 1, Q.hw - 1), y1 = min(y0 + 1, Q.hh - 1);
   const float fx = clampf_(sub(px, fpx), 0.0f, 1.0f), fy = clampf_(sub(py, fpy), 0.0f, 1.0f);
   const float gx = sub(1.0f, fx), gy = sub(1.0f, fy);
-  const float4 low = add4(scale4(bloom[size_t(y0) * Q.hw + x0], gx), scale4(bloom[size_t(y0) * Q.hw + x1], fx));
-  const float4 high = add4(scale4(bloom[size_t(y1) * Q.hw + x0], gx), scale4(bloom[size_t(y1) * Q.hw + x1], fx));
+  const float4 low = add4(scale4(bloom[bloom_index(Q, x0, y0)], gx), scale4(bloom[bloom_index(Q, x1, y0)], fx));
+  const float4 high = add4(scale4(bloom[bloom_index(Q, x0, y1)], gx), scale4(bloom[bloom_index(Q, x1, y1)], fx));
   return add4(scale4(low, gy), scale4(high, fy));
 }
 
@@ -139,15 +173,14 @@ __device__ __forceinline__ float display_channel(float v) {
 }
 
 // _resolve, postprocess.py:155-174: one thread per pixel, threads along the
-// image's contiguous axis.
+// image's contiguous axis (Q.x_fast).
 __global__ void __launch_bounds__(256) k_post_resolve(PostParams Q, ImageLayout L, const float* __restrict__ hdr,
                                                       float* __restrict__ display, const float4* __restrict__ bloom,
                                                       float exposure, float strength, int use_bloom, int tone_map) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= int64_t(L.width) * L.height) return;
-  const bool y_fast = (L.sy < 0 ? -L.sy : L.sy) <= (L.sx < 0 ? -L.sx : L.sx);
-  const int x = y_fast ? int(i / L.height) : int(i % L.width);
-  const int y = y_fast ? int(i % L.height) : int(i / L.width);
+  const int x = Q.x_fast ? int(i % L.width) : int(i / L.height);
+  const int y = Q.x_fast ? int(i / L.width) : int(i % L.height);
   float4 v = scale4(load_rgb(hdr, L, x, y), exposure);
   if (use_bloom) {
     const float u = __fdiv_rn(add(float(x), 0.5f), float(L.width));
@@ -168,6 +201,11 @@ __global__ void __launch_bounds__(256) k_post_resolve(PostParams Q, ImageLayout 
 
 }  // namespace
 
+bool image_x_fast(const ImageLayout& L) {
+  const int64_t ax = L.sx < 0 ? -L.sx : L.sx, ay = L.sy < 0 ? -L.sy : L.sy;
+  return ax < ay;
+}
+
 cudaError_t launch_post(const PostParams& Q, const ImageLayout& L, const float* hdr, float* display, float4* bloom_a,
                         float4* bloom_b, float exposure, float strength, int passes, bool use_bloom, bool tone_map,
                         const float4** bloom_out, cudaStream_t s) {
@@ -177,11 +215,15 @@ cudaError_t launch_post(const PostParams& Q, const ImageLayout& L, const float* 
     k_post_extract<<<(n + 255) / 256, 256, 0, s>>>(Q, L, hdr, 0.25f * exposure, bloom_a);  // exact: a power of two
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const dim3 grid((Q.hw + kTileX - 1) / kTileX, (Q.hh + kTileY - 1) / kTileY);
+    const int nf = Q.x_fast ? Q.hw : Q.hh, ns = Q.x_fast ? Q.hh : Q.hw;
+    const dim3 grid((nf + kTileF - 1) / kTileF, (ns + kTileS - 1) / kTileS);
     float4* src = bloom_a;
     float4* dst = bloom_b;
     for (int p = 0; p < passes; ++p) {
-      k_post_blur<<<grid, kTileX * kTileY, 0, s>>>(Q, src, dst);
+      if (Q.x_fast)
+        k_post_blur<true><<<grid, kTileF * kTileS, 0, s>>>(Q, src, dst);
+      else
+        k_post_blur<false><<<grid, kTileF * kTileS, 0, s>>>(Q, src, dst);
       e = cudaGetLastError();
       if (e != cudaSuccess) return e;
       float4* tmp = src;
@@ -194,6 +236,13 @@ cudaError_t launch_post(const PostParams& Q, const ImageLayout& L, const float* 
   const int64_t pixels = int64_t(L.width) * L.height;
   k_post_resolve<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(Q, L, hdr, display, bloom, exposure, strength,
                                                                  use_bloom ? 1 : 0, tone_map ? 1 : 0);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_post_read_bloom(const PostParams& Q, const float4* bloom, float4* dst, cudaStream_t s) {
+  const size_t n = size_t(Q.hw) * Q.hh;
+  if (Q.x_fast) return cudaMemcpyAsync(dst, bloom, n * sizeof(float4), cudaMemcpyDeviceToDevice, s);
+  k_post_transpose<<<unsigned((n + 255) / 256), 256, 0, s>>>(bloom, dst, Q.hw, Q.hh);
   return cudaGetLastError();
 }
 
