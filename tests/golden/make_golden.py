@@ -28,7 +28,11 @@ Scenarios:
       (twilight / terminator), composite sampled at selected pixels;
   postprocess
       the display post-process (src/planet_renderer/postprocess.py) on
-      seeded HDR images, eight configurations.
+      seeded HDR images, nine configurations;
+  shading
+      the surface shading that consumes prepare_frame's outputs
+      (renderer.py:1277-1575) on seeded G-buffers: land, ocean (BRDF,
+      refracted seabed) and sky pixels, five configurations.
 
 The script reads the reference only when it runs; the tests read the .npz.
 """
@@ -300,6 +304,126 @@ def postprocess_reference(reference: Path) -> dict:
     return out
 
 
+def shading_reference(reference: Path) -> dict:
+    """The reference's surface shading (PlanetRenderer._shade_surface,
+    src/planet_renderer/renderer.py:1277-1575), the consumer of
+    prepare_frame's surface_sun_transmittance / surface_sky_radiance, run
+    unmodified on seeded G-buffers with land, ocean and sky pixels: the
+    Lambert path, the ocean BRDF with refracted seabed reconstruction from the
+    terrain snapshot, the flat-ocean fallback and the albedo debug mode."""
+
+    shim.install()
+    sys.path.insert(0, str(reference / "src"))
+    from planet_renderer.ocean import OCEAN_SURFACE_ID, OceanConfig  # type: ignore
+    from planet_renderer.renderer import PlanetRenderer  # type: ignore
+
+    from planet_renderer_gb300 import camera as cam
+
+    ocean = OceanConfig()
+    cases = [
+        # (width, height, seed, advanced_ocean, mode, refraction strength, max offset px, yaw, pitch)
+        (24, 16, 11, 1, 0, ocean.refraction_strength, ocean.refraction_max_offset_pixels, 10.0, -20.0),
+        (17, 11, 12, 1, 0, 0.5, 0.3, -40.0, -35.0),  # offsets clamped to 0.3 px
+        (24, 16, 13, 0, 0, ocean.refraction_strength, ocean.refraction_max_offset_pixels, 0.0, -10.0),
+        (24, 16, 14, 1, 1, ocean.refraction_strength, ocean.refraction_max_offset_pixels, 0.0, -10.0),
+        (20, 12, 15, 1, 0, 0.0, ocean.refraction_max_offset_pixels, 75.0, -60.0),
+    ]
+    out = {}
+    for k, (w, h, seed, advanced, mode, strength, max_offset, yaw, pitch) in enumerate(cases):
+        rng = np.random.default_rng(seed)
+        f32 = np.float32
+
+        def vec_field(values):
+            fld = shim.Vector.field(values.shape[-1], dtype=shim.f32, shape=(w, h))
+            fld.from_numpy(values.astype(f32))
+            return fld
+
+        def scalar_field(values, dtype):
+            fld = shim.field(dtype=dtype, shape=(w, h))
+            fld.from_numpy(values)
+            return fld
+
+        tanfov = cam.tangent_half_fov(60.0)
+        basis = cam.view_basis(yaw, pitch)
+        # view-space positions along the pixels' rays at 50 m - 3 km
+        xs = (np.arange(w) + 0.5) / w * 2.0 - 1.0
+        ys = (np.arange(h) + 0.5) / h * 2.0 - 1.0
+        aspect = w / h
+        rays = np.stack(np.broadcast_arrays(xs[:, None] * tanfov * aspect, ys[None, :] * tanfov,
+                                            np.ones((w, h))), -1)
+        depth = rng.uniform(50.0, 3000.0, (w, h))
+        position = rays * depth[..., None]
+        surface_id = np.where(rng.random((w, h)) < 0.5, OCEAN_SURFACE_ID, rng.integers(0, 1000, (w, h)))
+        surface_id[:, -2:] = -1  # sky rows at the top
+        surface_id = surface_id.astype(np.int32)
+        up = np.array([0.0, 1.0, 0.0])
+        normal = up + rng.normal(0.0, 0.25, (w, h, 3))
+        albedo = rng.uniform(0.02, 0.5, (w, h, 3))
+        water_depth = rng.uniform(0.0, 120.0, (w, h))
+        seabed_albedo = rng.uniform(0.05, 0.4, (w, h, 3))
+        seabed_normal = up + rng.normal(0.0, 0.3, (w, h, 3))
+        slope_variance = rng.uniform(0.0, 0.05, (w, h))
+        # opaque terrain snapshot: the seabed a little behind the water surface
+        terrain_position = position + rays * rng.uniform(0.0, 40.0, (w, h))[..., None]
+        terrain_id = np.where(rng.random((w, h)) < 0.85, rng.integers(0, 1000, (w, h)), -1).astype(np.int32)
+        terrain_normal = up + rng.normal(0.0, 0.3, (w, h, 3))
+        terrain_albedo = rng.uniform(0.05, 0.4, (w, h, 3))
+        sun_t = rng.uniform(0.05, 1.0, (w, h, 3))
+        sky_l = rng.uniform(0.001, 0.3, (w, h, 3))
+        sun = np.array(cam.sun_from_zenith(float(rng.uniform(10.0, 85.0)), float(rng.uniform(0.0, 360.0))))
+
+        renderer = PlanetRenderer.__new__(PlanetRenderer)  # fields only: the kernel reads nothing else
+        renderer.width, renderer.height = w, h
+        renderer.gbuffer_position = vec_field(position)
+        renderer.gbuffer_normal = vec_field(normal)
+        renderer.gbuffer_albedo = vec_field(albedo)
+        renderer.gbuffer_water_depth_m = scalar_field(water_depth.astype(f32), shim.f32)
+        renderer.gbuffer_seabed_albedo = vec_field(seabed_albedo)
+        renderer.gbuffer_seabed_normal = vec_field(seabed_normal)
+        renderer.gbuffer_ocean_slope_variance = scalar_field(slope_variance.astype(f32), shim.f32)
+        renderer.gbuffer_surface_id = scalar_field(surface_id, shim.i32)
+        renderer.terrain_position = vec_field(terrain_position)
+        renderer.terrain_normal = vec_field(terrain_normal)
+        renderer.terrain_albedo = vec_field(terrain_albedo)
+        renderer.terrain_surface_id = scalar_field(terrain_id, shim.i32)
+        renderer.surface_hdr = shim.Vector.field(3, dtype=shim.f32, shape=(w, h))
+        sun_t_field, sky_field = vec_field(sun_t), vec_field(sky_l)
+        args = dict(sun_global=tuple(float(v) for v in sun), solar_irradiance=(4.0, 3.9, 3.7),
+                    view_right_global=tuple(float(v) for v in basis[0]),
+                    view_up_global=tuple(float(v) for v in basis[1]),
+                    view_forward_global=tuple(float(v) for v in basis[2]),
+                    advanced_ocean_enabled=advanced, ocean_roughness=ocean.roughness, ocean_f0=ocean.dielectric_f0,
+                    ocean_sky_strength=ocean.sky_reflection_strength,
+                    ocean_absorption=tuple(ocean.absorption_per_m), ocean_scattering=tuple(ocean.scattering_per_m),
+                    ocean_max_depth=ocean.max_visible_depth_m, ocean_refraction_index=ocean.refraction_index,
+                    ocean_refraction_strength=float(strength), ocean_refraction_max_offset_pixels=float(max_offset),
+                    sun_angular_radius=math.radians(0.266), tangent_half_fov=float(tanfov), mode=mode)
+        renderer._shade_surface(args["sun_global"], args["solar_irradiance"], sun_t_field, sky_field,
+                                *(args[n] for n in ("view_right_global", "view_up_global", "view_forward_global",
+                                                   "advanced_ocean_enabled", "ocean_roughness", "ocean_f0",
+                                                   "ocean_sky_strength", "ocean_absorption", "ocean_scattering",
+                                                   "ocean_max_depth", "ocean_refraction_index",
+                                                   "ocean_refraction_strength",
+                                                   "ocean_refraction_max_offset_pixels", "sun_angular_radius",
+                                                   "tangent_half_fov", "mode")))
+        for name, fld in (("position", renderer.gbuffer_position), ("normal", renderer.gbuffer_normal),
+                          ("albedo", renderer.gbuffer_albedo), ("water_depth", renderer.gbuffer_water_depth_m),
+                          ("seabed_albedo", renderer.gbuffer_seabed_albedo),
+                          ("seabed_normal", renderer.gbuffer_seabed_normal),
+                          ("slope_variance", renderer.gbuffer_ocean_slope_variance),
+                          ("surface_id", renderer.gbuffer_surface_id),
+                          ("terrain_position", renderer.terrain_position),
+                          ("terrain_normal", renderer.terrain_normal), ("terrain_albedo", renderer.terrain_albedo),
+                          ("terrain_surface_id", renderer.terrain_surface_id),
+                          ("sun_transmittance", sun_t_field), ("sky_radiance", sky_field),
+                          ("surface_hdr", renderer.surface_hdr)):
+            out[f"case{k}_{name}"] = fld.to_numpy()
+        out[f"case{k}_args"] = np.array(json.dumps(args))
+    out["meta"] = np.array(json.dumps({"name": "shading", "cases": len(cases), "ocean_surface_id": OCEAN_SURFACE_ID,
+                                       "generator": "reference renderer.py _shade_surface through taichi_f32_shim"}))
+    return out
+
+
 def earth_config1_kwargs():
     return dict(
         mie_extinction_per_m=(3.996e-6 + 4.4e-6,) * 3,
@@ -342,6 +466,8 @@ def main() -> None:
         np.savez_compressed(HERE / f"tiny_orbit{suffix}.npz", **out)
     if want("model_reference") and args.precision == "f32":
         np.savez_compressed(HERE / "model_reference.npz", **model_reference(args.reference))
+    if want("shading") and args.precision == "f32":
+        np.savez_compressed(HERE / "shading.npz", **shading_reference(args.reference))
     if want("postprocess") and args.precision == "f32":
         np.savez_compressed(HERE / "postprocess.npz", **postprocess_reference(args.reference))
     renderer = None

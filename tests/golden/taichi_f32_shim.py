@@ -39,6 +39,16 @@ import numpy as np
 f32 = np.float32
 i32 = np.int32
 f64 = np.float64
+# integer and other types that only appear in annotations and field
+# declarations of modules the golden scripts import but do not run
+u8 = np.uint8
+u16 = np.uint16
+u32 = np.uint32
+u64 = np.uint64
+i8 = np.int8
+i16 = np.int16
+i64 = np.int64
+f16 = np.float16
 
 _F = np.float32
 
@@ -166,7 +176,7 @@ class Field:
         self.data = np.zeros(full, dtype=self.dtype)
 
     def _key(self, idx):
-        if isinstance(idx, (tuple, list)):
+        if isinstance(idx, (tuple, list, np.ndarray)):
             return tuple(int(v) for v in idx)
         return (int(idx),)
 
@@ -201,6 +211,9 @@ class Field:
 
 class _VectorNamespace:
     def __call__(self, values, dt=None):
+        items = list(values) if isinstance(values, (list, tuple)) else None
+        if items and all(isinstance(v, (int, np.integer)) and not isinstance(v, bool) for v in items):
+            return Vec(items, dtype=np.int64)  # an integer vector (ti.i32)
         return Vec(values)
 
     @staticmethod
@@ -234,8 +247,16 @@ def static(value):
 
 def cast(value, dtype):
     if dtype is i32:
+        if isinstance(value, (np.ndarray, tuple, list)):  # vectors: element-wise, truncating
+            return Vec(np.trunc(np.asarray(value, dtype=np.float64)).astype(np.int64), dtype=np.int64)
         return int(value)
+    if isinstance(value, (tuple, list)):
+        return Vec([_FLOAT(v) for v in value])
     return _FLOAT(value)
+
+
+def select(cond, a, b):
+    return a if cond else b
 
 
 def _is_py(value) -> bool:
@@ -262,6 +283,7 @@ cos = _unary(np.cos, _pymath.cos)
 sin = _unary(np.sin, _pymath.sin)
 abs = _unary(np.abs, _builtins.abs)  # noqa: A001 - mirrors ti.abs
 floor = _unary(np.floor, _pymath.floor)
+tan = _unary(np.tan, _pymath.tan)
 
 
 def pow(x, a):  # noqa: A001 - mirrors ti.pow
@@ -313,10 +335,20 @@ class _VectorType:
         self.dtype = dtype
 
 
+class _Annotation:
+    """Placeholder for annotations of kernels the golden scripts never call."""
+
+    def __init__(self, *args, **kwargs):
+        self.args, self.kwargs = args, kwargs
+
+
 class _Types:
     @staticmethod
     def vector(n, dtype):
         return _VectorType(n, dtype)
+
+    ndarray = _Annotation
+    matrix = _Annotation
 
 
 types_ = _Types()
