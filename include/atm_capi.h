@@ -451,6 +451,58 @@ int atm_post_process(AtmPost* post, const float* hdr, float* display, const AtmI
  * dims), for inspection. */
 int atm_post_read_bloom(const AtmPost* post, int32_t dims[2], float* dst_device, void* stream);
 
+/* ---- surface shading -----------------------------------------------------
+ * PlanetRenderer._shade_surface (src/planet_renderer/renderer.py:1277-1575),
+ * the consumer of atm_prepare_frame's surface_sun_transmittance and
+ * surface_sky_radiance: Lambertian land; ocean pixels (advanced ocean on) with
+ * a GGX-style sun specular, Fresnel sky reflection and a water body over a
+ * seabed reconstructed along the refracted view ray from the opaque terrain
+ * snapshot.  Arguments as the reference kernel's (rounded to float32). */
+typedef struct AtmShadeParams {
+  double sun_global[3];
+  double solar_irradiance[3];
+  double view_right_global[3];
+  double view_up_global[3];
+  double view_forward_global[3];
+  int32_t advanced_ocean_enabled;
+  int32_t mode; /* 0 lit; otherwise albedo (the debug views) */
+  double ocean_roughness;
+  double ocean_f0;
+  double ocean_sky_strength;
+  double ocean_absorption[3];
+  double ocean_scattering[3];
+  double ocean_max_depth;
+  double ocean_refraction_index;
+  double ocean_refraction_strength;
+  double ocean_refraction_max_offset_pixels;
+  double sun_angular_radius; /* radians */
+  double tangent_half_fov;
+  int32_t ocean_surface_id; /* OCEAN_SURFACE_ID (ocean.py:17) */
+  int32_t reserved;
+} AtmShadeParams;
+/* Device images, all of `image`'s shape and element strides: float images
+ * with image->channels floats per element (the first three read or written),
+ * water_depth and slope_variance one float, the ids one int32. */
+typedef struct AtmShadeImages {
+  const float* position;       /* view space (gbuffer_position) */
+  const float* normal;         /* global frame (gbuffer_normal) */
+  const float* albedo;
+  const float* water_depth;    /* gbuffer_water_depth_m */
+  const float* seabed_albedo;
+  const float* seabed_normal;
+  const float* slope_variance; /* gbuffer_ocean_slope_variance */
+  const int32_t* surface_id;
+  const float* terrain_position; /* the opaque terrain snapshot */
+  const float* terrain_normal;
+  const float* terrain_albedo;
+  const int32_t* terrain_surface_id;
+  const float* sun_transmittance; /* atm_prepare_frame outputs */
+  const float* sky_radiance;
+  float* surface_hdr;             /* output */
+} AtmShadeImages;
+int atm_shade_surface(const AtmShadeParams* params, const AtmShadeImages* images, const AtmImage* image,
+                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif

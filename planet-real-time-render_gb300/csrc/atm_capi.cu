@@ -1216,3 +1216,52 @@ ATM_API int atm_post_read_bloom(const AtmPost* p, int32_t dims[2], float* dst_de
   }
   return ATM_OK;
 }
+
+// ---- surface shading -------------------------------------------------------------
+ATM_API int atm_shade_surface(const AtmShadeParams* p, const AtmShadeImages* im, const AtmImage* image,
+                              void* stream) {
+  if (!p || !im || !image) return fail(ATM_E_INVALID, "null argument");
+  if (image->width < 1 || image->height < 1) return fail(ATM_E_INVALID, "image must be at least 1x1");
+  if (image->channels != 3 && image->channels != 4) return fail(ATM_E_INVALID, "channels must be 3 or 4");
+  if (image->stride_x <= 0 || image->stride_y <= 0) return fail(ATM_E_INVALID, "image strides must be positive");
+  const void* required[] = {im->position, im->normal, im->albedo, im->water_depth, im->seabed_albedo,
+                            im->seabed_normal, im->slope_variance, im->surface_id, im->terrain_position,
+                            im->terrain_normal, im->terrain_albedo, im->terrain_surface_id, im->sun_transmittance,
+                            im->sky_radiance, im->surface_hdr};
+  for (const void* q : required)
+    if (!q) return fail(ATM_E_INVALID, "null image pointer");
+  const double* finite[] = {p->sun_global, p->solar_irradiance, p->view_right_global, p->view_up_global,
+                            p->view_forward_global, p->ocean_absorption, p->ocean_scattering};
+  for (const double* v : finite)
+    if (!finite_n(v, 3)) return fail(ATM_E_INVALID, "vector arguments must be finite");
+  atm::ShadeParams S{};
+  to_f32(p->sun_global, S.sun, 3);
+  to_f32(p->solar_irradiance, S.E, 3);
+  to_f32(p->view_right_global, S.right, 3);
+  to_f32(p->view_up_global, S.up, 3);
+  to_f32(p->view_forward_global, S.fwd, 3);
+  S.advanced = p->advanced_ocean_enabled != 0;
+  S.mode = p->mode;
+  S.roughness = float(p->ocean_roughness);
+  S.f0 = float(p->ocean_f0);
+  S.sky_strength = float(p->ocean_sky_strength);
+  for (int k = 0; k < 3; ++k) {  // renderer.py:1521, :1546-1549, in float32
+    S.extinction[k] = float(p->ocean_absorption[k]) + float(p->ocean_scattering[k]);
+    S.scattering_albedo[k] = float(p->ocean_scattering[k]) / std::max(S.extinction[k], 1.0e-6f);
+  }
+  S.max_depth = float(p->ocean_max_depth);
+  S.eta = 1.0f / float(p->ocean_refraction_index);  // :1402
+  S.strength = float(p->ocean_refraction_strength);
+  S.max_offset = float(p->ocean_refraction_max_offset_pixels);
+  const float t = std::tan(float(p->sun_angular_radius));  // :1345
+  S.solar_slope_variance = t * t;
+  S.tanfov = float(p->tangent_half_fov);
+  S.four_pi = float(4.0 * kPi);
+  S.ocean_id = p->ocean_surface_id;
+  atm::ShadeImages I{im->position,       im->normal,         im->albedo,         im->water_depth,
+                     im->seabed_albedo,  im->seabed_normal,  im->slope_variance, im->surface_id,
+                     im->terrain_position, im->terrain_normal, im->terrain_albedo, im->terrain_surface_id,
+                     im->sun_transmittance, im->sky_radiance, im->surface_hdr};
+  ATM_CUDA(atm::launch_shade_surface(S, layout_of(image), I, static_cast<cudaStream_t>(stream)), "surface shading");
+  return ATM_OK;
+}

@@ -169,6 +169,44 @@ struct PostParams {
 cudaError_t launch_post(const PostParams& Q, const ImageLayout& L, const float* hdr, float* display, float4* bloom_a,
                         float4* bloom_b, float exposure, float strength, int passes, bool use_bloom, bool tone_map,
                         const float4** bloom_out, cudaStream_t s);
+// Surface shading (atm_shade.cu): the kernel's float32 arguments and the
+// quantities the reference forms from them once per frame, rounded on the host.
+struct ShadeParams {
+  float sun[3], E[3], right[3], up[3], fwd[3];  // global frame
+  int advanced;                                 // advanced ocean BRDF on
+  float roughness, f0, sky_strength;
+  float extinction[3];         // f32(absorption) + f32(scattering)
+  float scattering_albedo[3];  // scattering / max(extinction, 1e-6)
+  float max_depth, eta;        // eta = 1 / f32(refraction_index)
+  float strength, max_offset;  // refraction strength, max offset (pixels)
+  float solar_slope_variance;  // tanf(f32(sun angular radius))^2
+  float tanfov;
+  float four_pi;               // f32(4 pi)
+  int mode;                    // 0 lit, otherwise albedo
+  int32_t ocean_id;            // surface id of ocean pixels
+};
+// Images of one call: float images with the layout's channels per element,
+// scalar and id images with one value per element, all at the same element
+// strides.
+struct ShadeImages {
+  const float* position;
+  const float* normal;
+  const float* albedo;
+  const float* water_depth;
+  const float* seabed_albedo;
+  const float* seabed_normal;
+  const float* slope_variance;
+  const int32_t* surface_id;
+  const float* terrain_position;
+  const float* terrain_normal;
+  const float* terrain_albedo;
+  const int32_t* terrain_surface_id;
+  const float* sun_transmittance;
+  const float* sky_radiance;
+  float* surface_hdr;
+};
+cudaError_t launch_shade_surface(const ShadeParams& S, const ImageLayout& L, const ShadeImages& I, cudaStream_t s);
+
 // Whether x is the image's contiguous axis (the orientation of its bloom planes).
 bool image_x_fast(const ImageLayout& L);
 // A bloom plane of orientation Q.x_fast copied into dst as float4 [y][x].

@@ -175,6 +175,40 @@ ATM_SURROGATE_SKY = 0
 ATM_SURROGATE_AERIAL = 1
 
 
+class AtmShadeParams(ctypes.Structure):
+    _fields_ = [
+        ("sun_global", c_double3),
+        ("solar_irradiance", c_double3),
+        ("view_right_global", c_double3),
+        ("view_up_global", c_double3),
+        ("view_forward_global", c_double3),
+        ("advanced_ocean_enabled", ctypes.c_int32),
+        ("mode", ctypes.c_int32),
+        ("ocean_roughness", ctypes.c_double),
+        ("ocean_f0", ctypes.c_double),
+        ("ocean_sky_strength", ctypes.c_double),
+        ("ocean_absorption", c_double3),
+        ("ocean_scattering", c_double3),
+        ("ocean_max_depth", ctypes.c_double),
+        ("ocean_refraction_index", ctypes.c_double),
+        ("ocean_refraction_strength", ctypes.c_double),
+        ("ocean_refraction_max_offset_pixels", ctypes.c_double),
+        ("sun_angular_radius", ctypes.c_double),
+        ("tangent_half_fov", ctypes.c_double),
+        ("ocean_surface_id", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+SHADE_IMAGES = ("position", "normal", "albedo", "water_depth", "seabed_albedo", "seabed_normal", "slope_variance",
+                "surface_id", "terrain_position", "terrain_normal", "terrain_albedo", "terrain_surface_id",
+                "sun_transmittance", "sky_radiance", "surface_hdr")
+
+
+class AtmShadeImages(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in SHADE_IMAGES]
+
+
 class AtmPostConfig(ctypes.Structure):
     _fields_ = [
         ("exposure_ev", ctypes.c_double),
@@ -244,6 +278,8 @@ SIGNATURES = {
     "atm_post_destroy": (ctypes.c_int, [_P]),
     "atm_post_process": (ctypes.c_int, [_P, _P, _P, ctypes.POINTER(AtmImage), _D, _I32, _I32, _P]),
     "atm_post_read_bloom": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P, _P]),
+    "atm_shade_surface": (ctypes.c_int, [ctypes.POINTER(AtmShadeParams), ctypes.POINTER(AtmShadeImages),
+                                         ctypes.POINTER(AtmImage), _P]),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,
