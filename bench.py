@@ -412,6 +412,9 @@ def main() -> None:
     parser.add_argument("--no-mlp", action="store_true", help="skip the surrogate frame (training + timing)")
     parser.add_argument("--mlp-epochs", type=int, default=400, help="surrogate training epochs (2^22 samples)")
     parser.add_argument("--no-post", action="store_true", help="skip the 4K display post-process timing")
+    parser.add_argument("--mlp-sweep", type=int, default=0,
+                        help="also run the aerial-surrogate frame workload over this many 4K frames with cameras "
+                             "log-uniform 1 m - 4000 km (e.g. 64)")
     args = parser.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -760,11 +763,91 @@ def _frame_4k(device, args) -> dict:
                      "steps_per_network": reports["sky"].steps,
                      "held_out": {name: rep.held_out for name, rep in reports.items()}},
         "networks": "aerial 11->4x64->6 (one for cameras inside the shell, one above it), sky 10->3x64->3; SiLU; "
-                    "BF16 mma.sync m16n8k16 with FP32 accumulation",
+                    "BF16 operands on tcgen05 with FP32 accumulators in tensor memory",
     })
-    del graphs, r, frames
+    if args.mlp_sweep:
+        del graphs
+        out["sweep"] = _mlp_sweep(r, cfg, sg, args.mlp_sweep, device)
+    else:
+        del graphs
+    del r, frames
     torch.cuda.empty_cache()
     return out
+
+
+def _mlp_sweep(r, cfg, sg, n_frames, device, n_pixels=300) -> dict:
+    """The aerial-surrogate frame workload as configured: n_frames frames of
+    the fBm G-buffer at the renderer's size with cameras log-uniform 1 m -
+    4000 km (surrogate_sweep_cameras).  Per frame the plain and the surrogate
+    chain are timed with CUDA events after one untimed call each (which also
+    rebuilds the camera's sky-view LUT), and both images are compared with the
+    FP64 oracle at n_pixels random pixels."""
+
+    import numpy as np
+    import torch
+
+    from oracle.atm import Oracle
+    from planet_renderer_gb300.atmosphere import scene
+    from planet_renderer_gb300.atmosphere.surrogate import stats_summary
+    from planet_renderer_gb300.atmosphere.workloads import (EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG,
+                                                            surrogate_sweep_cameras)
+    from planet_renderer_gb300.lighting import LightingState
+
+    o = Oracle("f64")
+    ar = math.radians(SUN_ANGULAR_RADIUS_DEG)
+    tl = o.build_transmittance(cfg, EARTH_RADIUS_M)
+    ms = o.build_multi_scattering(cfg, EARTH_RADIUS_M, SOLAR_IRRADIANCE, ar, tl)
+    ap = np.zeros((cfg.aerial_lut_width, cfg.aerial_lut_height, cfg.aerial_lut_depth, 3))
+    W, H = r.width, r.height
+    rng = np.random.default_rng(SEED + 1)
+    stats = torch.zeros(8, dtype=torch.float32, device=device)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    totals = {"plain": 0.0, "mlp": 0.0}
+    errors = {"plain": [], "mlp": []}
+    cameras = []
+    for v in surrogate_sweep_cameras(SEED, n_frames):
+        gb = scene.synthesize_gbuffer(W, H, EARTH_RADIUS_M, v.altitude_m, v.basis, v.tangent_half_fov, v.sun_local,
+                                      SOLAR_IRRADIANCE, seed=SEED, device=device)
+        gb["hdr"] = torch.zeros_like(gb["scene_hdr"])
+        light = LightingState(v.sun_local, SUN_ANGULAR_RADIUS_DEG, SOLAR_IRRADIANCE)
+        pix = np.stack([rng.integers(0, W, n_pixels), rng.integers(0, H, n_pixels)], 1)
+        px, py = torch.as_tensor(pix[:, 0], device=device), torch.as_tensor(pix[:, 1], device=device)
+        values, ms_cam = {}, {}
+        runs = (("plain", lambda: _chain(r, v, gb, light)),
+                ("mlp", lambda: _chain_surrogate(r, v, gb, light, sg, stats)))
+        for name, fn in runs:
+            fn()
+            torch.cuda.synchronize(device)
+            start.record()
+            fn()
+            end.record()
+            torch.cuda.synchronize(device)
+            ms_cam[name] = start.elapsed_time(end)
+            totals[name] += ms_cam[name]
+            values[name] = gb["hdr"][px, py].cpu().numpy().astype(np.float64)
+        alt = v.altitude_m
+        sv = o.build_sky_view(cfg, EARTH_RADIUS_M, alt, float(v.sun_local[1]), SOLAR_IRRADIANCE, ar, tl, ms)
+        full = {k: gb[k].cpu().numpy().astype(np.float64) for k in ("scene_hdr", "space_hdr", "position_view")}
+        sid = gb["surface_id"].cpu().numpy()
+        plist = (pix[:, 0].astype(np.int64) * H + pix[:, 1]).astype(np.int32)
+        hdr, _ = o.composite(cfg, full["scene_hdr"], full["space_hdr"], sid, full["position_view"], EARTH_RADIUS_M,
+                             alt, alt, v.sun_local, SOLAR_IRRADIANCE, light.sun_disk_radiance, ar, v.basis,
+                             v.tangent_half_fov, 4.0, 12.0, 0, tl, ms, sv, ap, pixel_list=plist)
+        ref = hdr[pix[:, 0], pix[:, 1]]
+        floor = 1e-4 * np.abs(ref).max()
+        cam = {"altitude_m": alt, "sun_zenith_deg": v.sun_zenith_deg, **{f"{k}_ms": t for k, t in ms_cam.items()}}
+        for name, got in values.items():
+            e = np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor), axis=1)
+            errors[name].append(e)
+            cam[f"{name}_error_mean"] = float(e.mean())
+        cameras.append(cam)
+        del gb, full
+    error = {name: {"mean": float(np.concatenate(es).mean()), "p99": float(np.quantile(np.concatenate(es), 0.99))}
+             for name, es in errors.items()}
+    return {"frames": n_frames, "width": W, "height": H, "pixels_per_frame": n_pixels,
+            "plain_ms_mean": totals["plain"] / n_frames, "mlp_ms_mean": totals["mlp"] / n_frames,
+            "speedup": totals["plain"] / totals["mlp"], "error_vs_fp64": error, "gate": stats_summary(stats),
+            "cameras": cameras}
 
 
 if __name__ == "__main__":

@@ -61,6 +61,18 @@ def frame_chain_cameras(seed: int = 2027) -> list[CameraView]:
     return views
 
 
+def surrogate_sweep_cameras(seed: int = 2027, frames: int = 64) -> list[CameraView]:
+    """Cameras of the aerial-surrogate frame workload: altitude log-uniform
+    1 m - 4000 km, sun zenith uniform 0-100 deg, sun azimuth uniform, the
+    frame chain's pitch and field of view.  Seeded."""
+
+    rng = np.random.default_rng(seed)
+    altitude = np.exp(rng.uniform(np.log(1.0), np.log(4.0e6), frames))
+    zenith = rng.uniform(0.0, 100.0, frames)
+    azimuth = rng.uniform(0.0, 360.0, frames)
+    return [CameraView(float(a), float(z), float(b)) for a, z, b in zip(altitude, zenith, azimuth)]
+
+
 # ---- batched LUT builds ----------------------------------------------------
 SKY_VIEW_SIZES = ((96, 54), (128, 72), (192, 108), (256, 144), (384, 216))
 AERIAL_SIDES = (16, 24, 32, 48, 64)
