@@ -108,3 +108,32 @@ def test_c_abi_rejects_what_the_reference_rejects(field, value):
     assert field in lib.atm_last_error().decode()
     cfg = _native.AtmPostConfig(0.0, 1.0, 0.5, 8.0, 0.08, 4)
     assert lib.atm_post_create(ctypes.byref(cfg), 0, 32, ctypes.byref(out)) == _native.ATM_E_INVALID
+
+
+def test_c_abi_shading_rejects_bad_arguments():
+    """atm_shade_surface validates before it touches the GPU."""
+
+    from planet_renderer_gb300 import _native
+
+    lib = _native.library()
+    params = _native.AtmShadeParams()
+    images = _native.AtmShadeImages()
+    image = _native.AtmImage(16, 8, 8, 1, 3)
+    assert lib.atm_shade_surface(None, ctypes.byref(images), ctypes.byref(image), None) == _native.ATM_E_INVALID
+    # every image pointer is required
+    assert lib.atm_shade_surface(ctypes.byref(params), ctypes.byref(images), ctypes.byref(image),
+                                 None) == _native.ATM_E_INVALID
+    assert "null image pointer" in lib.atm_last_error().decode()
+    bad = _native.AtmImage(16, 8, 8, 1, 5)  # rejected before any pointer is looked at
+    assert lib.atm_shade_surface(ctypes.byref(params), ctypes.byref(images), ctypes.byref(bad),
+                                 None) == _native.ATM_E_INVALID
+    assert "channels" in lib.atm_last_error().decode()
+
+
+def test_c_abi_post_process_rejects_null_handles():
+    from planet_renderer_gb300 import _native
+
+    lib = _native.library()
+    image = _native.AtmImage(16, 8, 8, 1, 3)
+    assert lib.atm_post_process(None, None, None, ctypes.byref(image), 0.0, 1, 1, None) == _native.ATM_E_INVALID
+    assert lib.atm_post_read_bloom(None, None, None, None) == _native.ATM_E_INVALID
