@@ -3,9 +3,10 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-Workload (one "step"): the plain per-frame chain of the reference's frame
-scheduler (atmosphere/renderer.py update -> prepare_frame -> composite) at
-1920x1080 FP32 for the three cameras of ``workloads.frame_chain_cameras``
+Workload (one "step": 16 passes over the three cameras): the plain
+per-frame chain of the reference's frame scheduler (atmosphere/renderer.py
+update -> prepare_frame -> composite) at 1920x1080 FP32 for the three
+cameras of ``workloads.frame_chain_cameras``
 (2 km, 50 km, 2000 km altitude; pitch -35 deg; stratified sun zeniths in
 [0, 100] deg; seed 2027) on a seeded fBm G-buffer (+/- 4 km).  Per camera the
 chain is: sky-view LUT rebuild (a moving camera changes its key every frame),
@@ -58,6 +59,11 @@ COMPOSITE_FLOP_PER_SAMPLE = 406.16
 # scene 12 + space 12 read, hdr 12 written (LUTs stay in L2).
 COMPOSITE_BYTES_PER_PIXEL = 52
 MLP_CHECK_FRACTION = 0.01  # share of MLP pixels the plain path re-integrates
+# A step is this many passes of the three cameras' chains (48 frames of
+# 1080p, ~57 ms): with the usual 20 timed steps the timed region lasts over a
+# second.  Every pass redoes the whole chain (sky-view rebuild, surface
+# lighting, aerial volume, composite) on inputs larger than L2.
+PASSES_PER_STEP = 16
 SMS, FP32_LANES = 152, 128
 
 
@@ -386,7 +392,7 @@ def _config_block(extra=None) -> dict:
         "workload": "plain per-frame chain (sky-view rebuild + surface lighting + aerial volume + composite), "
                     "1920x1080 FP32, 3 cameras (2 km / 50 km / 2000 km, pitch -35 deg, stratified sun zenith "
                     "0-100 deg), seeded fBm G-buffer +/-4 km, CUDA graph per camera",
-        "width": WIDTH, "height": HEIGHT, "cameras": 3, "seed": SEED,
+        "width": WIDTH, "height": HEIGHT, "cameras": 3, "passes_per_step": PASSES_PER_STEP, "seed": SEED,
         "params": "Earth: R 6360 km, top 100 km, Mie ext 8.396e-6; T 256x64/40, MS 32x32 64 dirs x 20 steps, "
                   "SV 192x108/30, AP 32x32x32 x2, 48 limb intervals, 8 terminator substeps",
         "l2": "inputs larger than L2 (3 cameras x 108 MB of G-buffer + hdr per step)",
@@ -399,7 +405,8 @@ def _config_block(extra=None) -> dict:
 def main() -> None:
     parser = argparse.ArgumentParser()
     parser.add_argument("--gpus", type=int, default=1)
-    parser.add_argument("--steps", type=int, default=100)
+    parser.add_argument("--steps", type=int, default=20,
+                        help=f"timed steps of {PASSES_PER_STEP} passes of the 3-camera 1080p chain each")
     parser.add_argument("--warmup", type=int, default=5)
     parser.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     parser.add_argument("--cpu-stride", type=int, default=1,
@@ -412,6 +419,7 @@ def main() -> None:
     parser.add_argument("--no-mlp", action="store_true", help="skip the surrogate frame (training + timing)")
     parser.add_argument("--mlp-epochs", type=int, default=400, help="surrogate training epochs (2^22 samples)")
     parser.add_argument("--no-post", action="store_true", help="skip the 4K display post-process timing")
+    parser.add_argument("--no-luts", action="store_true", help="skip the plain LUT-build timing")
     parser.add_argument("--mlp-sweep", type=int, default=0,
                         help="also run the aerial-surrogate frame workload over this many 4K frames with cameras "
                              "log-uniform 1 m - 4000 km (e.g. 64)")
@@ -436,8 +444,8 @@ def main() -> None:
     r.radiance_samples(reset=True)
     for g in graphs:
         g.replay()
-    samples_per_step = r.radiance_samples(reset=True)
-    for _ in range(args.warmup):
+    samples_per_step = PASSES_PER_STEP * r.radiance_samples(reset=True)
+    for _ in range(args.warmup * PASSES_PER_STEP):
         for g in graphs:
             g.replay()
     torch.cuda.synchronize(device)
@@ -445,7 +453,7 @@ def main() -> None:
     if world > 1:
         dist.barrier()
     sampler.start()
-    ms_total = _timed_graph_region(graphs, args.steps, device)
+    ms_total = _timed_graph_region(graphs, args.steps * PASSES_PER_STEP, device)
     clocks = sampler.stop()
     if world > 1:
         dist.barrier()
@@ -474,9 +482,10 @@ def main() -> None:
     comp_bytes = WIDTH * HEIGHT * COMPOSITE_BYTES_PER_PIXEL
     achieved_gbs = comp_bytes / (statistics.mean(comp_ms) / 1e3) / 1e9
 
-    e2e_s, e2e_samples, h2d, d2h = _e2e(r, frames, max(args.steps // 4, 5), 2, device)
-    e2e_steps = max(args.steps // 4, 5)
+    e2e_steps = 100
+    e2e_s, e2e_samples, h2d, d2h = _e2e(r, frames, e2e_steps, 2, device)
 
+    luts = None if args.no_luts else _lut_builds(device, args)
     frame_4k = None
     if not args.no_4k:
         frame_4k = _frame_4k(device, args)
@@ -501,7 +510,8 @@ def main() -> None:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": _config_block(),
-            "frame_ms_1080p": ms_per_step / 3.0,
+            "frame_ms_1080p": ms_per_step / (3.0 * PASSES_PER_STEP),
+            "lut_build": luts,
             "frame_ms_4k": frame_4k,
             "batch": batch,
             "postprocess_4k": post,
@@ -510,7 +520,7 @@ def main() -> None:
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / e2e_steps,
                     "path": "AtmosphereRenderer.update/prepare_frame/composite, pinned host buffers, "
                             "uploads/read-backs on a copy stream overlapping the other cameras' kernels"},
-            "gpu_launches": 12 * args.steps,
+            "gpu_launches": 12 * PASSES_PER_STEP * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                          "frac": achieved_tflops / peak_tflops, "traffic": None, "kernel": "k_composite",
                          "peak_source": f"derived: {SMS} SMs x {FP32_LANES} FP32 lanes x 2 x median SM clock "
@@ -525,9 +535,40 @@ def main() -> None:
             "cpu_baseline": cpu,
             "clocks": clocks,
         }
+        line.update(_summary(frame_4k, luts, ms_total / 1e3))
         print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def _summary(frame_4k, luts, timed_s) -> dict:
+    """Short top-level keys that close the line: the surrogate's headline
+    (4K frames of the three cameras; the 64-frame sweep when it ran) and the
+    LUT build, next to the length of the timed region."""
+
+    out = {"timed_region_s": timed_s}
+    if luts:
+        out["lut_build_us"] = {k: round(luts[k]["us"], 2) for k in ("transmittance", "multi_scattering",
+                                                                     "sky_view", "aerial")}
+    if frame_4k:
+        out["plain_4k_ms"] = frame_4k["plain_ms"]
+        if frame_4k.get("mlp_ms"):
+            err = frame_4k["error_vs_fp64"]
+            out.update({
+                "mlp_4k_ms": frame_4k["mlp_ms"], "mlp_4k_speedup": frame_4k["speedup"],
+                "mlp_4k_err_mean": err["all"]["mlp"]["mean"], "mlp_4k_err_p99": err["all"]["mlp"]["p99"],
+                "mlp_4k_err_worst_camera": max(c["mlp"]["mean"] for c in err["cameras"]),
+                "plain_4k_err_mean": err["all"]["plain"]["mean"],
+            })
+        sweep = frame_4k.get("sweep")
+        if sweep:
+            out.update({
+                "sweep_frames": sweep["frames"], "sweep_speedup": sweep["speedup"],
+                "sweep_err_mean": sweep["error_vs_fp64"]["mlp"]["mean"],
+                "sweep_err_p99": sweep["error_vs_fp64"]["mlp"]["p99"],
+                "sweep_err_worst_frame": max(c["mlp_error_mean"] for c in sweep["cameras"]),
+            })
+    return out
 
 
 def _composite_args(v, light):
@@ -538,6 +579,57 @@ def _composite_args(v, light):
 
 
 POST_BYTES_PER_PIXEL = 36  # float3 HDR read by the extract and by the resolve, float3 display written
+
+
+def _lut_builds(device, args) -> dict:
+    """The plain LUT build (Earth parameters, FP32): each of the four LUT
+    kernels at its configured size for a camera at 2 km with the sun at
+    45 deg zenith, timed alone with CUDA events over repeated launches.
+    Samples are the analytic counts of each build (texels x steps; the
+    multi-scattering build: texels x directions x steps)."""
+
+    import torch
+
+    from planet_renderer_gb300 import camera
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.workloads import EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG
+
+    cfg = earth_baseline()
+    r = AtmosphereRenderer(WIDTH, HEIGHT, cfg, device=device)
+    sun = camera.sun_from_zenith(45.0, 0.0)
+    kw = dict(planet_radius_m=EARTH_RADIUS_M, camera_altitude_m=2000.0, sun_zenith_cosine=float(sun[1]),
+              sun_local=sun, solar_irradiance=SOLAR_IRRADIANCE, sun_angular_radius_degrees=SUN_ANGULAR_RADIUS_DEG,
+              view_basis=camera.view_basis(0.0, -35.0), tangent_half_fov=camera.tangent_half_fov(60.0))
+    counts = {
+        "transmittance": cfg.transmittance_lut_width * cfg.transmittance_lut_height * cfg.transmittance_steps,
+        "multi_scattering": cfg.multi_scattering_lut_width * cfg.multi_scattering_lut_height
+                            * cfg.multi_scattering_directions * cfg.multi_scattering_steps,
+        "sky_view": cfg.sky_view_lut_width * cfg.sky_view_lut_height * cfg.sky_view_steps,
+        "aerial": cfg.aerial_lut_width * cfg.aerial_lut_height * cfg.aerial_lut_depth * cfg.aerial_steps_per_slice,
+    }
+    reps = 200
+    out = {"workload": "plain LUT build, Earth (Mie ext 8.396e-6), camera 2 km, sun zenith 45 deg: T 256x64/40, "
+                       "MS 32x32 x 64 dirs x 20, SV 192x108/30, AP 32^3 x 2; each kernel launched alone "
+                       f"{reps} times (LUTs stay in L2)"}
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    total_us = 0.0
+    for kind in ("transmittance", "multi_scattering", "sky_view", "aerial"):
+        for _ in range(max(args.warmup, 3)):
+            r.build_lut(kind, **kw)
+        torch.cuda.synchronize(device)
+        start.record()
+        for _ in range(reps):
+            r.build_lut(kind, **kw)
+        end.record()
+        torch.cuda.synchronize(device)
+        us = start.elapsed_time(end) * 1e3 / reps
+        total_us += us
+        out[kind] = {"us": us, "samples": counts[kind], "samples_per_s": counts[kind] / (us * 1e-6)}
+    out["all_four_us"] = total_us
+    out["samples_per_s"] = sum(counts.values()) / (total_us * 1e-6)
+    r.close()
+    return out
 
 
 def _postprocess_4k(device, args) -> dict:
@@ -558,7 +650,7 @@ def _postprocess_4k(device, args) -> dict:
     pp = PostProcessor(width, height, config, device=device)
     for i in range(args.warmup):
         pp.process(hdrs[i % 2], display, 0.0, bloom=True, tone_map=True)
-    steps = max(args.steps // 4, 10)
+    steps = 50
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(device)
     start.record()
@@ -604,7 +696,7 @@ def _batch(device, args) -> dict:
         builder.build(jobs, tuning, arena=arena, prepared=prepared)
     torch.cuda.synchronize(device)
     builder.samples(reset=True)
-    steps = max(args.steps // 10, 3)
+    steps = 5
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record()
     for _ in range(steps):
@@ -725,7 +817,7 @@ def _frame_4k(device, args) -> dict:
     for _ in range(3):
         for g in graphs:
             g.replay()
-    steps = max(args.steps // 10, 5)
+    steps = 20
     plain_ms = _timed_graph_region(graphs, steps, device) / steps / 3.0
     plain_imgs = []
     for v, gb, light in frames:

@@ -360,12 +360,17 @@ typedef struct AtmSurrogate {
                             sky pixels read the sky-view LUT (e.g. 0.1)       */
   double limb_degrees;   /* gate: view ray within this of the limb (e.g. 0.5) */
   uint32_t seed;         /* picks the checked pixels                            */
-  uint32_t reserved;
+  int32_t tc_wait_polls; /* bound of each tensor-core completion wait, in
+                            mbarrier polls: 0 = the library's bound (2^20
+                            polls, far beyond any MMA's latency); -1 = no
+                            poll, every wait gives up at once (exercises the
+                            timeout path: every MLP pixel then takes the plain
+                            path); other values as given                       */
   float* stats;          /* device float[8] accumulated into, or null: checked
                             pixels, sum and max of their relative error, gated
                             surface pixels, MLP surface pixels, MLP sky pixels,
-                            sky-view-LUT sky pixels, blocks whose tensor-core
-                            MMA did not complete in time (0)                    */
+                            sky-view-LUT sky pixels, 128-pixel tiles whose
+                            tensor-core MMA did not complete in time (0)       */
 } AtmSurrogate;
 
 /* COMPOSITE view of atm_composite with the per-pixel limb integrator replaced
@@ -379,8 +384,11 @@ typedef struct AtmSurrogate {
  * segment's start, middle or end; for sky pixels the camera's sun cosine
  * below sky_twilight_cosine or the camera above the shell), and re-integrates
  * check_fraction of the MLP pixels, whose error goes to stats; those pixels
- * keep the plain result.  Allocates the handle's fallback queue (4 bytes a
- * pixel) on first use; stream-ordered and capturable afterwards. */
+ * keep the plain result.  A 128-pixel tile whose tensor-core MMA does not
+ * complete within the wait bound gives its MLP pixels to the plain path (the
+ * frame stays correct) and sets the handle's timeout flag, which atm_check
+ * reports.  Allocates the handle's fallback queue (4 bytes a pixel) on first
+ * use; stream-ordered and capturable afterwards. */
 int atm_composite_surrogate(AtmHandle* handle, const float* scene_hdr, const float* space_hdr,
                             const int32_t* surface_id, const float* position_view, float* hdr, const AtmImage* image,
                             double planet_radius_m, double camera_radius_m, const double sun_local[3],
@@ -388,6 +396,13 @@ int atm_composite_surrogate(AtmHandle* handle, const float* scene_hdr, const flo
                             double sun_angular_radius_degrees, const double view_basis[9], double tangent_half_fov,
                             double star_contrast_start, double star_contrast_end, const AtmSurrogate* surrogate,
                             void* stream);
+
+/* Synchronises `stream` and reports, then clears, the device-side errors of
+ * the handle's earlier stream-ordered calls: ATM_E_TIMEOUT when a
+ * tensor-core wait of atm_composite_surrogate gave up since the last check
+ * (those pixels took the plain path), ATM_OK otherwise.  No counterpart in
+ * the reference, whose kernels have no bounded waits. */
+int atm_check(AtmHandle* handle, void* stream);
 
 /* COMPOSITE view of atm_composite that allocates nothing.  No counterpart in
  * the reference.  For callers that may not call cudaMalloc: an engine or

@@ -166,7 +166,8 @@ struct AtmHandle {
   double sky_key[6] = {};  // altitude, sun cosine, E[3], angular radius
   bool aerial_available = false;
   AtmState state{};
-  // surrogate composite: fallback queue (width * height entries + 2 counters)
+  // surrogate composite: fallback queue (4 header words: entries, ticket,
+  // timeout flag, padding; then width * height entries)
   uint32_t* queue = nullptr;
   int sm_count = 0;
 };
@@ -521,6 +522,21 @@ ATM_API int atm_read_sample_counter(AtmHandle* h, int32_t reset, uint64_t* out, 
   ATM_CUDA(cudaStreamSynchronize(s), "sample counter sync");
   if (out) *out = v;
   return ATM_OK;
+}
+
+ATM_API int atm_check(AtmHandle* h, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ATM_CUDA(cudaStreamSynchronize(s), "check");
+  if (!h->queue) return ATM_OK;
+  uint32_t status = 0;
+  ATM_CUDA(cudaMemcpy(&status, h->queue + 2, sizeof(status), cudaMemcpyDeviceToHost), "check");
+  if (status == 0) return ATM_OK;
+  ATM_CUDA(cudaMemset(h->queue + 2, 0, sizeof(status)), "check");
+  return fail(ATM_E_TIMEOUT,
+              "a tensor-core MMA of atm_composite_surrogate did not complete within its wait bound; the "
+              "affected pixels took the plain integrator");
 }
 
 // ---- batched builds ------------------------------------------------------
@@ -1017,16 +1033,20 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
   nets.floor = float(sg->aerial_floor);
   nets.floor_t = float(sg->aerial_floor_t);
   nets.sky_floor = float(sg->sky_floor);
+  if (sg->tc_wait_polls < -1) return fail(ATM_E_INVALID, "tc_wait_polls must be -1, 0 or positive");
+  nets.wait_tries = sg->tc_wait_polls == 0 ? atm::kTcWaitTries : sg->tc_wait_polls < 0 ? 0 : sg->tc_wait_polls;
   if (!h->queue) {
     const size_t cap = size_t(h->width) * size_t(h->height);
-    ATM_CUDA(cudaMalloc(&h->queue, (cap + 2) * sizeof(uint32_t)), "fallback queue");
+    ATM_CUDA(cudaMalloc(&h->queue, (cap + 4) * sizeof(uint32_t)), "fallback queue");
+    ATM_CUDA(cudaMemset(h->queue, 0, 4 * sizeof(uint32_t)), "fallback queue");
     int dev = 0;
     ATM_CUDA(cudaGetDevice(&dev), "device query");
     ATM_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev), "device query");
   }
   atm::SurrogateQueue Q{};
   Q.count = h->queue;
-  Q.items = h->queue + 2;
+  Q.status = h->queue + 2;
+  Q.items = h->queue + 4;
   Q.stats = sg->stats;
   Q.check_fraction = float(sg->check_fraction);
   Q.seed = sg->seed;
@@ -1063,6 +1083,9 @@ ATM_API int atm_composite_noalloc(const AtmParams* params, const void* transmitt
   if (image->width < 1 || image->height < 1 || image->stride_x <= 0 || image->stride_y <= 0 ||
       (image->channels != 3 && image->channels != 4))
     return fail(ATM_E_INVALID, "invalid AtmImage");
+  if (image->width > 16384 || image->height > 16384)
+    return fail(ATM_E_INVALID, "frame %dx%d: width and height are limited to 16384, as for atm_create",
+                image->width, image->height);
   const long long tiles = (long long)((image->width + 15) / 16) * ((image->height + 15) / 16);
   if (tiles > atm::noalloc_max_tiles())
     return fail(ATM_E_INVALID,
@@ -1073,7 +1096,8 @@ ATM_API int atm_composite_noalloc(const AtmParams* params, const void* transmitt
       tangent_half_fov <= 0.0 || !std::isfinite(planet_radius_m) || !std::isfinite(camera_radius_m))
     return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
   uint32_t* scratch = nullptr;
-  ATM_CUDA(atm::noalloc_tile_scratch(&scratch), "no-allocation scratch set-up (cudaGetSymbolAddress)");
+  ATM_CUDA(atm::noalloc_tile_scratch(&scratch, static_cast<cudaStream_t>(stream)),
+           "no-allocation scratch set-up (cudaGetSymbolAddress; make the first call on a device before any capture)");
   const double alt = std::fmax(camera_radius_m - planet_radius_m, 0.0);
   atm::CompositeScalars A{};
   A.bottom = float(planet_radius_m);

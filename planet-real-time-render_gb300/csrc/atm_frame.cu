@@ -70,6 +70,38 @@ __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayou
   out_sky[o + 2] = sky.z;
 }
 
+// One pixel of the COMPOSITE view (:1860-1940): writes hdr and adds the
+// pixel's radiance samples to `samples`.  Shared by the composite and its
+// no-allocation variant so that the two cannot drift apart.
+__device__ __forceinline__ void composite_pixel(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                                                const float* __restrict__ scene, const float* __restrict__ space,
+                                                const int32_t* __restrict__ sid, const float* __restrict__ pos,
+                                                const float4* __restrict__ tlut, const float4* __restrict__ mslut,
+                                                const float4* __restrict__ svlut, float* __restrict__ hdr, int x,
+                                                int y, uint32_t& samples) {
+  const size_t e = pix_offset(L, x, y);
+  const size_t o = e * L.channels;
+  Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+  PixelRay pr = pixel_ray(L, A, x, y);
+  f3 color = ld3(scene + o);
+  if (sid[e] >= 0) {
+    const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
+    float sd = norm(ld3(pos + o));
+    float start, end;
+    if (surface_interval(P, G, A.bottom, sd, start, end)) {
+      f3 scat = integrate_surface(P, F, G, pr.ray, start, end, samples);
+      f3 tr = surface_segment_t(P, F, G, pr.ray, start, end);
+      color = scat + color * tr;
+    }
+  } else {
+    color = composite_sky(P, F, A, svlut, pr.ray, color, ld3(space + o), float(L.height));
+  }
+  color = vmax(color, 0.0f);
+  hdr[o + 0] = color.x;
+  hdr[o + 1] = color.y;
+  hdr[o + 2] = color.z;
+}
+
 // COMPOSITE view (:1860-1940): the per-frame path.
 __global__ void __launch_bounds__(256, 3) k_composite(DevParams P, ImageLayout L, CompositeScalars A,
                                                    const float* __restrict__ scene, const float* __restrict__ space,
@@ -78,31 +110,8 @@ __global__ void __launch_bounds__(256, 3) k_composite(DevParams P, ImageLayout L
                                                    const float4* __restrict__ svlut, float* __restrict__ hdr,
                                                    unsigned long long* counter) {
   int x, y;
-  const bool inside = tile_pixel(L, x, y);
   uint32_t samples = 0;
-  if (inside) {
-    const size_t e = pix_offset(L, x, y);
-    const size_t o = e * L.channels;
-    Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
-    PixelRay pr = pixel_ray(L, A, x, y);
-    f3 color = ld3(scene + o);
-    if (sid[e] >= 0) {
-      const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
-      float sd = norm(ld3(pos + o));
-      float start, end;
-      if (surface_interval(P, G, A.bottom, sd, start, end)) {
-        f3 scat = integrate_surface(P, F, G, pr.ray, start, end, samples);
-        f3 tr = surface_segment_t(P, F, G, pr.ray, start, end);
-        color = scat + color * tr;
-      }
-    } else {
-      color = composite_sky(P, F, A, svlut, pr.ray, color, ld3(space + o), float(L.height));
-    }
-    color = vmax(color, 0.0f);
-    hdr[o + 0] = color.x;
-    hdr[o + 1] = color.y;
-    hdr[o + 2] = color.z;
-  }
+  if (tile_pixel(L, x, y)) composite_pixel(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, hdr, x, y, samples);
   warp_count(samples, counter);
 }
 
@@ -253,8 +262,9 @@ static __device__ __align__(256) uint32_t g_noalloc_tile_samples[kNoAllocMaxTile
 
 namespace {
 
-// COMPOSITE view of k_composite; the block's sample count goes to its tile
-// slot instead of an atomic counter (every launched block writes its slot).
+// COMPOSITE view of k_composite (the same composite_pixel); the block's
+// sample count goes to its tile slot instead of an atomic counter (every
+// launched block writes its slot).
 __global__ void __launch_bounds__(256, 3) k_composite_tiles(DevParams P, ImageLayout L, CompositeScalars A,
                                                          const float* __restrict__ scene,
                                                          const float* __restrict__ space,
@@ -266,31 +276,8 @@ __global__ void __launch_bounds__(256, 3) k_composite_tiles(DevParams P, ImageLa
                                                          uint32_t* __restrict__ tile_samples) {
   __shared__ uint32_t s_warp[8];
   int x, y;
-  const bool inside = tile_pixel(L, x, y);
   uint32_t samples = 0;
-  if (inside) {
-    const size_t e = pix_offset(L, x, y);
-    const size_t o = e * L.channels;
-    Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
-    PixelRay pr = pixel_ray(L, A, x, y);
-    f3 color = ld3(scene + o);
-    if (sid[e] >= 0) {
-      const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
-      float sd = norm(ld3(pos + o));
-      float start, end;
-      if (surface_interval(P, G, A.bottom, sd, start, end)) {
-        f3 scat = integrate_surface(P, F, G, pr.ray, start, end, samples);
-        f3 tr = surface_segment_t(P, F, G, pr.ray, start, end);
-        color = scat + color * tr;
-      }
-    } else {
-      color = composite_sky(P, F, A, svlut, pr.ray, color, ld3(space + o), float(L.height));
-    }
-    color = vmax(color, 0.0f);
-    hdr[o + 0] = color.x;
-    hdr[o + 1] = color.y;
-    hdr[o + 2] = color.z;
-  }
+  if (tile_pixel(L, x, y)) composite_pixel(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, hdr, x, y, samples);
   __syncwarp();
 #pragma unroll
   for (int k = 16; k > 0; k >>= 1) samples += __shfl_xor_sync(kFull, samples, k);
@@ -325,17 +312,26 @@ uint32_t* g_noalloc_address[kMaxDevices] = {};
 
 int noalloc_max_tiles() { return kNoAllocMaxTiles; }
 
-cudaError_t noalloc_tile_scratch(uint32_t** out) {
+// The array's device address on the current device.  Outside a stream
+// capture the address is looked up afresh (a device reset reloads the module
+// and may move the array); while `s` is capturing, the address of the last
+// lookup on this device is used, so the first call on a device must come
+// before any capture.
+cudaError_t noalloc_tile_scratch(uint32_t** out, cudaStream_t s) {
   int device = 0;
   cudaError_t e = cudaGetDevice(&device);
   if (e != cudaSuccess) return e;
   if (device < 0 || device >= kMaxDevices) return cudaErrorInvalidDevice;
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  const bool capturing = cudaStreamIsCapturing(s, &capture) != cudaSuccess || capture != cudaStreamCaptureStatusNone;
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (g_noalloc_address[device] == nullptr) {
+  if (!capturing) {
     void* address = nullptr;
     e = cudaGetSymbolAddress(&address, g_noalloc_tile_samples);  // with `device` current
     if (e != cudaSuccess) return e;
     g_noalloc_address[device] = static_cast<uint32_t*>(address);
+  } else if (g_noalloc_address[device] == nullptr) {
+    return cudaErrorStreamCaptureUnsupported;  // first call on this device inside a capture
   }
   *out = g_noalloc_address[device];
   return cudaSuccess;

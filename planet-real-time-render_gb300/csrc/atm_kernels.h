@@ -102,6 +102,10 @@ struct SurrogateSetDev {
   float bottom;
   float lhr_n, lhm_n;  // normalised log scale heights (features 4, 5)
 };
+// Bound of a tensor-core completion wait, in mbarrier polls (each try_wait
+// itself suspends for a bounded time): far beyond any MMA's latency.
+constexpr int kTcWaitTries = 1 << 20;
+
 struct SurrogateNets {
   const unsigned char* ap;   // packed BF16 aerial network (11 -> 4x64 -> 6) or null
   const unsigned char* sky;  // packed BF16 sky network (10 -> 3x64 -> 3) or null
@@ -112,6 +116,7 @@ struct SurrogateNets {
   float twilight_cos;        // gate: |sun cosine| at a surface segment below this -> plain path
   float sky_twilight_cos;    // gate: |sun cosine| at the camera below this -> sky-view LUT
   float limb_rad;            // gate: view ray within this of the limb -> plain path
+  int wait_tries;            // bound of each tensor-core completion wait (mbarrier polls)
 };
 // Pixels the surrogate composite hands to the plain integrator: entry =
 // kind << 30 | (y * width + x).  count and next are reset by each frame.
@@ -119,14 +124,17 @@ enum : uint32_t { kQueueSurface = 0u, kQueueSurfaceCheck = 1u, kQueueSkyCheck = 
 struct SurrogateQueue {
   uint32_t* items;    // capacity = width * height
   uint32_t* count;    // [0] = entries, [1] = fallback ticket
+  uint32_t* status;   // bit 0 set when a block's tensor-core MMA timed out;
+                      // kept across frames until the owner reads and clears it
   float* stats;       // null or kSurrogateStats floats, accumulated
   float check_fraction;
   uint32_t seed;
 };
 // stats: checked pixels, sum of their relative errors, max relative error,
 // gated surface pixels (plain integrator), MLP surface pixels, MLP sky
-// pixels, gated sky pixels (sky-view LUT), blocks whose tensor-core MMA timed
-// out (0 unless the hardware misbehaves)
+// pixels, gated sky pixels (sky-view LUT), 128-pixel tiles whose tensor-core
+// MMA timed out (their MLP pixels took the plain path; 0 unless the hardware
+// misbehaves or the wait bound is set to zero)
 constexpr int kSurrogateStats = 8;
 struct SampleShaping {
   float top_fraction;      // share of aerial segments starting at the shell top
@@ -148,7 +156,7 @@ cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L,
 // 16x16 tiles, and the COMPOSITE-view launch that uses it.
 constexpr int kMaxDevices = 64;
 int noalloc_max_tiles();
-cudaError_t noalloc_tile_scratch(uint32_t** out);
+cudaError_t noalloc_tile_scratch(uint32_t** out, cudaStream_t s);
 cudaError_t launch_composite_noalloc(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                      const float* scene, const float* space, const int32_t* sid, const float* pos,
                                      const float4* tlut, const float4* mslut, const float4* svlut, float* hdr,

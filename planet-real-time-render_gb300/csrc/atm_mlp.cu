@@ -340,13 +340,14 @@ __global__ void __launch_bounds__(128) k_mlp_forward_tc(MlpShape m, const unsign
     float x[16] = {}, y[8];
     if (r < n)
       for (int k = 0; k < m.n_in; ++k) x[k] = inputs[r * m.n_in + k];
-    ok = mlp_tile_tc<kHidden>(smw, m.n_in, T, x, y) && ok;
+    ok = mlp_tile_tc<kHidden>(smw, m.n_in, T, x, y);
+    if (!ok) break;  // block-uniform (one tile per block); no MMA is issued after it
     if (r < n)
       for (int k = 0; k < m.n_out; ++k) outputs[r * m.n_out + k] = y[k];
   }
-  if (!ok) atomicExch(error, 1);
+  if (!ok && threadIdx.x == 0) atomicExch(error, 1);
   // before the tensor memory is freed, no MMA of this CTA may be in flight:
-  // after a timed-out wait, wait once more (bounded) for the last commit
+  // after a timed-out wait, wait once more (bounded) for its one commit
   tc::fence_before_sync();
   if (__syncthreads_or(!ok)) tc::mbar_wait(&s_mbar, T.phase ^ 1u, kTcWaitTries);
   __syncthreads();

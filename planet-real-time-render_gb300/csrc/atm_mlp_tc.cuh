@@ -10,6 +10,7 @@
 
 #include <cstdint>
 
+#include "atm_kernels.h"
 #include "atm_mlp_tile.cuh"
 #include "atm_tc.cuh"
 
@@ -32,7 +33,6 @@ __host__ __device__ inline int tc_w_offset(int n, int k, int n_pad) {
 
 constexpr uint32_t kTcLbo = 128;  // K-adjacent core matrices
 constexpr uint32_t kTcSbo = 256;  // N-adjacent core matrices
-constexpr int kTcWaitTries = 1 << 20;
 
 // Per-tile state of a network run.
 struct TcTile {
@@ -47,14 +47,16 @@ struct TcTile {
 // Runs the network (n_in <= 16 inputs, kHidden layers of 64, n_out <= 8) for
 // the tile's 128 rows; every thread of the tile calls with its row's inputs
 // (unused ones zero) and receives its row's outputs.  w: generic pointer to the packed network
-// in shared memory.  Returns false if an MMA did not complete in time (the
-// outputs are then not valid).
+// in shared memory.  Each completion wait polls the mbarrier at most
+// wait_tries times.  Returns false, in every thread of the tile, if a layer's
+// MMAs did not complete in time: the outputs are then not valid, no further
+// MMA was issued, and exactly one commit (parity T.phase ^ 1) may still be
+// in flight - the caller waits for it before it frees the tensor memory.
 template <int kHidden>
 __device__ __forceinline__ bool mlp_tile_tc(const unsigned char* w, int n_in, TcTile& T, const float (&x)[16],
-                                            float (&y)[8]) {
+                                            float (&y)[8], int wait_tries = kTcWaitTries) {
   const uint32_t lane_off = uint32_t(T.row & ~31) << 16;  // the warp's quarter of the lanes
   const bool issuer = T.row == 0;
-  bool ok = true;
   // inputs -> A columns 0..7 (K = 16, BF16 pairs)
   {
     uint32_t v[8];
@@ -84,8 +86,9 @@ __device__ __forceinline__ bool mlp_tile_tc(const unsigned char* w, int n_in, Tc
       }
       tc::commit(T.mbar);
     }
-    ok = tc::mbar_wait(T.mbar, T.phase, kTcWaitTries) && ok;
+    const bool done = tc::tile_all(T.tile, tc::mbar_wait(T.mbar, T.phase, wait_tries));
     T.phase ^= 1u;
+    if (!done) return false;  // tile-uniform: stop issuing, leave tensor memory alone
     tc::fence_after_sync();
     if (!last) {
       // SiLU epilogue: D (64 FP32 columns) -> A (32 columns of BF16 pairs)
@@ -113,7 +116,7 @@ __device__ __forceinline__ bool mlp_tile_tc(const unsigned char* w, int n_in, Tc
   // every lane has read D before the next tile's MMAs overwrite it
   tc::fence_before_sync();
   tc::tile_sync(T.tile);
-  return ok;
+  return true;
 }
 
 }  // namespace atm

@@ -293,28 +293,37 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
   }
 
   // the networks on the tensor cores, each run by the whole block when any
-  // of its pixels needs it (block-uniform: every barrier stays convergent)
+  // of its pixels needs it (block-uniform: every barrier stays convergent).
+  // tc_ok is uniform over a tile; a tile whose wait timed out issues nothing
+  // more and its MLP pixels take the plain path below.
   float yv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   bool tc_ok = true;
   if (__syncthreads_or(kind == kSurfMlp)) {
     float t[8];
-    tc_ok = mlp_tile_tc<kSurrogateApHidden>(smem, kSurrogateApIn, T, fx, t) && tc_ok;
+    tc_ok = mlp_tile_tc<kSurrogateApHidden>(smem, kSurrogateApIn, T, fx, t, nets.wait_tries);
     if (kind == kSurfMlp)
       for (int k = 0; k < 8; ++k) yv[k] = t[k];
   }
-  if (__syncthreads_or(kind == kSkyMlp)) {
+  if (__syncthreads_or(kind == kSkyMlp) && tc_ok) {
     float t[8];
-    tc_ok = mlp_tile_tc<kSurrogateSkyHidden>(smem + nets.ap_bytes, kSurrogateSkyIn, T, fx, t) && tc_ok;
+    tc_ok = mlp_tile_tc<kSurrogateSkyHidden>(smem + nets.ap_bytes, kSurrogateSkyIn, T, fx, t, nets.wait_tries);
     if (kind == kSkyMlp)
       for (int k = 0; k < 8; ++k) yv[k] = t[k];
   }
-  // tensor memory is freed once no MMA is in flight (after a timed-out
-  // wait: one more bounded wait for the last commit of the tile)
+  // tensor memory is freed once no MMA is in flight: a tile that timed out
+  // has exactly one commit outstanding, waited for here with the library's
+  // full bound whatever the frame's own bound was
   tc::fence_before_sync();
-  if (__syncthreads_or(!tc_ok)) tc::mbar_wait(T.mbar, T.phase ^ 1u, kTcWaitTries);
+  if (!tc_ok) tc::mbar_wait(T.mbar, T.phase ^ 1u, kTcWaitTries);
   __syncthreads();
   tc::fence_after_sync();
   if (threadIdx.x < 32) tc::dealloc(s_tmem, kSurrogateTmemCols);
+  if (!tc_ok) {
+    // the networks' outputs are not valid: the plain path for these pixels
+    if (kind == kSurfMlp) kind = kSurfPlain;
+    if (kind == kSkyMlp) kind = kSkyLut;
+    if ((threadIdx.x & 127) == 0) atomicOr(Q.status, 1u);
+  }
 
   bool queued = false;
   uint32_t qkind = kQueueSurface;
@@ -360,7 +369,7 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
       Q.items[base + __popc(qm & ((1u << lane) - 1u))] = (qkind << 30) | uint32_t(cy * L.width + cx);
   }
   if (Q.stats != nullptr) {
-    if (!tc_ok && threadIdx.x == 0) atomicAdd(Q.stats + 7, 1.0f);  // tensor-core timeouts
+    if (!tc_ok && (threadIdx.x & 127) == 0) atomicAdd(Q.stats + 7, 1.0f);  // tiles whose MMA timed out
     const unsigned gs = __ballot_sync(kAll, kind == kSurfPlain), ms = __ballot_sync(kAll, kind == kSurfMlp);
     const unsigned mk_ = __ballot_sync(kAll, kind == kSkyMlp), ls = __ballot_sync(kAll, kind == kSkyLut);
     if (lane == 0) {

@@ -123,6 +123,19 @@ __device__ __forceinline__ void wait_st() { asm volatile("tcgen05.wait::st.sync.
 __device__ __forceinline__ void tile_sync(int tile) {
   asm volatile("bar.sync %0, 128;" ::"r"(tile + 1) : "memory");
 }
+// The same barrier, returning whether v holds in every thread of the tile:
+// a bounded wait can end true in one thread and false in another, and the
+// tile must take one path afterwards (its barriers stay matched).
+__device__ __forceinline__ bool tile_all(int tile, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 p, %1, 0;\n\tbar.red.and.pred q, %2, 128, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(uint32_t(v)), "r"(tile + 1)
+      : "memory");
+  return r != 0;
+}
 
 }  // namespace tc
 }  // namespace atm

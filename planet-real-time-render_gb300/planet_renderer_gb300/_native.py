@@ -166,7 +166,7 @@ class AtmSurrogate(ctypes.Structure):
         ("sky_twilight_cosine", ctypes.c_double),
         ("limb_degrees", ctypes.c_double),
         ("seed", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32),
+        ("tc_wait_polls", ctypes.c_int32),
         ("stats", ctypes.c_void_p),
     ]
 
@@ -245,6 +245,7 @@ SIGNATURES = {
     "atm_read_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_load_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_read_sample_counter": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
+    "atm_check": (ctypes.c_int, [_P, _P]),
     "atm_batch_create": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), ctypes.POINTER(ctypes.c_double), _I32, c_double3, _D, ctypes.POINTER(_P), _P],

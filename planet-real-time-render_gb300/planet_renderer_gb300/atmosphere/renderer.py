@@ -294,6 +294,14 @@ class AtmosphereRenderer:
         _native.check(self._lib.atm_build_lut(self._handle, _KINDS[kind], ctypes.byref(a),
                                               _stream_handle(self.device)))
 
+    def check(self) -> None:
+        """Synchronise the stream and raise the device-side errors of earlier
+        calls (``AtmError`` with ``ATM_E_TIMEOUT`` when a tensor-core wait of
+        ``composite_surrogate`` gave up: those pixels took the plain
+        integrator).  Clears what it reports."""
+
+        _native.check(self._lib.atm_check(self._handle, _stream_handle(self.device)))
+
     def radiance_samples(self, reset: bool = False) -> int:
         """Radiance samples evaluated by composites (synchronises the stream)."""
 

@@ -308,6 +308,9 @@ class Surrogate:
     twilight_cosine = 0.02
     sky_twilight_cosine = 0.1
     limb_degrees = 0.5
+    # bound of each tensor-core completion wait: 0 = the library's; -1 = none
+    # (every wait gives up at once, the MLP pixels take the plain path)
+    tc_wait_polls = 0
 
     def native(self, check_fraction: float = 0.01, seed: int = 0, stats=None) -> _native.AtmSurrogate:
         s = _native.AtmSurrogate()
@@ -325,6 +328,7 @@ class Surrogate:
         s.sky_twilight_cosine = float(self.sky_twilight_cosine)
         s.limb_degrees = float(self.limb_degrees)
         s.seed = int(seed) & 0xFFFFFFFF
+        s.tc_wait_polls = int(self.tc_wait_polls)
         s.stats = stats
         return s
 

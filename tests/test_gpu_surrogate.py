@@ -255,6 +255,45 @@ def test_checked_pixels_keep_the_plain_result(trained):
     r.close()
 
 
+def test_tensor_core_timeout_takes_the_plain_path_and_is_reported(trained):
+    """A wait bound of no polls makes every tensor-core completion wait give
+    up at once.  Every MLP pixel must then take the plain path (surface pixels
+    the limb integrator, sky pixels the sky-view LUT: the frame equals the
+    plain frame), the timed-out tiles are counted, and the handle's next
+    check reports ATM_E_TIMEOUT once, whether or not stats were passed."""
+
+    from planet_renderer_gb300._native import ATM_E_TIMEOUT, AtmError
+    from planet_renderer_gb300.atmosphere.surrogate import Surrogate
+
+    sg_full, _, _ = trained
+    sg = Surrogate(sg_full.aerial, sg_full.sky, sg_full.planet_radius_m, sg_full.top_altitude_m,
+                   sg_full.scale_height_range)
+    r, gb, args, _ = _frame(320, 180, 2000.0, 40.0, 30.0)
+    plain = _plain(r, gb, args)
+    r.check()
+    sg.tc_wait_polls = -1
+    got, stats = _surrogate(r, gb, args, sg)
+    np.testing.assert_allclose(got.cpu().numpy(), plain.cpu().numpy(), rtol=2e-5, atol=1e-9)
+    n_tiles = ((320 + 15) // 16) * ((180 + 15) // 16) * 2
+    assert 0 < int(stats[7]) <= n_tiles
+    assert int(stats[4]) == 0 and int(stats[5]) == 0  # no pixel kept a network output
+    with pytest.raises(AtmError) as err:
+        r.check()
+    assert err.value.code == ATM_E_TIMEOUT
+    r.check()  # reported once, then cleared
+    hdr = torch.zeros_like(gb["scene_hdr"])
+    r.composite_surrogate(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"], hdr, *args,
+                          surrogate=sg, stats=None, check_fraction=0.0)
+    with pytest.raises(AtmError):
+        r.check()
+    # the library's own bound: no timeout, the networks' outputs are used
+    sg.tc_wait_polls = 0
+    _, stats = _surrogate(r, gb, args, sg)
+    r.check()
+    assert int(stats[7]) == 0 and int(stats[4]) > 0
+    r.close()
+
+
 def _fp64_pixels(r, gb, args, v, pixels, diagnostic_view=0, scene=None):
     """FP64 oracle composite at the given (x, y) pixels (own FP64 LUTs)."""
 
