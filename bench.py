@@ -423,10 +423,15 @@ def main() -> None:
     parser.add_argument("--mlp-sweep", type=int, default=0,
                         help="also run the aerial-surrogate frame workload over this many 4K frames with cameras "
                              "log-uniform 1 m - 4000 km (e.g. 64)")
+    parser.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
+                        help="run one small case for an ncu capture instead of the benchmark (prints one line)")
     args = parser.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.profile_case:
+        PROFILE_CASES[args.profile_case](args)
         return
 
     import torch
@@ -491,6 +496,7 @@ def main() -> None:
         frame_4k = _frame_4k(device, args)
     batch = None if args.no_batch else _batch(device, args)
     post = None if args.no_post else _postprocess_4k(device, args)
+    shade = None if args.no_post else _shading_4k(device, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -515,6 +521,7 @@ def main() -> None:
             "frame_ms_4k": frame_4k,
             "batch": batch,
             "postprocess_4k": post,
+            "shading_4k": shade,
             "samples_per_step": samples_per_step,
             "e2e": {"value": world * e2e_samples / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / e2e_steps,
@@ -673,6 +680,55 @@ def _postprocess_4k(device, args) -> dict:
     del hdrs, display
     torch.cuda.empty_cache()
     return out
+
+
+SHADE_BYTES_LAND = 84     # position 12 + normal 12 + albedo 12 + id 4 + sun T 12 + sky 12 read, hdr 12 written
+SHADE_BYTES_OCEAN = 148   # + water depth 4, seabed albedo 12 and normal 12, slope 4, 4 terrain taps ~32
+
+
+def _shading_4k(device, args, steps=20) -> dict:
+    """Surface shading (shading.shade_surface, the consumer of prepare_frame's
+    surface lighting) at 3840x2160 on the land-and-ocean inputs of the 2 km
+    camera's fBm G-buffer: device time per frame with CUDA events."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere import scene
+    from planet_renderer_gb300.atmosphere.workloads import (EARTH_RADIUS_M, SOLAR_IRRADIANCE,
+                                                            SUN_ANGULAR_RADIUS_DEG)
+    from planet_renderer_gb300.shading import OceanShading, shade_surface
+
+    width, height = 3840, 2160
+    r, cfg, frames = _setup_chain(device, width, height)
+    v, gb, light = frames[0]
+    _chain(r, v, gb, light)
+    inputs = scene.shading_inputs(gb, EARTH_RADIUS_M, v.altitude_m, v.basis)
+    out = torch.empty_like(gb["scene_hdr"])
+    run = lambda: shade_surface(inputs, r.surface_sun_transmittance, r.surface_sky_radiance, out, v.sun_local,
+                                SOLAR_IRRADIANCE, v.basis, OceanShading(), math.radians(SUN_ANGULAR_RADIUS_DEG),
+                                v.tangent_half_fov)
+    for _ in range(args.warmup):
+        run()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(device)
+    start.record()
+    for _ in range(steps):
+        run()
+    end.record()
+    torch.cuda.synchronize(device)
+    ms = start.elapsed_time(end) / steps
+    n_ocean = int((inputs["water_depth"] > 0).sum())
+    n_land = int((inputs["surface_id"] == 0).sum())
+    algo = n_land * SHADE_BYTES_LAND + n_ocean * SHADE_BYTES_OCEAN
+    peaks = _peaks()
+    res = {"workload": "3840x2160 surface shading of the 2 km camera's fBm G-buffer (hits below the sphere are "
+                       "ocean: BRDF, refraction, seabed taps; the rest Lambertian land)",
+           "ms": ms, "land_px": n_land, "ocean_px": n_ocean, "algorithmic_bytes": algo,
+           "achieved_gbs": algo / (ms / 1e3) / 1e9, "frac": algo / (ms / 1e3) / 1e9 / peaks["hbm_gbs"]}
+    r.close()
+    del gb, inputs, out
+    torch.cuda.empty_cache()
+    return res
 
 
 def _batch(device, args) -> dict:
@@ -867,6 +923,88 @@ def _frame_4k(device, args) -> dict:
     return out
 
 
+SKY_ALTITUDES_M = (2_000.0, 20_000.0, 60_000.0)
+
+
+def _sky_4k(device, args, sg, n_pixels=1500) -> dict:
+    """The learned sky-view workload: the sky radiance of every pixel of a
+    3840x2160 view (cameras at 2, 20 and 60 km, pitch +15 deg, the frame-chain
+    workload's sun positions) by the plain integrator per pixel (the
+    sky-view march along each pixel's ray), by the sky network (plain where a
+    gate trips), and by the reference's sky-view LUT lookup; device ms per
+    frame and each one's error against the FP64 oracle's march."""
+
+    import numpy as np
+    import torch
+
+    from oracle.atm import Oracle
+    from planet_renderer_gb300 import camera
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.scene import pixel_rays
+    from planet_renderer_gb300.atmosphere.workloads import (EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG,
+                                                            frame_chain_cameras)
+
+    width, height = 3840, 2160
+    cfg = earth_baseline()
+    r = AtmosphereRenderer(width, height, cfg, device=device)
+    out = torch.empty((width, height, 3), device=device)
+    o = Oracle("f64")
+    ar = math.radians(SUN_ANGULAR_RADIUS_DEG)
+    tl = o.build_transmittance(cfg, EARTH_RADIUS_M)
+    ms = o.build_multi_scattering(cfg, EARTH_RADIUS_M, SOLAR_IRRADIANCE, ar, tl)
+    rng = np.random.default_rng(SEED + 2)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = {"plain": 0.0, "net": 0.0, "lut": 0.0}
+    errors = {k: [] for k in times}
+    cams = []
+    basis = camera.view_basis(0.0, 15.0)
+    tanfov = camera.tangent_half_fov(60.0)
+    for alt, v in zip(SKY_ALTITUDES_M, frame_chain_cameras(SEED)):
+        cr = EARTH_RADIUS_M + alt
+        sun = v.sun_local
+        r.update(EARTH_RADIUS_M, cr, sun.copy(), SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG)
+        a = (EARTH_RADIUS_M, cr, sun, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG, basis, tanfov)
+        xs = torch.as_tensor(rng.integers(0, width, n_pixels))
+        ys = torch.as_tensor(rng.integers(0, height, n_pixels))
+        rays = pixel_rays(width, height, basis, tanfov, xs, ys).numpy()
+        ref = o.sky_rays(cfg, EARTH_RADIUS_M, np.full(n_pixels, alt), rays, np.tile(sun, (n_pixels, 1)),
+                         SOLAR_IRRADIANCE, ar, tl, ms)
+        floor = 1e-4 * np.abs(ref).max()
+        cam = {"altitude_m": alt, "sun_zenith_deg": v.sun_zenith_deg}
+        for mode in times:
+            run = lambda: r.sky_pixels(out, *a, mode=mode, surrogate=sg if mode == "net" else None)
+            for _ in range(3):
+                run()
+            torch.cuda.synchronize(device)
+            start.record()
+            for _ in range(10):
+                run()
+            end.record()
+            torch.cuda.synchronize(device)
+            ms_mode = start.elapsed_time(end) / 10
+            times[mode] += ms_mode
+            got = out[xs.to(device), ys.to(device)].cpu().numpy().astype(np.float64)
+            e = np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor), axis=1)
+            errors[mode].append(e)
+            cam[f"{mode}_ms"] = ms_mode
+            cam[f"{mode}_err_mean"] = float(e.mean())
+        cams.append(cam)
+    r.check()
+    r.close()
+    del out
+    torch.cuda.empty_cache()
+    err = {k: {"mean": float(np.concatenate(v).mean()), "p99": float(np.quantile(np.concatenate(v), 0.99))}
+           for k, v in errors.items()}
+    n = len(SKY_ALTITUDES_M)
+    return {"workload": "sky radiance of every pixel of 3840x2160 views (cameras 2 / 20 / 60 km, pitch +15 deg, "
+                        "frame-chain sun positions): plain per-pixel sky-view march vs sky network (plain where "
+                        "|sun cosine| < 0.1 or within 0.5 deg of the limb) vs sky-view LUT lookup",
+            "plain_ms": times["plain"] / n, "net_ms": times["net"] / n, "lut_lookup_ms": times["lut"] / n,
+            "net_speedup_vs_plain": times["plain"] / times["net"], "error_vs_fp64": err,
+            "pixels_per_camera": n_pixels, "cameras": cams}
+
+
 def _mlp_sweep(r, cfg, sg, n_frames, device, n_pixels=300) -> dict:
     """The aerial-surrogate frame workload as configured: n_frames frames of
     the fBm G-buffer at the renderer's size with cameras log-uniform 1 m -
@@ -940,6 +1078,137 @@ def _mlp_sweep(r, cfg, sg, n_frames, device, n_pixels=300) -> dict:
             "plain_ms_mean": totals["plain"] / n_frames, "mlp_ms_mean": totals["mlp"] / n_frames,
             "speedup": totals["plain"] / totals["mlp"], "error_vs_fp64": error, "gate": stats_summary(stats),
             "cameras": cameras}
+
+
+# ---- small cases for ncu captures (python bench.py --profile-case NAME) ------
+# Each runs its kernels a few times on one workload of the benchmark, so that
+# `ncu -k regex:<kernel> -s <skip> -c <count>` captures a warm launch.
+
+
+def _profile_frame(args, width, height, camera):
+    import torch
+
+    device = torch.device("cuda:0")
+    torch.cuda.set_device(device)
+    r, cfg, frames = _setup_chain(device, width, height)
+    v, gb, light = frames[camera]
+    for _ in range(3):
+        _chain(r, v, gb, light)
+    torch.cuda.synchronize(device)
+    return r, frames
+
+
+def _profile_frame_1080p(args):
+    """Plain chain, 1080p, the 2 km camera: k_sky_view, k_prepare_surface,
+    k_aerial, k_composite three times each."""
+
+    _profile_frame(args, WIDTH, HEIGHT, 0)
+    print("profile case frame1080p: 3 chains of the 2 km camera at 1920x1080")
+
+
+def _profile_frame_4k_mlp(args):
+    """Surrogate chain at 4K for the 2 km camera, networks trained for
+    --mlp-epochs epochs (the kernels' cost does not depend on how well the
+    networks are trained): k_composite_surrogate and k_surrogate_fallback
+    three times each, after the training kernels."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere.surrogate import train_surrogate
+
+    device = torch.device("cuda:0")
+    torch.cuda.set_device(device)
+    r, cfg, frames = _setup_chain(device, 3840, 2160)
+    sg, _ = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device)
+    v, gb, light = frames[0]
+    for _ in range(3):
+        _chain_surrogate(r, v, gb, light, sg, None)
+    torch.cuda.synchronize(device)
+    r.check()
+    print(f"profile case frame4k_mlp: 3 surrogate chains of the 2 km camera at 3840x2160 "
+          f"({args.mlp_epochs} training epochs)")
+
+
+def _profile_luts(args):
+    """The four plain LUT builds of the Earth workload, three times each."""
+
+    args.warmup = 0
+    out = _lut_builds(__import__("torch").device("cuda:0"), argparse.Namespace(warmup=3))
+    print("profile case luts:", {k: round(out[k]["us"], 2) for k in ("transmittance", "multi_scattering",
+                                                                      "sky_view", "aerial")})
+
+
+def _profile_batch(args):
+    """One persistent batched build of the first 512 jobs of the batched
+    workload (a mix of sky-view LUTs and aerial volumes of both parameter
+    sets), tiles from the autotuner's defaults, three launches."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere.batch import BatchedLutBuilder, Tuning
+    from planet_renderer_gb300.atmosphere.workloads import batched_lut_jobs, batched_lut_sets
+
+    device = torch.device("cuda:0")
+    builder = BatchedLutBuilder(batched_lut_sets(), device=device)
+    jobs = batched_lut_jobs(SEED)[:512]
+    tuning = Tuning(64, 4, 3)
+    for _ in range(3):
+        builder.build(jobs, tuning)
+    torch.cuda.synchronize(device)
+    builder.close()
+    print("profile case batch: 3 launches over 512 jobs")
+
+
+def _profile_train(args):
+    """MLP training and batch inference of the aerial network (11 -> 4x64 ->
+    6): 8 Adam steps of 16,384 samples (k_mlp_grad, k_reduce_partials,
+    k_adam), then tcgen05 and mma.sync forwards of 2^20 samples."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere.mlp import Mlp
+
+    device = torch.device("cuda:0")
+    torch.cuda.set_device(device)
+    g = torch.Generator(device=device).manual_seed(SEED)
+    net = Mlp(11, 4, 6, seed=3, device=device)
+    x = torch.rand((16384, 11), device=device, generator=g) * 2 - 1
+    t = torch.randn((16384, 6), device=device, generator=g)
+    for _ in range(8):
+        net.train_step(x, t, lr=1e-3)
+    net.pack()
+    xb = torch.rand((1 << 20, 11), device=device, generator=g) * 2 - 1
+    for precision in ("bf16_tc", "bf16") * 3:
+        net.forward(xb, precision)
+    torch.cuda.synchronize(device)
+    print("profile case train: 8 Adam steps, 3 tcgen05 + 3 mma.sync forwards of 2^20 samples")
+
+
+def _profile_post(args):
+    """The display post-process at 4K (default configuration), three frames."""
+
+    args.steps = 0
+    _postprocess_4k(__import__("torch").device("cuda:0"), argparse.Namespace(warmup=3, steps=0))
+    print("profile case post4k")
+
+
+def _profile_shade(args):
+    """Surface shading at 4K on the synthetic land-and-ocean G-buffer of the
+    2 km camera, three launches."""
+
+    out = _shading_4k(__import__("torch").device("cuda:0"), argparse.Namespace(warmup=3), steps=3)
+    print("profile case shade4k:", round(out["ms"], 3), "ms")
+
+
+PROFILE_CASES = {
+    "frame1080p": _profile_frame_1080p,
+    "frame4k_mlp": _profile_frame_4k_mlp,
+    "luts": _profile_luts,
+    "batch": _profile_batch,
+    "train": _profile_train,
+    "post4k": _profile_post,
+    "shade4k": _profile_shade,
+}
 
 
 if __name__ == "__main__":

@@ -333,6 +333,14 @@ typedef struct AtmSampleOptions {
                                 [surface_min_m, surface_max_m] (where the ray reaches it) */
   double surface_min_m;
   double surface_max_m;
+  double start_min_m;        /* segments start at an altitude in [start_min_m, start_max_m]
+                                (uniform in the altitude feature) when start_min_m <
+                                start_max_m; otherwise anywhere in the shell           */
+  double start_max_m;
+  double sun_angle_fraction;    /* share of samples whose sun zenith at the start is uniform in
+                                   angle in [0, sun_angle_max_degrees] (the rest uniform in the
+                                   sun feature, which concentrates on the horizon)          */
+  double sun_angle_max_degrees;
 } AtmSampleOptions;
 int atm_surrogate_samples(AtmBatch* batch, int32_t kind, int64_t n, uint64_t seed, const AtmSampleOptions* options,
                           const double scale_height_range[4], float* features, float* targets, void* stream);
@@ -396,6 +404,30 @@ int atm_composite_surrogate(AtmHandle* handle, const float* scene_hdr, const flo
                             double sun_angular_radius_degrees, const double view_basis[9], double tangent_half_fov,
                             double star_contrast_start, double star_contrast_end, const AtmSurrogate* surrogate,
                             void* stream);
+
+/* Sky radiance of every pixel along its own view ray from the camera (the
+ * learned sky-view workload; no G-buffer: every pixel is treated as sky),
+ * written to the first three floats of each `radiance` element:
+ *  ATM_SKY_PIXELS_PLAIN  the plain integrator per pixel: the sky-view LUT's
+ *                        march (:1208-1302, sky_view_steps warped segments)
+ *                        along the pixel's ray;
+ *  ATM_SKY_PIXELS_NET    the sky network of `surrogate` (BF16 on tcgen05), the
+ *                        plain integrator where a gate trips (|sun cosine|
+ *                        at the camera below sky_twilight_cosine, the ray
+ *                        within limb_degrees of the limb, the camera above
+ *                        the shell) or a tensor-core wait gives up (which
+ *                        sets the flag atm_check reports);
+ *  ATM_SKY_PIXELS_LUT    the reference's path: a bilinear tap of the sky-view
+ *                        LUT (:1474-1525) built by atm_update.
+ * Plain pixels add their samples to the radiance-sample counter.  No
+ * counterpart in the reference, whose sky is the LUT path only. */
+#define ATM_SKY_PIXELS_PLAIN 0
+#define ATM_SKY_PIXELS_NET 1
+#define ATM_SKY_PIXELS_LUT 2
+int atm_sky_pixels(AtmHandle* handle, int32_t mode, float* radiance, const AtmImage* image, double planet_radius_m,
+                   double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
+                   double sun_angular_radius_degrees, const double view_basis[9], double tangent_half_fov,
+                   const AtmSurrogate* surrogate, void* stream);
 
 /* Synchronises `stream` and reports, then clears, the device-side errors of
  * the handle's earlier stream-ordered calls: ATM_E_TIMEOUT when a
@@ -517,6 +549,25 @@ typedef struct AtmShadeImages {
 } AtmShadeImages;
 int atm_shade_surface(const AtmShadeParams* params, const AtmShadeImages* images, const AtmImage* image,
                       void* stream);
+
+/* The frame's last three steps in one pass over the pixels: the surface
+ * lighting of atm_prepare_frame (:1422-1472), the surface shading of
+ * atm_shade_surface (renderer.py:1277-1575) and the COMPOSITE view of
+ * atm_composite (or, with `surrogate`, of atm_composite_surrogate), as the
+ * reference's frame calls them in sequence (renderer.py:1671-1727).  Each
+ * pixel's lighting and shaded colour stay in registers: the three
+ * full-resolution images the separate calls write and read back
+ * (surface_sun_transmittance, surface_sky_radiance, surface_hdr) are not
+ * formed, and `images`' sun_transmittance, sky_radiance and surface_hdr may
+ * be null.  The aerial-perspective volume of prepare_frame (which the
+ * COMPOSITE view does not read) is not rebuilt.  Needs the LUTs of a
+ * preceding atm_update.  No counterpart in the reference. */
+int atm_render_frame(AtmHandle* handle, const AtmShadeParams* shade, const AtmShadeImages* images,
+                     const float* space_hdr, float* hdr, const AtmImage* image, double planet_radius_m,
+                     double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
+                     const double sun_disk_radiance[3], double sun_angular_radius_degrees, const double view_basis[9],
+                     double tangent_half_fov, double star_contrast_start, double star_contrast_end,
+                     const AtmSurrogate* surrogate, void* stream);
 
 #ifdef __cplusplus
 }

@@ -931,15 +931,26 @@ ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t
   if (!b || !features || !targets || n < 1) return fail(ATM_E_INVALID, "invalid surrogate sample arguments");
   if (kind != ATM_SURROGATE_SKY && kind != ATM_SURROGATE_AERIAL) return fail(ATM_E_INVALID, "unknown kind %d", kind);
   if (!valid_range(scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
-  atm::SampleShaping shaping{0.0f, 0.0f, 0.0f, 0.0f};
+  atm::SampleShaping shaping{0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   if (options) {
     const AtmSampleOptions& o = *options;
     if (!(o.shell_top_fraction >= 0.0 && o.shell_top_fraction <= 1.0 && o.surface_fraction >= 0.0 &&
           o.surface_fraction <= 1.0 && std::isfinite(o.surface_min_m) && std::isfinite(o.surface_max_m) &&
-          o.surface_min_m <= o.surface_max_m))
+          o.surface_min_m <= o.surface_max_m && std::isfinite(o.start_min_m) && std::isfinite(o.start_max_m) &&
+          o.sun_angle_fraction >= 0.0 && o.sun_angle_fraction <= 1.0 && o.sun_angle_max_degrees >= 0.0 &&
+          o.sun_angle_max_degrees <= 180.0))
       return fail(ATM_E_INVALID, "sample options out of range");
     shaping = {float(o.shell_top_fraction), float(o.surface_fraction), float(o.surface_min_m),
-               float(o.surface_max_m)};
+               float(o.surface_max_m), 0.0f, 0.0f, float(o.sun_angle_fraction),
+               float(o.sun_angle_max_degrees * (kPi / 180.0))};
+    if (o.start_min_m < o.start_max_m) {
+      // the altitude feature 2 sqrt(h / top) - 1 of both ends of the band
+      const double top = b->params[0].top_altitude_m;
+      if (!(o.start_min_m >= 0.0 && o.start_max_m <= top))
+        return fail(ATM_E_INVALID, "start altitude band must lie inside the shell [0, %g] m", top);
+      shaping.x0_lo = float(2.0 * std::sqrt(o.start_min_m / top) - 1.0);
+      shaping.x0_hi = float(2.0 * std::sqrt(o.start_max_m / top) - 1.0);
+    }
   }
   const int n_sets = int(b->params.size());
   for (int i = 1; i < n_sets; ++i)
@@ -973,24 +984,11 @@ ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t
   return ATM_OK;
 }
 
-ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const float* space_hdr,
-                                    const int32_t* surface_id, const float* position_view, float* hdr,
-                                    const AtmImage* image, double planet_radius_m, double camera_radius_m,
-                                    const double sun_local[3], const double solar_irradiance[3],
-                                    const double sun_disk_radiance[3], double sun_angular_radius_degrees,
-                                    const double view_basis[9], double tangent_half_fov, double star_contrast_start,
-                                    double star_contrast_end, const AtmSurrogate* sg, void* stream) {
-  int rc = check_handle(h);
-  if (rc) return rc;
-  if ((rc = check_image(h, image))) return rc;
-  if (!scene_hdr || !space_hdr || !surface_id || !position_view || !hdr || !sun_local || !solar_irradiance ||
-      !sun_disk_radiance || !view_basis || !sg)
-    return fail(ATM_E_INVALID, "null pointer argument to atm_composite_surrogate");
-  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
-      tangent_half_fov <= 0.0)
-    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
-  if (int64_t(image->width) * image->height > (int64_t(1) << 30))
-    return fail(ATM_E_INVALID, "frame larger than 2^30 pixels");
+// Validation of an AtmSurrogate against the frame, and the device-side view
+// of its networks, gates and the handle's fallback queue (allocated on first
+// use).  Shared by the surrogate composite and the fused frame.
+int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m, double camera_radius_m,
+                    atm::SurrogateNets& nets, atm::SurrogateQueue& Q) {
   if (!valid_range(sg->scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
   if (!(sg->check_fraction >= 0.0 && sg->check_fraction <= 1.0))
     return fail(ATM_E_INVALID, "check_fraction must be in [0, 1]");
@@ -1002,7 +1000,7 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
         std::fabs(sg->trained_top_altitude_m - h->params.top_altitude_m) > 1.0)
       return fail(ATM_E_INVALID, "the networks were trained for another planet radius or shell top");
   }
-  atm::SurrogateNets nets{};
+  nets = atm::SurrogateNets{};
   // the camera above the shell: every segment starts at the shell top
   const bool above = camera_radius_m - planet_radius_m > h->params.top_altitude_m;
   const AtmMlp* aerial = above && sg->aerial_above_shell ? sg->aerial_above_shell : sg->aerial;
@@ -1043,13 +1041,37 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
     ATM_CUDA(cudaGetDevice(&dev), "device query");
     ATM_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev), "device query");
   }
-  atm::SurrogateQueue Q{};
+  Q = atm::SurrogateQueue{};
   Q.count = h->queue;
   Q.status = h->queue + 2;
   Q.items = h->queue + 4;
   Q.stats = sg->stats;
   Q.check_fraction = float(sg->check_fraction);
   Q.seed = sg->seed;
+  return ATM_OK;
+}
+
+ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const float* space_hdr,
+                                    const int32_t* surface_id, const float* position_view, float* hdr,
+                                    const AtmImage* image, double planet_radius_m, double camera_radius_m,
+                                    const double sun_local[3], const double solar_irradiance[3],
+                                    const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                                    const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                                    double star_contrast_end, const AtmSurrogate* sg, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!scene_hdr || !space_hdr || !surface_id || !position_view || !hdr || !sun_local || !solar_irradiance ||
+      !sun_disk_radiance || !view_basis || !sg)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_composite_surrogate");
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  if (int64_t(image->width) * image->height > (int64_t(1) << 30))
+    return fail(ATM_E_INVALID, "frame larger than 2^30 pixels");
+  atm::SurrogateNets nets{};
+  atm::SurrogateQueue Q{};
+  if ((rc = surrogate_setup(h, sg, planet_radius_m, camera_radius_m, nets, Q))) return rc;
   const atm::CompositeScalars A =
       composite_scalars(h, planet_radius_m, camera_radius_m, sun_local, solar_irradiance, sun_disk_radiance,
                         sun_angular_radius_degrees, view_basis, tangent_half_fov, star_contrast_start,
@@ -1059,6 +1081,68 @@ ATM_API int atm_composite_surrogate(AtmHandle* h, const float* scene_hdr, const 
                                            h->lut[ATM_LUT_MULTI_SCATTERING], h->lut[ATM_LUT_SKY_VIEW], nets, Q, hdr,
                                            h->samples, h->sm_count, static_cast<cudaStream_t>(stream)),
            "surrogate composite");
+  return ATM_OK;
+}
+
+ATM_API int atm_sky_pixels(AtmHandle* h, int32_t mode, float* radiance, const AtmImage* image,
+                           double planet_radius_m, double camera_radius_m, const double sun_local[3],
+                           const double solar_irradiance[3], double sun_angular_radius_degrees,
+                           const double view_basis[9], double tangent_half_fov, const AtmSurrogate* sg,
+                           void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!radiance || !sun_local || !solar_irradiance || !view_basis)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_sky_pixels");
+  if (mode < ATM_SKY_PIXELS_PLAIN || mode > ATM_SKY_PIXELS_LUT) return fail(ATM_E_INVALID, "unknown mode %d", mode);
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  atm::SurrogateNets nets{};
+  if (mode == ATM_SKY_PIXELS_NET) {
+    if (!sg || !sg->sky) return fail(ATM_E_INVALID, "the network mode needs a surrogate with a sky network");
+    if (!mlp_is(sg->sky, atm::kSurrogateSkyIn, atm::kSurrogateSkyHidden, atm::kSurrogateSkyOut))
+      return fail(ATM_E_INVALID, "sky network must be 10 -> 3 x 64 -> 3");
+    if (!sg->sky->packed_current) return fail(ATM_E_STATE, "sky network not packed (atm_mlp_pack_bf16)");
+    if (!valid_range(sg->scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
+    if (std::fabs(sg->trained_planet_radius_m - planet_radius_m) > 1.0 ||
+        std::fabs(sg->trained_top_altitude_m - h->params.top_altitude_m) > 1.0)
+      return fail(ATM_E_INVALID, "the networks were trained for another planet radius or shell top");
+    if (!(sg->sky_floor > 0.0 && sg->sky_floor < 1.0)) return fail(ATM_E_INVALID, "radiance floors must be in (0, 1)");
+    if (!(sg->sky_twilight_cosine >= 0.0 && sg->sky_twilight_cosine <= 1.0 && sg->limb_degrees >= 0.0 &&
+          sg->limb_degrees <= 90.0))
+      return fail(ATM_E_INVALID, "gate thresholds out of range");
+    if (sg->tc_wait_polls < -1) return fail(ATM_E_INVALID, "tc_wait_polls must be -1, 0 or positive");
+    nets.sky = static_cast<const unsigned char*>(sg->sky->packed_tc);
+    nets.sky_bytes = int(atm::mlp_tc_bytes(sg->sky->shape));
+    if (nets.sky_bytes % 16) return fail(ATM_E_STATE, "packed network size not a multiple of 16");
+    const double* r = sg->scale_height_range;
+    nets.lhr_n = log_feature(h->params.rayleigh_scale_height_m, r[0], r[1]);
+    nets.lhm_n = log_feature(h->params.mie_scale_height_m, r[2], r[3]);
+    nets.sky_floor = float(sg->sky_floor);
+    nets.sky_twilight_cos = float(sg->sky_twilight_cosine);
+    nets.limb_rad = float(sg->limb_degrees * (kPi / 180.0));
+    nets.wait_tries =
+        sg->tc_wait_polls == 0 ? atm::kTcWaitTries : sg->tc_wait_polls < 0 ? 0 : sg->tc_wait_polls;
+  }
+  if (mode == ATM_SKY_PIXELS_LUT && !h->sky_valid)
+    return fail(ATM_E_STATE, "the LUT mode needs a sky-view LUT (atm_update first)");
+  if (!h->queue) {  // the timeout flag lives in the fallback queue's header
+    const size_t cap = size_t(h->width) * size_t(h->height);
+    ATM_CUDA(cudaMalloc(&h->queue, (cap + 4) * sizeof(uint32_t)), "fallback queue");
+    ATM_CUDA(cudaMemset(h->queue, 0, 4 * sizeof(uint32_t)), "fallback queue");
+    int dev = 0;
+    ATM_CUDA(cudaGetDevice(&dev), "device query");
+    ATM_CUDA(cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, dev), "device query");
+  }
+  const double zero3[3] = {0.0, 0.0, 0.0};
+  const atm::CompositeScalars A =
+      composite_scalars(h, planet_radius_m, camera_radius_m, sun_local, solar_irradiance, zero3,
+                        sun_angular_radius_degrees, view_basis, tangent_half_fov, 0.0, 1.0);
+  ATM_CUDA(atm::launch_sky_pixels(mode, h->dev, layout_of(image), A, h->lut[ATM_LUT_TRANSMITTANCE],
+                                  h->lut[ATM_LUT_MULTI_SCATTERING], h->lut[ATM_LUT_SKY_VIEW], nets, h->queue + 2,
+                                  radiance, h->samples, static_cast<cudaStream_t>(stream)),
+           "sky pixels");
   return ATM_OK;
 }
 
@@ -1242,23 +1326,24 @@ ATM_API int atm_post_read_bloom(const AtmPost* p, int32_t dims[2], float* dst_de
 }
 
 // ---- surface shading -------------------------------------------------------------
-ATM_API int atm_shade_surface(const AtmShadeParams* p, const AtmShadeImages* im, const AtmImage* image,
-                              void* stream) {
-  if (!p || !im || !image) return fail(ATM_E_INVALID, "null argument");
-  if (image->width < 1 || image->height < 1) return fail(ATM_E_INVALID, "image must be at least 1x1");
-  if (image->channels != 3 && image->channels != 4) return fail(ATM_E_INVALID, "channels must be 3 or 4");
-  if (image->stride_x <= 0 || image->stride_y <= 0) return fail(ATM_E_INVALID, "image strides must be positive");
-  const void* required[] = {im->position, im->normal, im->albedo, im->water_depth, im->seabed_albedo,
-                            im->seabed_normal, im->slope_variance, im->surface_id, im->terrain_position,
-                            im->terrain_normal, im->terrain_albedo, im->terrain_surface_id, im->sun_transmittance,
-                            im->sky_radiance, im->surface_hdr};
+// AtmShadeParams in the float32 form of the reference kernel's arguments;
+// the images of `im` the shading reads are checked (with_lighting: also the
+// surface lighting and the output of a separate shading pass).
+int shade_setup(const AtmShadeParams* p, const AtmShadeImages* im, bool with_lighting, atm::ShadeParams& S,
+                atm::ShadeImages& I) {
+  if (!p || !im) return fail(ATM_E_INVALID, "null shading argument");
+  const void* required[] = {im->position,       im->normal,          im->albedo,         im->water_depth,
+                            im->seabed_albedo,  im->seabed_normal,   im->slope_variance, im->surface_id,
+                            im->terrain_position, im->terrain_normal, im->terrain_albedo, im->terrain_surface_id};
   for (const void* q : required)
     if (!q) return fail(ATM_E_INVALID, "null image pointer");
+  if (with_lighting && (!im->sun_transmittance || !im->sky_radiance || !im->surface_hdr))
+    return fail(ATM_E_INVALID, "null image pointer");
   const double* finite[] = {p->sun_global, p->solar_irradiance, p->view_right_global, p->view_up_global,
                             p->view_forward_global, p->ocean_absorption, p->ocean_scattering};
   for (const double* v : finite)
     if (!finite_n(v, 3)) return fail(ATM_E_INVALID, "vector arguments must be finite");
-  atm::ShadeParams S{};
+  S = atm::ShadeParams{};
   to_f32(p->sun_global, S.sun, 3);
   to_f32(p->solar_irradiance, S.E, 3);
   to_f32(p->view_right_global, S.right, 3);
@@ -1282,10 +1367,64 @@ ATM_API int atm_shade_surface(const AtmShadeParams* p, const AtmShadeImages* im,
   S.tanfov = float(p->tangent_half_fov);
   S.four_pi = float(4.0 * kPi);
   S.ocean_id = p->ocean_surface_id;
-  atm::ShadeImages I{im->position,       im->normal,         im->albedo,         im->water_depth,
-                     im->seabed_albedo,  im->seabed_normal,  im->slope_variance, im->surface_id,
-                     im->terrain_position, im->terrain_normal, im->terrain_albedo, im->terrain_surface_id,
-                     im->sun_transmittance, im->sky_radiance, im->surface_hdr};
+  I = atm::ShadeImages{im->position,       im->normal,         im->albedo,         im->water_depth,
+                       im->seabed_albedo,  im->seabed_normal,  im->slope_variance, im->surface_id,
+                       im->terrain_position, im->terrain_normal, im->terrain_albedo, im->terrain_surface_id,
+                       im->sun_transmittance, im->sky_radiance, im->surface_hdr};
+  return ATM_OK;
+}
+
+ATM_API int atm_shade_surface(const AtmShadeParams* p, const AtmShadeImages* im, const AtmImage* image,
+                              void* stream) {
+  if (!p || !im || !image) return fail(ATM_E_INVALID, "null argument");
+  if (image->width < 1 || image->height < 1) return fail(ATM_E_INVALID, "image must be at least 1x1");
+  if (image->channels != 3 && image->channels != 4) return fail(ATM_E_INVALID, "channels must be 3 or 4");
+  if (image->stride_x <= 0 || image->stride_y <= 0) return fail(ATM_E_INVALID, "image strides must be positive");
+  atm::ShadeParams S;
+  atm::ShadeImages I;
+  int rc = shade_setup(p, im, true, S, I);
+  if (rc) return rc;
   ATM_CUDA(atm::launch_shade_surface(S, layout_of(image), I, static_cast<cudaStream_t>(stream)), "surface shading");
+  return ATM_OK;
+}
+
+ATM_API int atm_render_frame(AtmHandle* h, const AtmShadeParams* shade, const AtmShadeImages* images,
+                             const float* space_hdr, float* hdr, const AtmImage* image, double planet_radius_m,
+                             double camera_radius_m, const double sun_local[3], const double solar_irradiance[3],
+                             const double sun_disk_radiance[3], double sun_angular_radius_degrees,
+                             const double view_basis[9], double tangent_half_fov, double star_contrast_start,
+                             double star_contrast_end, const AtmSurrogate* sg, void* stream) {
+  int rc = check_handle(h);
+  if (rc) return rc;
+  if ((rc = check_image(h, image))) return rc;
+  if (!space_hdr || !hdr || !sun_local || !solar_irradiance || !sun_disk_radiance || !view_basis)
+    return fail(ATM_E_INVALID, "null pointer argument to atm_render_frame");
+  if (!finite_n(view_basis, 9) || !finite_n(sun_local, 3) || !std::isfinite(tangent_half_fov) ||
+      tangent_half_fov <= 0.0)
+    return fail(ATM_E_INVALID, "non-finite or non-positive frame argument");
+  atm::ShadeParams S;
+  atm::ShadeImages I;
+  if ((rc = shade_setup(shade, images, false, S, I))) return rc;
+  if (!h->t_valid || !h->ms_valid || !h->sky_valid)
+    return fail(ATM_E_STATE, "the frame needs the renderer's LUTs (atm_update first)");
+  const atm::CompositeScalars A =
+      composite_scalars(h, planet_radius_m, camera_radius_m, sun_local, solar_irradiance, sun_disk_radiance,
+                        sun_angular_radius_degrees, view_basis, tangent_half_fov, star_contrast_start,
+                        star_contrast_end);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const atm::ImageLayout L = layout_of(image);
+  if (sg == nullptr) {
+    ATM_CUDA(atm::launch_frame(h->dev, L, A, S, I, space_hdr, h->lut[ATM_LUT_TRANSMITTANCE],
+                               h->lut[ATM_LUT_MULTI_SCATTERING], h->lut[ATM_LUT_SKY_VIEW], hdr, h->samples, s),
+             "fused frame");
+    return ATM_OK;
+  }
+  atm::SurrogateNets nets{};
+  atm::SurrogateQueue Q{};
+  if ((rc = surrogate_setup(h, sg, planet_radius_m, camera_radius_m, nets, Q))) return rc;
+  ATM_CUDA(atm::launch_composite_surrogate(h->dev, L, A, nullptr, space_hdr, images->surface_id, images->position,
+                                           h->lut[ATM_LUT_TRANSMITTANCE], h->lut[ATM_LUT_MULTI_SCATTERING],
+                                           h->lut[ATM_LUT_SKY_VIEW], nets, Q, hdr, h->samples, h->sm_count, s, &S, &I),
+           "fused surrogate frame");
   return ATM_OK;
 }

@@ -35,56 +35,27 @@ __global__ void __launch_bounds__(256) k_prepare_surface(DevParams P, ImageLayou
   const size_t o = e * L.channels;
   Frame F = make_frame(P, tlut, mslut, bottom, ar, sun, splat(0.0f));
   f3 st = splat(1.0f), sky = splat(0.0f);
-  if (sid[e] >= 0) {
-    f3 vp = ld3(pos + o);
-    f3 lp = (right * vp.x + up * vp.y) + fwd * vp.z;
-    f3 pp = mk(lp.x, (bottom + cam_alt) + lp.y, lp.z);
-    float radius = norm(pp);
-    f3 radial = pp / mx(radius, 1.0f);
-    float sd = norm(lp);
-    f3 lr = lp / mx(sd, 1.0f);
-    float h, sc;
-    if (!far_camera(P, bottom, cam_alt)) {
-      h = altitude_on_ray(cam_alt, lr.y, sd, bottom);
-      sc = dot(radial, sun);
-    } else {  // camera above the shell: pivot at the closest approach (RayGeom)
-      const RayGeom G = camera_ray_geom(P, bottom, cam_alt, lr);
-      h = altitude_at(G, sd, bottom);
-      // p . sun = o . sun + t_c lr . sun + (t - t_c) lr . sun, the first two in
-      // FP64 (the point's own coordinates cancel like its altitude)
-      const double s0 = (double(bottom) + double(cam_alt)) * double(sun.y) +
-                        double(G.tc) * (double(lr.x) * sun.x + double(lr.y) * sun.y + double(lr.z) * sun.z);
-      sc = (float(s0) + (sd - G.tc) * dot(lr, sun)) * frcp(bottom + h);
-    }
-    Horizon H = horizon_at(h, bottom);
-    float vis;
-    st = sample_solar_t(P, F, h, sc, H, vis);
-    sky = sample_ms(P, F, h, sc, H.hc);
-  }
+  if (sid[e] >= 0) surface_lighting(P, F, cam_alt, right, up, fwd, ld3(pos + o), st, sky);
   out_t[o + 0] = st.x;
   out_t[o + 1] = st.y;
   out_t[o + 2] = st.z;
-  sky = vmax(sky, 0.0f);
   out_sky[o + 0] = sky.x;
   out_sky[o + 1] = sky.y;
   out_sky[o + 2] = sky.z;
 }
 
-// One pixel of the COMPOSITE view (:1860-1940): writes hdr and adds the
-// pixel's radiance samples to `samples`.  Shared by the composite and its
-// no-allocation variant so that the two cannot drift apart.
-__device__ __forceinline__ void composite_pixel(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
-                                                const float* __restrict__ scene, const float* __restrict__ space,
-                                                const int32_t* __restrict__ sid, const float* __restrict__ pos,
-                                                const float4* __restrict__ tlut, const float4* __restrict__ mslut,
-                                                const float4* __restrict__ svlut, float* __restrict__ hdr, int x,
-                                                int y, uint32_t& samples) {
-  const size_t e = pix_offset(L, x, y);
-  const size_t o = e * L.channels;
-  Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+// One pixel of the COMPOSITE view (:1860-1940) given its surface colour
+// (scene_hdr) and surface id: writes hdr and adds the pixel's radiance
+// samples to `samples`.  Shared by the composite, its no-allocation variant
+// and the fused frame so that they cannot drift apart.
+__device__ __forceinline__ void composite_pixel_with(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                                                     const Frame& F, f3 color, int32_t sidv,
+                                                     const float* __restrict__ space, const float* __restrict__ pos,
+                                                     const float4* __restrict__ svlut, float* __restrict__ hdr, int x,
+                                                     int y, uint32_t& samples) {
+  const size_t o = pix_offset(L, x, y) * L.channels;
   PixelRay pr = pixel_ray(L, A, x, y);
-  f3 color = ld3(scene + o);
-  if (sid[e] >= 0) {
+  if (sidv >= 0) {
     const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, pr.ray);
     float sd = norm(ld3(pos + o));
     float start, end;
@@ -101,6 +72,16 @@ __device__ __forceinline__ void composite_pixel(const DevParams& P, const ImageL
   hdr[o + 1] = color.y;
   hdr[o + 2] = color.z;
 }
+__device__ __forceinline__ void composite_pixel(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                                                const float* __restrict__ scene, const float* __restrict__ space,
+                                                const int32_t* __restrict__ sid, const float* __restrict__ pos,
+                                                const float4* __restrict__ tlut, const float4* __restrict__ mslut,
+                                                const float4* __restrict__ svlut, float* __restrict__ hdr, int x,
+                                                int y, uint32_t& samples) {
+  const size_t e = pix_offset(L, x, y);
+  const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+  composite_pixel_with(P, L, A, F, ld3(scene + e * L.channels), sid[e], space, pos, svlut, hdr, x, y, samples);
+}
 
 // COMPOSITE view (:1860-1940): the per-frame path.
 __global__ void __launch_bounds__(256, 3) k_composite(DevParams P, ImageLayout L, CompositeScalars A,
@@ -112,6 +93,28 @@ __global__ void __launch_bounds__(256, 3) k_composite(DevParams P, ImageLayout L
   int x, y;
   uint32_t samples = 0;
   if (tile_pixel(L, x, y)) composite_pixel(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, hdr, x, y, samples);
+  warp_count(samples, counter);
+}
+
+// The frame in one pass: per pixel the surface lighting (:1422-1472), the
+// surface shading (renderer.py:1277-1575) and the COMPOSITE view
+// (:1860-1940), with the lighting and the shaded colour in registers instead
+// of the three full-resolution images that the separate calls write and
+// read back.
+__global__ void __launch_bounds__(256, 3) k_frame(DevParams P, ImageLayout L, CompositeScalars A, ShadeParams S,
+                                               ShadeImages I, const float* __restrict__ space,
+                                               const float4* __restrict__ tlut, const float4* __restrict__ mslut,
+                                               const float4* __restrict__ svlut, float* __restrict__ hdr,
+                                               unsigned long long* counter) {
+  int x, y;
+  uint32_t samples = 0;
+  if (tile_pixel(L, x, y)) {
+    const size_t e = pix_offset(L, x, y);
+    const int32_t sidv = I.surface_id[e];
+    const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+    const f3 scene = shaded_scene(P, F, A, S, L, I, x, y, e, sidv);
+    composite_pixel_with(P, L, A, F, scene, sidv, space, I.position, svlut, hdr, x, y, samples);
+  }
   warp_count(samples, counter);
 }
 
@@ -233,6 +236,13 @@ cudaError_t launch_prepare_surface(const DevParams& P, const ImageLayout& L, con
   const unsigned blocks = unsigned((static_cast<long long>(L.width) * L.height + 255) / 256);
   k_prepare_surface<<<blocks, 256, 0, s>>>(P, L, pos, sid, bottom, cam_alt, host3(sun), ar, host3(right),
                                                  host3(up), host3(fwd), tlut, mslut, out_sun_t, out_sky);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frame(const DevParams& P, const ImageLayout& L, const CompositeScalars& A, const ShadeParams& S,
+                         const ShadeImages& I, const float* space, const float4* tlut, const float4* mslut,
+                         const float4* svlut, float* hdr, unsigned long long* sample_counter, cudaStream_t s) {
+  k_frame<<<tile_grid(L), 256, 0, s>>>(P, L, A, S, I, space, tlut, mslut, svlut, hdr, sample_counter);
   return cudaGetLastError();
 }
 

@@ -6,6 +6,7 @@
 
 #include "atm_device.cuh"
 #include "atm_kernels.h"
+#include "atm_shade.cuh"
 
 namespace atm {
 
@@ -108,6 +109,40 @@ __device__ __forceinline__ void shadow_roots_far(float h0, f3 df, f3 sf, float b
 }
 
 // Geometry of a camera ray (sine from the horizontal components).
+__device__ __forceinline__ RayGeom camera_ray_geom(const DevParams& P, float bottom, float h0, f3 ray);
+
+// _prepare_surface_lighting :1422-1472 for one surface pixel: the finite-disk
+// sun transmittance `st` and the multi-scattering sky radiance `sky`
+// (clamped at 0) at its view-space position vp.
+__device__ __forceinline__ void surface_lighting(const DevParams& P, const Frame& F, float cam_alt, f3 right, f3 up,
+                                                 f3 fwd, f3 vp, f3& st, f3& sky) {
+  const float bottom = F.bottom;
+  const f3 sun = F.sun;
+  f3 lp = (right * vp.x + up * vp.y) + fwd * vp.z;
+  f3 pp = mk(lp.x, (bottom + cam_alt) + lp.y, lp.z);
+  float radius = norm(pp);
+  f3 radial = pp / mx(radius, 1.0f);
+  float sd = norm(lp);
+  f3 lr = lp / mx(sd, 1.0f);
+  float h, sc;
+  if (!far_camera(P, bottom, cam_alt)) {
+    h = altitude_on_ray(cam_alt, lr.y, sd, bottom);
+    sc = dot(radial, sun);
+  } else {  // camera above the shell: pivot at the closest approach (RayGeom)
+    const RayGeom G = camera_ray_geom(P, bottom, cam_alt, lr);
+    h = altitude_at(G, sd, bottom);
+    // p . sun = o . sun + t_c lr . sun + (t - t_c) lr . sun, the first two in
+    // FP64 (the point's own coordinates cancel like its altitude)
+    const double s0 = (double(bottom) + double(cam_alt)) * double(sun.y) +
+                      double(G.tc) * (double(lr.x) * sun.x + double(lr.y) * sun.y + double(lr.z) * sun.z);
+    sc = (float(s0) + (sd - G.tc) * dot(lr, sun)) * frcp(bottom + h);
+  }
+  Horizon H = horizon_at(h, bottom);
+  float vis;
+  st = sample_solar_t(P, F, h, sc, H, vis);
+  sky = vmax(sample_ms(P, F, h, sc, H.hc), 0.0f);
+}
+
 __device__ __forceinline__ RayGeom camera_ray_geom(const DevParams& P, float bottom, float h0, f3 ray) {
   return ray_geom(P, bottom, h0, ray.y, sqrtf(ray.x * ray.x + ray.z * ray.z));
 }
@@ -275,5 +310,24 @@ __device__ __forceinline__ f3 composite_sky(const DevParams& P, const Frame& F, 
                             height);
 }
 
+
+// The surface colour the composite reads as scene_hdr, formed in registers:
+// the pixel's surface lighting (_prepare_surface_lighting) feeding its
+// surface shading (_shade_surface), clamped at 0 as the shading writes it.
+// `pos` and `sid` are the G-buffer the shading images I also hold.
+__device__ __forceinline__ f3 shaded_scene(const DevParams& P, const Frame& F, const CompositeScalars& A,
+                                           const ShadeParams& S, const ImageLayout& L, const ShadeImages& I, int x,
+                                           int y, size_t e, int32_t sid) {
+  shading::v3 T = {0.0f, 0.0f, 0.0f}, sky = {0.0f, 0.0f, 0.0f};
+  if (sid >= 0 && S.mode == 0) {
+    f3 st, sk;
+    surface_lighting(P, F, A.cam_alt, arr3(A.right), arr3(A.up), arr3(A.fwd), ld3(I.position + e * L.channels), st,
+                     sk);
+    T = {st.x, st.y, st.z};
+    sky = {sk.x, sk.y, sk.z};
+  }
+  const shading::v3 c = shading::vmax0(shading::shade_pixel(S, L, I, x, y, int64_t(e), sid, T, sky));
+  return mk(c.x, c.y, c.z);
+}
 
 }  // namespace atm

@@ -140,16 +140,27 @@ struct SampleShaping {
   float top_fraction;      // share of aerial segments starting at the shell top
   float surface_fraction;  // share ending at an altitude in [surface_min, surface_max]
   float surface_min, surface_max;
+  float x0_lo, x0_hi;      // feature 0 (start altitude) drawn uniform in [x0_lo, x0_hi] when x0_lo < x0_hi
+  float sun_angle_fraction;  // share whose sun zenith at the start is uniform in angle in [0, sun_angle_max]
+  float sun_angle_max;       // radians
 };
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
                                const SampleShaping& shaping, const float E[3], float ar, float* features,
                                float* targets, unsigned long long* counter, cudaStream_t s);
 size_t surrogate_smem_bytes(const SurrogateNets& nets);
+// Sky radiance of every pixel: mode 0 the plain integrator per pixel, 1 the
+// sky network (plain where a gate trips; status bit 0 set on a tensor-core
+// timeout), 2 the sky-view LUT.
+cudaError_t launch_sky_pixels(int mode, const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                              const float4* tlut, const float4* mslut, const float4* svlut, const SurrogateNets& nets,
+                              uint32_t* status, float* out, unsigned long long* counter, cudaStream_t s);
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,
                                        const float4* tlut, const float4* mslut, const float4* svlut,
                                        const SurrogateNets& nets, const SurrogateQueue& Q, float* hdr,
-                                       unsigned long long* counter, int sm_count, cudaStream_t s);
+                                       unsigned long long* counter, int sm_count, cudaStream_t s,
+                                       const struct ShadeParams* shade = nullptr,
+                                       const struct ShadeImages* shade_images = nullptr);
 
 // atm_composite_noalloc: the per-device address of the file-scope tile
 // scratch (looked up on the first call on each device), its capacity in
@@ -214,6 +225,11 @@ struct ShadeImages {
   float* surface_hdr;
 };
 cudaError_t launch_shade_surface(const ShadeParams& S, const ImageLayout& L, const ShadeImages& I, cudaStream_t s);
+// The fused frame: surface lighting, shading and the COMPOSITE view per pixel
+// (I.sun_transmittance, I.sky_radiance and I.surface_hdr are not used).
+cudaError_t launch_frame(const DevParams& P, const ImageLayout& L, const CompositeScalars& A, const ShadeParams& S,
+                         const ShadeImages& I, const float* space, const float4* tlut, const float4* mslut,
+                         const float4* svlut, float* hdr, unsigned long long* sample_counter, cudaStream_t s);
 
 // Whether x is the image's contiguous axis (the orientation of its bloom planes).
 bool image_x_fast(const ImageLayout& L);

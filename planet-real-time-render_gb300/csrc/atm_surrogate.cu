@@ -127,13 +127,18 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
     const float R = S.bottom;
     float x[16];
     for (int k = 0; k < 4; ++k) x[k] = 2.0f * uniform01(seed, i, k + 1) - 1.0f;
+    if (shaping.x0_lo < shaping.x0_hi) x[0] = shaping.x0_lo + (shaping.x0_hi - shaping.x0_lo) * uniform01(seed, i, 9);
     if (kind == 1 && uniform01(seed, i, 6) < shaping.top_fraction) x[0] = 1.0f;
     // invert the feature maps
     const float h = P.top * 0.25f * (x[0] + 1.0f) * (x[0] + 1.0f);
     const float zen = sky_v_to_zenith(0.5f * (x[1] + 1.0f), sky_horizon_zenith(h, R));
     float sv, mu_v;
     sincosf(zen, &sv, &mu_v);
-    const float mu_s = sun_u_to_cosine(0.5f * (x[2] + 1.0f), h, R);
+    // the sun: uniform in the feature, or for a share uniform in zenith angle
+    // (the feature's horizon-concentrating map leaves a high sun sparse)
+    const float mu_s = uniform01(seed, i, 10) < shaping.sun_angle_fraction
+                           ? cosf(shaping.sun_angle_max * uniform01(seed, i, 11))
+                           : sun_u_to_cosine(0.5f * (x[2] + 1.0f), h, R);
     const float ss = sqrtf(mx(1.0f - mu_s * mu_s, 0.0f));
     const float cphi = x[3], sphi = sqrtf(mx(1.0f - cphi * cphi, 0.0f));
     const f3 ray = mk(sv, mu_v, 0.0f);
@@ -215,31 +220,32 @@ enum PixelKind : int { kNone = 0, kSurfMlp, kSurfPlain, kSurfEmpty, kSkyMlp, kSk
 // its accumulators at column 128 t and its activations at 128 t + 64.
 constexpr uint32_t kSurrogateTmemCols = 256;
 
-__global__ void __launch_bounds__(256, 2) k_composite_surrogate(
+// kShade: the surface colour comes from the fused surface lighting and
+// shading (shaded_scene) instead of the scene image.
+template <bool kShade>
+__global__ void __launch_bounds__(256, 3) k_composite_surrogate(
     DevParams P, ImageLayout L, CompositeScalars A, const float* __restrict__ scene, const float* __restrict__ space,
     const int32_t* __restrict__ sid, const float* __restrict__ pos, const float4* __restrict__ tlut,
     const float4* __restrict__ mslut, const float4* __restrict__ svlut, SurrogateNets nets, SurrogateQueue Q,
-    float* __restrict__ hdr) {
+    float* __restrict__ hdr, ShadeParams S, ShadeImages I) {
   extern __shared__ __align__(128) unsigned char smem[];  // the aerial network, then the sky network
-  __shared__ __align__(8) uint64_t s_mbar[2];
+  __shared__ __align__(8) uint64_t s_mbar[3];  // the two tiles' MMA completions, the weights' arrival
   __shared__ uint32_t s_tmem;
   const int wbytes = nets.ap_bytes + nets.sky_bytes;
-  for (int i = threadIdx.x * 16; i < wbytes; i += blockDim.x * 16) {
-    const unsigned char* src = i < nets.ap_bytes ? nets.ap + i : nets.sky + (i - nets.ap_bytes);
-    *reinterpret_cast<uint4*>(smem + i) = __ldg(reinterpret_cast<const uint4*>(src));
-  }
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor-core reads
-  if (threadIdx.x < 32) tc::alloc(&s_tmem, kSurrogateTmemCols);
   if (threadIdx.x == 0) {
     tc::mbar_init(&s_mbar[0], 1);
     tc::mbar_init(&s_mbar[1], 1);
+    tc::mbar_init(&s_mbar[2], 1);
     tc::mbar_init_fence();
   }
-  tc::fence_before_sync();
   __syncthreads();
-  tc::fence_after_sync();
+  // the weights arrive by bulk copy while the block computes its features
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&s_mbar[2], uint32_t(wbytes));
+    if (nets.ap_bytes > 0) tc::bulk_g2s(smem, nets.ap, uint32_t(nets.ap_bytes), &s_mbar[2]);
+    if (nets.sky_bytes > 0) tc::bulk_g2s(smem + nets.ap_bytes, nets.sky, uint32_t(nets.sky_bytes), &s_mbar[2]);
+  }
   const int tile = threadIdx.x >> 7;
-  TcTile T{s_tmem + 128u * tile, s_tmem + 128u * tile + 64u, &s_mbar[tile], 0u, tile, int(threadIdx.x & 127)};
 
   int x, y;
   const bool inside = tile_pixel(L, x, y);
@@ -294,30 +300,46 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
 
   // the networks on the tensor cores, each run by the whole block when any
   // of its pixels needs it (block-uniform: every barrier stays convergent).
+  // Tensor memory is taken only now, so that a block waiting for columns
+  // has its features done, and not at all by a block without MLP pixels.
   // tc_ok is uniform over a tile; a tile whose wait timed out issues nothing
   // more and its MLP pixels take the plain path below.
   float yv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   bool tc_ok = true;
-  if (__syncthreads_or(kind == kSurfMlp)) {
-    float t[8];
-    tc_ok = mlp_tile_tc<kSurrogateApHidden>(smem, kSurrogateApIn, T, fx, t, nets.wait_tries);
-    if (kind == kSurfMlp)
-      for (int k = 0; k < 8; ++k) yv[k] = t[k];
+  const bool need_ap = __syncthreads_or(kind == kSurfMlp);
+  const bool need_sky = __syncthreads_or(kind == kSkyMlp);
+  // the weights have arrived (each thread observes the mbarrier before any
+  // MMA of its tile reads them)
+  const bool weights_ok = __syncthreads_and(tc::mbar_wait(&s_mbar[2], 0u, kTcWaitTries));
+  if ((need_ap || need_sky) && weights_ok) {
+    if (threadIdx.x < 32) tc::alloc(&s_tmem, kSurrogateTmemCols);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    TcTile T{s_tmem + 128u * tile, s_tmem + 128u * tile + 64u, &s_mbar[tile], 0u, tile, int(threadIdx.x & 127)};
+    if (need_ap) {
+      float t[8];
+      tc_ok = mlp_tile_tc<kSurrogateApHidden>(smem, kSurrogateApIn, T, fx, t, nets.wait_tries);
+      if (kind == kSurfMlp)
+        for (int k = 0; k < 8; ++k) yv[k] = t[k];
+    }
+    if (need_sky && tc_ok) {
+      float t[8];
+      tc_ok = mlp_tile_tc<kSurrogateSkyHidden>(smem + nets.ap_bytes, kSurrogateSkyIn, T, fx, t, nets.wait_tries);
+      if (kind == kSkyMlp)
+        for (int k = 0; k < 8; ++k) yv[k] = t[k];
+    }
+    // tensor memory is freed once no MMA is in flight: a tile that timed out
+    // has exactly one commit outstanding, waited for here with the library's
+    // full bound whatever the frame's own bound was
+    tc::fence_before_sync();
+    if (!tc_ok) tc::mbar_wait(T.mbar, T.phase ^ 1u, kTcWaitTries);
+    __syncthreads();
+    tc::fence_after_sync();
+    if (threadIdx.x < 32) tc::dealloc(s_tmem, kSurrogateTmemCols);
+  } else if (need_ap || need_sky) {
+    tc_ok = false;  // the weights did not arrive in time
   }
-  if (__syncthreads_or(kind == kSkyMlp) && tc_ok) {
-    float t[8];
-    tc_ok = mlp_tile_tc<kSurrogateSkyHidden>(smem + nets.ap_bytes, kSurrogateSkyIn, T, fx, t, nets.wait_tries);
-    if (kind == kSkyMlp)
-      for (int k = 0; k < 8; ++k) yv[k] = t[k];
-  }
-  // tensor memory is freed once no MMA is in flight: a tile that timed out
-  // has exactly one commit outstanding, waited for here with the library's
-  // full bound whatever the frame's own bound was
-  tc::fence_before_sync();
-  if (!tc_ok) tc::mbar_wait(T.mbar, T.phase ^ 1u, kTcWaitTries);
-  __syncthreads();
-  tc::fence_after_sync();
-  if (threadIdx.x < 32) tc::dealloc(s_tmem, kSurrogateTmemCols);
   if (!tc_ok) {
     // the networks' outputs are not valid: the plain path for these pixels
     if (kind == kSurfMlp) kind = kSurfPlain;
@@ -328,7 +350,7 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
   bool queued = false;
   uint32_t qkind = kQueueSurface;
   if (inside && kind != kSurfPlain) {
-    f3 color = ld3(scene + o);
+    f3 color = kShade ? shaded_scene(P, F, A, S, L, I, x, y, e, sid[e]) : ld3(scene + o);
     if (kind == kSurfMlp) {
       // transmittance: the plain path's own two-tap LUT ratio (:1603-1665);
       // in-scattering: the network, ln(L / E + floor + floor_t T)
@@ -384,10 +406,11 @@ __global__ void __launch_bounds__(256, 2) k_composite_surrogate(
 // The plain integrator over the queued pixels: gated surface pixels get it
 // as their result; checked pixels compare the MLP's color (in hdr) with it,
 // then keep the plain result.  Warps take 32 entries per ticket.
+template <bool kShade>
 __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
     DevParams P, ImageLayout L, CompositeScalars A, const float* __restrict__ scene, const float* __restrict__ space,
     const float* __restrict__ pos, const float4* __restrict__ tlut, const float4* __restrict__ mslut,
-    SurrogateQueue Q, float* __restrict__ hdr, unsigned long long* counter) {
+    SurrogateQueue Q, float* __restrict__ hdr, unsigned long long* counter, ShadeParams S, ShadeImages I) {
   const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
   const int lane = threadIdx.x & 31;
   const uint32_t n = *Q.count;
@@ -403,9 +426,10 @@ __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
       const uint32_t entry = Q.items[i];
       const uint32_t kind = entry >> 30, p = entry & 0x3fffffffu;
       const int x = int(p % uint32_t(L.width)), y = int(p / uint32_t(L.width));
-      const size_t o = pix_offset(L, x, y) * L.channels;
+      const size_t e = pix_offset(L, x, y);
+      const size_t o = e * L.channels;
       const f3 ray = pixel_ray(L, A, x, y).ray;
-      f3 color = ld3(scene + o);
+      f3 color = kShade ? shaded_scene(P, F, A, S, L, I, x, y, e, I.surface_id[e]) : ld3(scene + o);
       if (kind == kQueueSkyCheck) {
         const f3 sky = sky_radiance(P, F, A.cam_alt, ray);
         samples += uint32_t(P.sv_steps);
@@ -446,7 +470,120 @@ __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
   }
 }
 
+// Sky radiance of every pixel of a frame, the pixel's own view ray from the
+// camera (the learned sky-view workload; the G-buffer is not read):
+//  * kSkyPixelsPlain: the plain integrator per pixel - the sky-view march of
+//    :1208-1302 (sv_steps warped segments) along the pixel's ray;
+//  * kSkyPixelsNet: the sky network on the tensor cores; where a gate trips
+//    (|sun cosine| at the camera below sky_twilight_cos, the view ray within
+//    limb_rad of the limb, the camera above the shell) the plain integrator;
+//  * kSkyPixelsLut: the reference's own path, a bilinear tap of the sky-view
+//    LUT (:1474-1525).
+// 256 threads = two 128-pixel tiles, as in k_composite_surrogate.
+enum : int { kSkyPixelsPlain = 0, kSkyPixelsNet = 1, kSkyPixelsLut = 2 };
+template <int kMode>
+__global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout L, CompositeScalars A,
+                                                       const float4* __restrict__ tlut,
+                                                       const float4* __restrict__ mslut,
+                                                       const float4* __restrict__ svlut, SurrogateNets nets,
+                                                       uint32_t* __restrict__ status, float* __restrict__ out,
+                                                       unsigned long long* counter) {
+  extern __shared__ __align__(128) unsigned char smem[];  // the sky network (kSkyPixelsNet)
+  __shared__ __align__(8) uint64_t s_mbar[3];
+  __shared__ uint32_t s_tmem;
+  if (kMode == kSkyPixelsNet) {
+    if (threadIdx.x == 0) {
+      tc::mbar_init(&s_mbar[0], 1);
+      tc::mbar_init(&s_mbar[1], 1);
+      tc::mbar_init(&s_mbar[2], 1);
+      tc::mbar_init_fence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc::mbar_arrive_expect_tx(&s_mbar[2], uint32_t(nets.sky_bytes));
+      tc::bulk_g2s(smem, nets.sky, uint32_t(nets.sky_bytes), &s_mbar[2]);
+    }
+  }
+  int x, y;
+  const bool inside = tile_pixel(L, x, y);
+  const int cx = inside ? x : 0, cy = inside ? y : 0;
+  const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+  const f3 ray = pixel_ray(L, A, cx, cy).ray;
+  uint32_t samples = 0;
+  f3 sky = splat(0.0f);
+  bool plain = kMode == kSkyPixelsPlain;
+  if (kMode == kSkyPixelsLut) sky = sample_sky_view(P, svlut, ray, F.sun, A.sky_alt, A.bottom);
+  if (kMode == kSkyPixelsNet) {
+    const bool near_limb =
+        fabsf(acosf(clampf(ray.y, -1.0f, 1.0f)) - sky_horizon_zenith(A.cam_alt, A.bottom)) < nets.limb_rad;
+    const bool net = inside && A.cam_alt <= P.top && fabsf(F.sun.y) >= nets.sky_twilight_cos && !near_limb;
+    plain = !net;
+    float fx[16] = {};
+    if (net) {
+      const float vl = sqrtf(ray.x * ray.x + ray.z * ray.z), sl = sqrtf(F.sun.x * F.sun.x + F.sun.z * F.sun.z);
+      const float cphi = (vl > 1e-6f && sl > 1e-6f) ? (ray.x * F.sun.x + ray.z * F.sun.z) / (vl * sl) : 1.0f;
+      geometry_features(P, A.bottom, A.cam_alt, ray.y, F.sun.y, cphi, fx);
+      fx[4] = nets.lhr_n;
+      fx[5] = nets.lhm_n;
+      sky_ray_features(P, A.bottom, A.cam_alt, ray, F.sun, fx);
+    }
+    const bool need = __syncthreads_or(net);
+    const bool weights_ok = __syncthreads_and(tc::mbar_wait(&s_mbar[2], 0u, kTcWaitTries));
+    bool tc_ok = weights_ok;
+    float yv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (need && weights_ok) {
+      if (threadIdx.x < 32) tc::alloc(&s_tmem, kSurrogateTmemCols);
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      const int tile = threadIdx.x >> 7;
+      TcTile T{s_tmem + 128u * tile, s_tmem + 128u * tile + 64u, &s_mbar[tile], 0u, tile, int(threadIdx.x & 127)};
+      tc_ok = mlp_tile_tc<kSurrogateSkyHidden>(smem, kSurrogateSkyIn, T, fx, yv, nets.wait_tries);
+      tc::fence_before_sync();
+      if (!tc_ok) tc::mbar_wait(T.mbar, T.phase ^ 1u, kTcWaitTries);
+      __syncthreads();
+      tc::fence_after_sync();
+      if (threadIdx.x < 32) tc::dealloc(s_tmem, kSurrogateTmemCols);
+    }
+    if (need && !tc_ok) {
+      plain = true;  // the network's outputs are not valid: the plain integrator
+      if ((threadIdx.x & 127) == 0) atomicOr(status, 1u);
+    } else if (net) {
+      sky = net_radiance(yv, A.E, splat(nets.sky_floor));
+    }
+  }
+  if (inside) {
+    if (plain) {
+      sky = sky_radiance(P, F, A.cam_alt, ray);
+      samples = uint32_t(P.sv_steps);
+    }
+    const size_t o = pix_offset(L, x, y) * L.channels;
+    out[o + 0] = sky.x;
+    out[o + 1] = sky.y;
+    out[o + 2] = sky.z;
+  }
+  warp_count(samples, counter);
+}
+
 }  // namespace
+
+cudaError_t launch_sky_pixels(int mode, const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
+                              const float4* tlut, const float4* mslut, const float4* svlut, const SurrogateNets& nets,
+                              uint32_t* status, float* out, unsigned long long* counter, cudaStream_t s) {
+  const dim3 grid((L.width + 15) / 16, (L.height + 15) / 16);
+  if (mode == kSkyPixelsNet) {
+    cudaError_t e = cudaFuncSetAttribute(k_sky_pixels<kSkyPixelsNet>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         nets.sky_bytes);
+    if (e != cudaSuccess) return e;
+    k_sky_pixels<kSkyPixelsNet><<<grid, 256, nets.sky_bytes, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out,
+                                                                  counter);
+  } else if (mode == kSkyPixelsLut) {
+    k_sky_pixels<kSkyPixelsLut><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter);
+  } else {
+    k_sky_pixels<kSkyPixelsPlain><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter);
+  }
+  return cudaGetLastError();
+}
 
 cudaError_t launch_gen_samples(const SurrogateSetDev* sets, int n_sets, int kind, long long n, unsigned long long seed,
                                const SampleShaping& shaping, const float E[3], float ar, float* features,
@@ -463,17 +600,33 @@ cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,
                                        const float4* tlut, const float4* mslut, const float4* svlut,
                                        const SurrogateNets& nets, const SurrogateQueue& Q, float* hdr,
-                                       unsigned long long* counter, int sm_count, cudaStream_t s) {
+                                       unsigned long long* counter, int sm_count, cudaStream_t s,
+                                       const ShadeParams* shade, const ShadeImages* shade_images) {
   cudaError_t e = cudaMemsetAsync(Q.count, 0, 2 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
   const int smem = int(surrogate_smem_bytes(nets));
-  e = cudaFuncSetAttribute(k_composite_surrogate, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
   const dim3 grid((L.width + 15) / 16, (L.height + 15) / 16);
-  k_composite_surrogate<<<grid, 256, smem, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, nets, Q, hdr);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_surrogate_fallback<<<2 * sm_count, 256, 0, s>>>(P, L, A, scene, space, pos, tlut, mslut, Q, hdr, counter);
+  const ShadeParams S = shade ? *shade : ShadeParams{};
+  const ShadeImages I = shade_images ? *shade_images : ShadeImages{};
+  if (shade) {
+    e = cudaFuncSetAttribute(k_composite_surrogate<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_composite_surrogate<true><<<grid, 256, smem, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, nets, Q,
+                                                        hdr, S, I);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_surrogate_fallback<true><<<2 * sm_count, 256, 0, s>>>(P, L, A, scene, space, pos, tlut, mslut, Q, hdr, counter,
+                                                            S, I);
+  } else {
+    e = cudaFuncSetAttribute(k_composite_surrogate<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_composite_surrogate<false><<<grid, 256, smem, s>>>(P, L, A, scene, space, sid, pos, tlut, mslut, svlut, nets,
+                                                         Q, hdr, S, I);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_surrogate_fallback<false><<<2 * sm_count, 256, 0, s>>>(P, L, A, scene, space, pos, tlut, mslut, Q, hdr,
+                                                             counter, S, I);
+  }
   return cudaGetLastError();
 }
 

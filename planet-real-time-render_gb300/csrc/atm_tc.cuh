@@ -99,6 +99,23 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, int m
   return false;
 }
 
+// Arrival of the calling thread that also expects `bytes` of transactions.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+               : "memory");
+}
+
+// ---- bulk copy (the TMA engine's untiled form) -----------------------------------
+// global -> this CTA's shared memory; completes `bytes` of transactions on
+// mbar.  Both addresses 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(static_cast<uint64_t>(__cvta_generic_to_global(src))), "r"(bytes), "r"(smem_addr(mbar))
+      : "memory");
+}
+
 // ---- tensor-memory loads and stores (32 lanes x 32 bit per warp) ----------------
 __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];

@@ -147,6 +147,10 @@ class AtmSampleOptions(ctypes.Structure):
         ("surface_fraction", ctypes.c_double),
         ("surface_min_m", ctypes.c_double),
         ("surface_max_m", ctypes.c_double),
+        ("start_min_m", ctypes.c_double),
+        ("start_max_m", ctypes.c_double),
+        ("sun_angle_fraction", ctypes.c_double),
+        ("sun_angle_max_degrees", ctypes.c_double),
     ]
 
 
@@ -171,6 +175,7 @@ class AtmSurrogate(ctypes.Structure):
     ]
 
 
+ATM_SKY_PIXELS_PLAIN, ATM_SKY_PIXELS_NET, ATM_SKY_PIXELS_LUT = 0, 1, 2
 ATM_SURROGATE_SKY = 0
 ATM_SURROGATE_AERIAL = 1
 
@@ -246,6 +251,8 @@ SIGNATURES = {
     "atm_load_lut": (ctypes.c_int, [_P, _I32, _P, _P]),
     "atm_read_sample_counter": (ctypes.c_int, [_P, _I32, ctypes.POINTER(ctypes.c_uint64), _P]),
     "atm_check": (ctypes.c_int, [_P, _P]),
+    "atm_sky_pixels": (ctypes.c_int, [_P, _I32, _P, ctypes.POINTER(AtmImage), _D, _D, c_double3, c_double3, _D,
+                                      c_double9, _D, ctypes.POINTER(AtmSurrogate), _P]),
     "atm_batch_create": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), ctypes.POINTER(ctypes.c_double), _I32, c_double3, _D, ctypes.POINTER(_P), _P],
@@ -281,6 +288,11 @@ SIGNATURES = {
     "atm_post_read_bloom": (ctypes.c_int, [_P, ctypes.POINTER(_I32), _P, _P]),
     "atm_shade_surface": (ctypes.c_int, [ctypes.POINTER(AtmShadeParams), ctypes.POINTER(AtmShadeImages),
                                          ctypes.POINTER(AtmImage), _P]),
+    "atm_render_frame": (
+        ctypes.c_int,
+        [_P, ctypes.POINTER(AtmShadeParams), ctypes.POINTER(AtmShadeImages), _P, _P, ctypes.POINTER(AtmImage), _D, _D,
+         c_double3, c_double3, c_double3, _D, c_double9, _D, _D, _D, ctypes.POINTER(AtmSurrogate), _P],
+    ),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,

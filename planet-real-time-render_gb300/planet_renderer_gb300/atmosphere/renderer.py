@@ -176,7 +176,7 @@ class AtmosphereRenderer:
         return int(self._state().aerial_rebuilds)
 
     # ---- images ------------------------------------------------------------
-    def _image(self, floats: list[torch.Tensor], ids: torch.Tensor) -> _native.AtmImage:
+    def _image(self, floats: list[torch.Tensor], ids: torch.Tensor | None) -> _native.AtmImage:
         img = None
         for t in floats:
             if not isinstance(t, torch.Tensor) or t.device != self.device or t.dtype != torch.float32:
@@ -195,6 +195,8 @@ class AtmosphereRenderer:
                 img = this
             elif this != img:
                 raise ValueError("all images of one call must share shape, strides and channels")
+        if ids is None:  # a call without a G-buffer
+            return _native.AtmImage(img[0], img[1], img[2], img[3], img[4])
         if not isinstance(ids, torch.Tensor) or ids.device != self.device or ids.dtype != torch.int32:
             raise ValueError("surface_id must be an int32 CUDA tensor on the renderer's device")
         id_strides = (ids.stride(0), ids.stride(1)) if self.layout == "wh" else (ids.stride(1), ids.stride(0))
@@ -266,7 +268,8 @@ class AtmosphereRenderer:
         if stats is not None and (stats.device != self.device or stats.dtype != torch.float32 or stats.numel() < 8):
             raise ValueError("stats must be a float32 tensor of 8 elements on the renderer's device")
         sg = surrogate.native(check_fraction=check_fraction, seed=seed,
-                              stats=None if stats is None else stats.data_ptr())
+                              stats=None if stats is None else stats.data_ptr(),
+                              camera_altitude_m=float(camera_radius_m) - float(planet_radius_m))
         _native.check(self._lib.atm_composite_surrogate(
             self._handle, ctypes.c_void_p(scene_hdr.data_ptr()), ctypes.c_void_p(space_hdr.data_ptr()),
             ctypes.c_void_p(surface_id.data_ptr()), ctypes.c_void_p(position_view.data_ptr()),
@@ -293,6 +296,70 @@ class AtmosphereRenderer:
         a.frame_width, a.frame_height = self.width, self.height
         _native.check(self._lib.atm_build_lut(self._handle, _KINDS[kind], ctypes.byref(a),
                                               _stream_handle(self.device)))
+
+    def render_frame(self, gbuffer: dict, space_hdr, hdr, planet_radius_m: float, camera_radius_m: float,
+                     sun_local, solar_irradiance, sun_disk_radiance, sun_angular_radius_degrees: float, view_basis,
+                     tangent_half_fov: float, star_contrast_start: float, star_contrast_end: float, *,
+                     sun_global=None, view_basis_global=None, ocean=None, shade_mode: int = 0,
+                     ocean_surface_id: int | None = None, surrogate=None, stats: torch.Tensor | None = None,
+                     check_fraction: float = 0.01, seed: int = 0) -> None:
+        """``prepare_frame`` -> surface shading -> ``composite`` (COMPOSITE
+        view) in one pass over the pixels, the surface lighting and shaded
+        colour of each pixel kept in registers (``atm_render_frame``).
+        ``gbuffer`` holds the shading's G-buffer and terrain-snapshot images
+        (``shading.GBUFFER_IMAGES``; ``position`` and ``surface_id`` are the
+        composite's ``position_view`` and ``surface_id``).  ``sun_global`` and
+        ``view_basis_global`` default to the local ones (a global frame equal
+        to the camera's local frame).  With ``surrogate`` the composite is
+        ``composite_surrogate``'s.  The aerial volume and the public surface
+        lighting images are not updated."""
+
+        from .. import shading
+
+        ocean = ocean or shading.OceanShading()
+        names = shading.GBUFFER_IMAGES
+        p, ptrs, image = shading.shade_arguments(
+            gbuffer, hdr, sun_local if sun_global is None else sun_global, solar_irradiance,
+            view_basis if view_basis_global is None else view_basis_global, ocean,
+            math.radians(sun_angular_radius_degrees), tangent_half_fov, shade_mode, self.layout,
+            shading.OCEAN_SURFACE_ID if ocean_surface_id is None else ocean_surface_id, names=names)
+        img = self._image([space_hdr, hdr, gbuffer["position"]], gbuffer["surface_id"])
+        if (img.width, img.height) != (image.width, image.height):
+            raise ValueError("images must have the renderer's frame shape")
+        sg = None
+        if surrogate is not None:
+            if stats is not None and (stats.device != self.device or stats.dtype != torch.float32
+                                      or stats.numel() < 8):
+                raise ValueError("stats must be a float32 tensor of 8 elements on the renderer's device")
+            sg = surrogate.native(check_fraction=check_fraction, seed=seed,
+                                  stats=None if stats is None else stats.data_ptr(),
+                                  camera_altitude_m=float(camera_radius_m) - float(planet_radius_m))
+        _native.check(self._lib.atm_render_frame(
+            self._handle, ctypes.byref(p), ctypes.byref(ptrs), ctypes.c_void_p(space_hdr.data_ptr()),
+            ctypes.c_void_p(hdr.data_ptr()), ctypes.byref(img), float(planet_radius_m), float(camera_radius_m),
+            _native.d3(sun_local), _native.d3(solar_irradiance), _native.d3(sun_disk_radiance),
+            float(sun_angular_radius_degrees), _native.d9(view_basis), float(tangent_half_fov),
+            float(star_contrast_start), float(star_contrast_end), None if sg is None else ctypes.byref(sg),
+            _stream_handle(self.device)))
+
+    def sky_pixels(self, radiance, planet_radius_m: float, camera_radius_m: float, sun_local, solar_irradiance,
+                   sun_angular_radius_degrees: float, view_basis, tangent_half_fov: float, mode: str = "plain",
+                   surrogate=None) -> None:
+        """Sky radiance along every pixel's view ray into ``radiance``
+        (``(W, H, 3|4)`` float32, the renderer's layout): ``mode`` "plain" the
+        sky-view march per pixel, "net" the sky network of ``surrogate`` with
+        the plain march where a gate trips, "lut" the sky-view LUT of the last
+        ``update``."""
+
+        code = {"plain": _native.ATM_SKY_PIXELS_PLAIN, "net": _native.ATM_SKY_PIXELS_NET,
+                "lut": _native.ATM_SKY_PIXELS_LUT}[mode]
+        img = self._image([radiance], None)
+        sg = None if surrogate is None else surrogate.native(check_fraction=0.0)
+        _native.check(self._lib.atm_sky_pixels(
+            self._handle, code, ctypes.c_void_p(radiance.data_ptr()), ctypes.byref(img), float(planet_radius_m),
+            float(camera_radius_m), _native.d3(sun_local), _native.d3(solar_irradiance),
+            float(sun_angular_radius_degrees), _native.d9(view_basis), float(tangent_half_fov),
+            None if sg is None else ctypes.byref(sg), _stream_handle(self.device)))
 
     def check(self) -> None:
         """Synchronise the stream and raise the device-side errors of earlier

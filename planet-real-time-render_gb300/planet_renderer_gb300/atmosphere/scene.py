@@ -237,3 +237,41 @@ def synthesize_gbuffer(width: int, height: int, planet_radius_m: float, camera_a
     if pixels is None:
         out = {k: v.reshape((width, height) + tuple(v.shape[1:])) for k, v in out.items()}
     return out
+
+
+def shading_inputs(gbuffer: dict, planet_radius_m: float, camera_altitude_m: float, basis,
+                   ocean_surface_id: int = 2_147_000_000) -> dict[str, torch.Tensor]:
+    """Land-and-ocean surface-shading inputs for a G-buffer of
+    :func:`synthesize_gbuffer` (the images ``shading.shade_surface`` reads
+    besides the surface lighting).  The global frame is the camera's local
+    frame.  The sea level is the median radius of the frame's hits: hits
+    below it are ocean (``ocean_surface_id``; water depth = how far below),
+    the rest land, so about half the surface takes the ocean BRDF.  Normals
+    are radial; the terrain snapshot is the hit surface itself.  A timing
+    and fusion workload, not a terrain model."""
+
+    pos = gbuffer["position_view"]
+    sid = gbuffer["surface_id"]
+    device = pos.device
+    right, up, forward = (torch.as_tensor(v, dtype=torch.float32, device=device) for v in basis)
+    local = pos[..., 0:1] * right + pos[..., 1:2] * up + pos[..., 2:3] * forward
+    local[..., 1] += float(planet_radius_m + camera_altitude_m)
+    radius = torch.linalg.norm(local.double(), dim=-1)
+    normal = (local.double() / radius[..., None].clamp_min(1.0)).float()
+    hit = sid >= 0
+    sea = torch.median(radius[hit]) if bool(hit.any()) else torch.tensor(float(planet_radius_m), device=device)
+    depth = (sea - radius).float().clamp_min(0.0)
+    ocean = hit & (depth > 0.0)
+    one = torch.ones_like(pos[..., :1])
+    land_albedo = torch.tensor([0.16, 0.20, 0.12], device=device) * one
+    ocean_albedo = torch.tensor([0.02, 0.05, 0.08], device=device) * one
+    albedo = torch.where(ocean[..., None], ocean_albedo, land_albedo)
+    surface_id = torch.where(ocean, torch.full_like(sid, ocean_surface_id), sid)
+    return {
+        "position": pos, "normal": normal, "albedo": albedo,
+        "water_depth": torch.where(ocean, depth, torch.zeros_like(depth)).contiguous(),
+        "seabed_albedo": torch.tensor([0.30, 0.28, 0.20], device=device) * one, "seabed_normal": normal,
+        "slope_variance": torch.full_like(depth, 0.01), "surface_id": surface_id.contiguous(),
+        "terrain_position": pos, "terrain_normal": normal, "terrain_albedo": land_albedo.contiguous(),
+        "terrain_surface_id": torch.where(hit, torch.zeros_like(sid), sid).contiguous(),
+    }

@@ -70,6 +70,15 @@ class TargetSpec:
     # where every surface pixel's segment ends
     shell_top_fraction: float = 0.0
     surface_fraction: float = 0.0
+    # aerial/sky sample shaping: segments start at an altitude inside this
+    # band (m) - a network specialised to the cameras of that band - or
+    # anywhere in the shell when None
+    start_range_m: tuple | None = None
+    # share of samples with the sun's zenith at the start uniform in angle in
+    # [0, sun_angle_max_degrees] (the sun feature's map concentrates samples
+    # on the horizon and leaves a high sun sparse)
+    sun_angle_fraction: float = 0.0
+    sun_angle_max_degrees: float = 100.0
 
 
 # Aerial defaults from frames against FP64 (three cameras, 2 km - 2000 km):
@@ -151,18 +160,23 @@ class SampleSource:
         self.device = self.builder.device
 
     def samples(self, kind: int, n: int, seed: int, shell_top_fraction: float = 0.0, surface_fraction: float = 0.0,
-                surface_range_m=SURFACE_RANGE_M):
+                surface_range_m=SURFACE_RANGE_M, start_range_m=None, sun_angle=(0.0, 100.0)):
         """(features, targets) of n samples.  Aerial samples: a share
         ``shell_top_fraction`` starts at the shell top (feature 0 = 1) and a
         share ``surface_fraction`` ends at an altitude uniform in
-        ``surface_range_m``; the rest is uniform over the input box."""
+        ``surface_range_m``; the rest is uniform over the input box.
+        ``start_range_m`` (lo, hi) confines the start altitudes to that band
+        (uniform in the altitude feature); ``sun_angle`` (share, max degrees)
+        draws that share of the sun zeniths uniform in angle."""
 
         n_in, _, n_out = SHAPES[kind]
         x = torch.empty((n, n_in), dtype=torch.float32, device=self.device)
         y = torch.empty((n, n_out), dtype=torch.float32, device=self.device)
         rng = (ctypes.c_double * 4)(*self.scale_height_range)
+        lo, hi = start_range_m if start_range_m is not None else (0.0, 0.0)
         opts = _native.AtmSampleOptions(float(shell_top_fraction), float(surface_fraction), float(surface_range_m[0]),
-                                        float(surface_range_m[1]))
+                                        float(surface_range_m[1]), float(lo), float(hi), float(sun_angle[0]),
+                                        float(sun_angle[1]))
         _native.check(self.builder._lib.atm_surrogate_samples(
             self.builder._handle, int(kind), int(n), int(seed) & (2**64 - 1), ctypes.byref(opts), rng,
             ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(y.data_ptr()), self.builder._stream()))
@@ -237,7 +251,9 @@ def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 
 
     spec = spec or DEFAULT_SPECS[kind]
     n_in, n_hidden, n_out = SHAPES[kind]
-    x, y = source.samples(kind, n_samples, seed, spec.shell_top_fraction, spec.surface_fraction)
+    x, y = source.samples(kind, n_samples, seed, spec.shell_top_fraction, spec.surface_fraction,
+                          start_range_m=spec.start_range_m,
+                          sun_angle=(spec.sun_angle_fraction, spec.sun_angle_max_degrees))
     t = to_targets(kind, y, spec)
     w = loss_weights(kind, y, spec)
     del y
@@ -270,11 +286,13 @@ def train(source: SampleSource, kind: int, n_samples: int = 2**22, batch: int = 
     net.pack()
     # held-out: the input box (segments starting at the shell top where the
     # network serves only those), and segments ending at a surface
-    xh, yh = source.samples(kind, held_out, seed + 7919, 1.0 if spec.shell_top_fraction >= 1.0 else 0.0)
+    xh, yh = source.samples(kind, held_out, seed + 7919, 1.0 if spec.shell_top_fraction >= 1.0 else 0.0,
+                            start_range_m=spec.start_range_m)
     report.held_out = {"bf16": held_out_error(net, kind, xh, yh, spec, "bf16"),
                        "f32": held_out_error(net, kind, xh, yh, spec, "f32")}
     if kind == AERIAL and spec.surface_fraction > 0.0:  # segments ending at a surface, as the frame's
-        xs, ys = source.samples(kind, held_out, seed + 7921, spec.shell_top_fraction, 1.0)
+        xs, ys = source.samples(kind, held_out, seed + 7921, spec.shell_top_fraction, 1.0,
+                                start_range_m=spec.start_range_m)
         report.held_out["bf16_surface"] = held_out_error(net, kind, xs, ys, spec, "bf16")
     report.spec = spec
     return net, report
@@ -289,16 +307,29 @@ class Surrogate:
     def __init__(self, aerial: Mlp | None, sky: Mlp | None, planet_radius_m: float = EARTH_RADIUS_M,
                  top_altitude_m: float = 100_000.0, scale_height_range=SCALE_HEIGHT_RANGE,
                  aerial_spec: TargetSpec | None = None, sky_spec: TargetSpec | None = None,
-                 aerial_above_shell: Mlp | None = None):
+                 aerial_above_shell: Mlp | None = None, aerial_bands=()):
         self.aerial, self.sky, self.aerial_above_shell = aerial, sky, aerial_above_shell
+        # (highest camera altitude in m, network) pairs, ascending: a camera
+        # inside the shell uses the first band that reaches its altitude
+        # (a network trained on segments starting in that band), else aerial
+        self.aerial_bands = sorted(((float(a), net) for a, net in aerial_bands), key=lambda b: b[0])
         self.planet_radius_m = float(planet_radius_m)
         self.top_altitude_m = float(top_altitude_m)
         self.scale_height_range = tuple(float(v) for v in scale_height_range)
         self.aerial_spec = aerial_spec or DEFAULT_SPECS[AERIAL]
         self.sky_spec = sky_spec or DEFAULT_SPECS[SKY]
-        for net in (aerial, sky, aerial_above_shell):
+        for net in (aerial, sky, aerial_above_shell, *(n for _, n in self.aerial_bands)):
             if net is not None:
                 net.pack()
+
+    def aerial_for(self, camera_altitude_m: float | None):
+        """The aerial network for a camera inside the shell at this altitude."""
+
+        if camera_altitude_m is not None:
+            for top, net in self.aerial_bands:
+                if camera_altitude_m <= top:
+                    return net
+        return self.aerial
 
     # gates -> plain path: |sun cosine| below twilight_cosine at a surface
     # segment's start, middle or end (measured: the aerial network's frame
@@ -312,9 +343,11 @@ class Surrogate:
     # (every wait gives up at once, the MLP pixels take the plain path)
     tc_wait_polls = 0
 
-    def native(self, check_fraction: float = 0.01, seed: int = 0, stats=None) -> _native.AtmSurrogate:
+    def native(self, check_fraction: float = 0.01, seed: int = 0, stats=None,
+               camera_altitude_m: float | None = None) -> _native.AtmSurrogate:
         s = _native.AtmSurrogate()
-        s.aerial = self.aerial.handle.value if self.aerial is not None else None
+        aerial = self.aerial_for(camera_altitude_m)
+        s.aerial = aerial.handle.value if aerial is not None else None
         s.sky = self.sky.handle.value if self.sky is not None else None
         s.aerial_above_shell = self.aerial_above_shell.handle.value if self.aerial_above_shell is not None else None
         s.scale_height_range[:] = list(self.scale_height_range)

@@ -26,6 +26,10 @@ FLOAT_IMAGES = ("position", "normal", "albedo", "seabed_albedo", "seabed_normal"
                 "terrain_normal", "terrain_albedo")
 SCALAR_IMAGES = ("water_depth", "slope_variance")
 ID_IMAGES = ("surface_id", "terrain_surface_id")
+# the G-buffer and terrain-snapshot images of a shading call (the rest of
+# _native.SHADE_IMAGES are the surface lighting and the output)
+GBUFFER_IMAGES = ("position", "normal", "albedo", "water_depth", "seabed_albedo", "seabed_normal", "slope_variance",
+                  "surface_id", "terrain_position", "terrain_normal", "terrain_albedo", "terrain_surface_id")
 
 
 @dataclass(frozen=True)
@@ -52,33 +56,32 @@ def _element_strides(t: torch.Tensor, per_element: int, layout: str) -> tuple:
     return sx // per_element, sy // per_element
 
 
-def shade_surface(gbuffer: dict, sun_transmittance: torch.Tensor, sky_radiance: torch.Tensor,
-                  surface_hdr: torch.Tensor, sun_global, solar_irradiance, view_basis_global,
-                  ocean: OceanShading, sun_angular_radius: float, tangent_half_fov: float, mode: int = 0,
-                  layout: str = "wh", ocean_surface_id: int = OCEAN_SURFACE_ID) -> None:
-    """_shade_surface (renderer.py:1277-1575) into ``surface_hdr``.  ``gbuffer``
-    holds the G-buffer and terrain-snapshot images named as in
-    ``_native.SHADE_IMAGES``; ``view_basis_global`` the camera's right, up and
-    forward directions in the global frame; ``sun_angular_radius`` radians."""
+def shade_arguments(images: dict, ref: torch.Tensor, sun_global, solar_irradiance, view_basis_global,
+                    ocean: OceanShading, sun_angular_radius: float, tangent_half_fov: float, mode: int = 0,
+                    layout: str = "wh", ocean_surface_id: int = OCEAN_SURFACE_ID, names=None):
+    """Checked native arguments of a shading call: (AtmShadeParams,
+    AtmShadeImages, AtmImage).  ``images`` maps the names of ``names``
+    (default: every image of ``_native.SHADE_IMAGES``) to tensors sharing
+    ``ref``'s frame shape, channels and strides; images left out of ``names``
+    are passed as null."""
 
     if layout not in ("wh", "hw"):
         raise ValueError("layout must be 'wh' (Taichi field layout) or 'hw'")
-    images = dict(gbuffer, sun_transmittance=sun_transmittance, sky_radiance=sky_radiance, surface_hdr=surface_hdr)
-    missing = [n for n in _native.SHADE_IMAGES if n not in images]
+    names = tuple(names or _native.SHADE_IMAGES)
+    missing = [n for n in names if n not in images]
     if missing:
         raise ValueError(f"missing images: {missing}")
-    ref = images["surface_hdr"]
     if not isinstance(ref, torch.Tensor) or ref.dim() != 3 or ref.shape[2] not in (3, 4) or ref.stride(2) != 1:
-        raise ValueError("surface_hdr must be a float32 CUDA tensor (W, H, 3|4) with contiguous channels")
+        raise ValueError("the frame's images must be float32 CUDA tensors (W, H, 3|4) with contiguous channels")
     channels = int(ref.shape[2])
     dims = (int(ref.shape[0]), int(ref.shape[1])) if layout == "wh" else (int(ref.shape[1]), int(ref.shape[0]))
     strides = _element_strides(ref, channels, layout)
-    for name in _native.SHADE_IMAGES:
+    for name in names:
         t = images[name]
         scalar = name in SCALAR_IMAGES or name in ID_IMAGES
         dtype = torch.int32 if name in ID_IMAGES else torch.float32
         if not isinstance(t, torch.Tensor) or t.device != ref.device or t.dtype != dtype:
-            raise ValueError(f"{name} must be a {dtype} CUDA tensor on surface_hdr's device")
+            raise ValueError(f"{name} must be a {dtype} CUDA tensor on the frame's device")
         shape = tuple(t.shape[:2]) if layout == "wh" else (int(t.shape[1]), int(t.shape[0]))
         if t.dim() != (2 if scalar else 3) or shape != dims:
             raise ValueError(f"{name} must have the frame's shape")
@@ -86,7 +89,7 @@ def shade_surface(gbuffer: dict, sun_transmittance: torch.Tensor, sky_radiance: 
             if _element_strides(t, 1, layout) != strides:
                 raise ValueError(f"{name} must share the images' element strides")
         elif t.shape[2] != channels or t.stride(2) != 1 or _element_strides(t, channels, layout) != strides:
-            raise ValueError(f"{name} must share surface_hdr's channels and strides")
+            raise ValueError(f"{name} must share the frame's channels and strides")
     p = _native.AtmShadeParams()
     p.sun_global[:] = [float(v) for v in sun_global]
     p.solar_irradiance[:] = [float(v) for v in solar_irradiance]
@@ -108,8 +111,23 @@ def shade_surface(gbuffer: dict, sun_transmittance: torch.Tensor, sky_radiance: 
     p.sun_angular_radius = float(sun_angular_radius)
     p.tangent_half_fov = float(tangent_half_fov)
     p.ocean_surface_id = int(ocean_surface_id)
-    ptrs = _native.AtmShadeImages(*[ctypes.c_void_p(images[n].data_ptr()) for n in _native.SHADE_IMAGES])
-    image = _native.AtmImage(dims[0], dims[1], strides[0], strides[1], channels)
+    ptrs = _native.AtmShadeImages(*[ctypes.c_void_p(images[n].data_ptr() if n in names else None)
+                                    for n in _native.SHADE_IMAGES])
+    return p, ptrs, _native.AtmImage(dims[0], dims[1], strides[0], strides[1], channels)
+
+
+def shade_surface(gbuffer: dict, sun_transmittance: torch.Tensor, sky_radiance: torch.Tensor,
+                  surface_hdr: torch.Tensor, sun_global, solar_irradiance, view_basis_global,
+                  ocean: OceanShading, sun_angular_radius: float, tangent_half_fov: float, mode: int = 0,
+                  layout: str = "wh", ocean_surface_id: int = OCEAN_SURFACE_ID) -> None:
+    """_shade_surface (renderer.py:1277-1575) into ``surface_hdr``.  ``gbuffer``
+    holds the G-buffer and terrain-snapshot images named as in
+    ``_native.SHADE_IMAGES``; ``view_basis_global`` the camera's right, up and
+    forward directions in the global frame; ``sun_angular_radius`` radians."""
+
+    images = dict(gbuffer, sun_transmittance=sun_transmittance, sky_radiance=sky_radiance, surface_hdr=surface_hdr)
+    p, ptrs, image = shade_arguments(images, surface_hdr, sun_global, solar_irradiance, view_basis_global, ocean,
+                                     sun_angular_radius, tangent_half_fov, mode, layout, ocean_surface_id)
     lib = _native.library()
     _native.check(lib.atm_shade_surface(ctypes.byref(p), ctypes.byref(ptrs), ctypes.byref(image),
-                                        ctypes.c_void_p(torch.cuda.current_stream(ref.device).cuda_stream)))
+                                        ctypes.c_void_p(torch.cuda.current_stream(surface_hdr.device).cuda_stream)))

@@ -1,6 +1,9 @@
 """Generate golden vectors by running the reference's own atmosphere code.
 
-    python tests/golden/make_golden.py [--reference PATH] [--only NAME ...]
+    python tests/golden/make_golden.py --reference PATH [--only NAME ...]
+
+PATH is the root of a checkout of the reference project (the directory that
+holds ``src/planet_renderer``).
 
 Imports ``planet_renderer.atmosphere`` from the reference checkout with the
 float32 Taichi stand-in of ``taichi_f32_shim.py`` installed as ``taichi``, and
@@ -438,7 +441,8 @@ def earth_config1_kwargs():
 
 def main() -> None:
     parser = argparse.ArgumentParser()
-    parser.add_argument("--reference", type=Path, default=Path("/root/reference"))
+    parser.add_argument("--reference", type=Path, required=True,
+                        help="root of the reference checkout (holds src/planet_renderer)")
     parser.add_argument("--only", nargs="*")
     parser.add_argument("--precision", choices=("f32", "f64"), default="f32",
                         help="f64 runs the same reference source in double (tiny scenarios only)")

@@ -380,3 +380,111 @@ def test_surrogate_frame_gains_over_the_plain_integrator(trained):
                                               hdr, *args, surrogate=sg, check_fraction=0.01, seed=1))
     assert plain / mlp > 2.0, (plain, mlp)
     r.close()
+
+
+# ---- the learned sky-view workload: sky radiance of every pixel ---------------------
+def _sky_frame(width=320, height=180, altitude_m=2000.0, zenith_deg=40.0, pitch_deg=15.0):
+    from planet_renderer_gb300 import camera
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.workloads import EARTH_RADIUS_M
+
+    r = AtmosphereRenderer(width, height, earth_baseline())
+    sun = camera.sun_from_zenith(zenith_deg, 30.0)
+    basis = camera.view_basis(0.0, pitch_deg)
+    tanfov = camera.tangent_half_fov(60.0)
+    cr = EARTH_RADIUS_M + altitude_m
+    r.update(EARTH_RADIUS_M, cr, sun.copy(), E, AR_DEG)
+    args = (EARTH_RADIUS_M, cr, sun, E, AR_DEG, basis, tanfov)
+    return r, args
+
+
+def _sky(r, args, mode, surrogate=None):
+    out = torch.full((r.width, r.height, 3), -1.0, device=r.device)
+    r.sky_pixels(out, *args, mode=mode, surrogate=surrogate)
+    torch.cuda.synchronize()
+    return out.cpu().numpy()
+
+
+def test_sky_pixels_plain_matches_the_oracle_march():
+    """The plain per-pixel integrator is the sky-view LUT's march along each
+    pixel's own ray: against the oracle's restatement (float32) at every
+    pixel of a small frame looking above and below the horizon, with the
+    radiance-sample count."""
+
+    from conftest import assert_parity
+    from oracle.atm import Oracle
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.scene import pixel_rays
+
+    r, args = _sky_frame(96, 54, pitch_deg=5.0)
+    R, cr, sun, E_, ar_deg, basis, tanfov = args
+    r.radiance_samples(reset=True)
+    got = _sky(r, args, "plain")
+    assert r.radiance_samples() == 96 * 54 * earth_baseline().sky_view_steps
+    xs = torch.arange(96).repeat_interleave(54)
+    ys = torch.arange(54).repeat(96)
+    rays = pixel_rays(96, 54, basis, tanfov, xs, ys).double().numpy()
+    o = Oracle("f32")
+    cfg = earth_baseline()
+    ar = math.radians(ar_deg)
+    tl = o.build_transmittance(cfg, R)
+    ms = o.build_multi_scattering(cfg, R, E_, ar, tl)
+    ref = o.sky_rays(cfg, R, np.full(len(rays), cr - R), rays, np.tile(sun, (len(rays), 1)), E_, ar, tl, ms)
+    assert_parity(got.reshape(-1, 3), ref, "sky pixels (plain)")
+    r.close()
+
+
+def test_sky_pixels_lut_is_the_composite_sky():
+    """The LUT mode is the plain composite's sky radiance: a frame of sky
+    pixels with no scene or stars composites to the same values away from
+    the sun's disk."""
+
+    from planet_renderer_gb300.lighting import LightingState
+
+    r, args = _sky_frame(160, 90, pitch_deg=20.0)
+    R, cr, sun, E_, ar_deg, basis, tanfov = args
+    got = _sky(r, args, "lut")
+    zero = torch.zeros((160, 90, 3), device=r.device)
+    sid = torch.full((160, 90), -1, dtype=torch.int32, device=r.device)
+    hdr = torch.zeros_like(zero)
+    r.prepare_frame(zero, sid, R, cr, sun, E_, ar_deg, basis, tanfov)
+    r.composite(zero, zero, sid, zero, hdr, R, cr, sun, E_, LightingState(sun, ar_deg, E_).sun_disk_radiance, ar_deg,
+                basis, tanfov, 4.0, 12.0)
+    from planet_renderer_gb300.atmosphere.scene import pixel_rays
+
+    rays = pixel_rays(160, 90, basis, tanfov, torch.arange(160).repeat_interleave(90),
+                      torch.arange(90).repeat(160)).numpy().reshape(160, 90, 3)
+    away = np.degrees(np.arccos(np.clip(rays @ np.asarray(sun), -1, 1))) > 3.0  # outside the disk's smoothing
+    assert away.mean() > 0.9
+    np.testing.assert_array_equal(np.maximum(got, 0.0)[away], hdr.cpu().numpy()[away])
+    r.close()
+
+
+def test_sky_pixels_network_against_the_plain_integrator(trained):
+    """The network mode at the reduced training budget: close to the plain
+    integrator at every pixel (the bench states the full budget's error
+    against FP64); with every pixel gated it is the plain integrator; with no
+    polls allowed it falls back to the plain integrator and reports the
+    timeout."""
+
+    from planet_renderer_gb300._native import ATM_E_TIMEOUT, AtmError
+    from planet_renderer_gb300.atmosphere.surrogate import Surrogate
+
+    sg_full, _, _ = trained
+    sg = Surrogate(None, sg_full.sky, sg_full.planet_radius_m, sg_full.top_altitude_m, sg_full.scale_height_range)
+    r, args = _sky_frame(320, 180, pitch_deg=15.0)
+    plain = _sky(r, args, "plain")
+    net = _sky(r, args, "net", sg)
+    floor = 1e-4 * np.abs(plain).max()
+    e = np.max(np.abs(net - plain) / np.maximum(np.abs(plain), floor), axis=-1)
+    assert np.mean(e) < 0.1, (np.mean(e), np.quantile(e, 0.99))
+    sg.sky_twilight_cosine = 1.0  # gate every pixel
+    np.testing.assert_allclose(_sky(r, args, "net", sg), plain, rtol=1e-6, atol=0)
+    sg.sky_twilight_cosine = 0.1
+    sg.tc_wait_polls = -1
+    np.testing.assert_allclose(_sky(r, args, "net", sg), plain, rtol=1e-6, atol=0)
+    with pytest.raises(AtmError) as err:
+        r.check()
+    assert err.value.code == ATM_E_TIMEOUT
+    r.close()
