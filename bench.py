@@ -923,6 +923,69 @@ def _frame_4k(device, args) -> dict:
     return out
 
 
+def _frame_fused_4k(device, args, sg) -> dict:
+    """The reference's frame order at 3840x2160 for the three frame-chain
+    cameras on land-and-ocean shading inputs: update -> prepare_frame ->
+    shade_surface -> composite as separate calls, against update ->
+    render_frame (surface lighting, shading and composite fused in one
+    pass), each with the plain composite and with the surrogate composite;
+    CUDA-graph replays, device ms per frame."""
+
+    import torch
+
+    from planet_renderer_gb300.atmosphere import scene
+    from planet_renderer_gb300.atmosphere.workloads import (EARTH_RADIUS_M, SOLAR_IRRADIANCE,
+                                                            SUN_ANGULAR_RADIUS_DEG)
+    from planet_renderer_gb300.shading import OceanShading, shade_surface
+
+    r, cfg, frames = _setup_chain(device, 3840, 2160)
+    shaded = []
+    for v, gb, light in frames:
+        images = scene.shading_inputs(gb, EARTH_RADIUS_M, v.altitude_m, v.basis)
+        shaded.append((v, gb, light, images, torch.empty_like(gb["scene_hdr"])))
+    ar = math.radians(SUN_ANGULAR_RADIUS_DEG)
+
+    def separate(v, gb, light, images, surface_hdr, surrogate):
+        sun = v.sun_local
+        r.update(EARTH_RADIUS_M, v.camera_radius_m, sun, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG)
+        r.prepare_frame(images["position"], images["surface_id"], EARTH_RADIUS_M, v.camera_radius_m, sun,
+                        SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG, v.basis, v.tangent_half_fov)
+        shade_surface(images, r.surface_sun_transmittance, r.surface_sky_radiance, surface_hdr, sun,
+                      SOLAR_IRRADIANCE, v.basis, OceanShading(), ar, v.tangent_half_fov)
+        if surrogate is None:
+            r.composite(surface_hdr, gb["space_hdr"], images["surface_id"], images["position"], gb["hdr"],
+                        *_composite_args(v, light))
+        else:
+            r.composite_surrogate(surface_hdr, gb["space_hdr"], images["surface_id"], images["position"], gb["hdr"],
+                                  *_composite_args(v, light), surrogate=surrogate, check_fraction=MLP_CHECK_FRACTION,
+                                  seed=SEED)
+
+    def fused(v, gb, light, images, surface_hdr, surrogate):
+        r.update(EARTH_RADIUS_M, v.camera_radius_m, v.sun_local, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG)
+        r.render_frame(images, gb["space_hdr"], gb["hdr"], *_composite_args(v, light), surrogate=surrogate,
+                       check_fraction=MLP_CHECK_FRACTION, seed=SEED)
+
+    out = {"workload": "3840x2160, frame-chain cameras, land-and-ocean shading inputs (sea level at the median hit "
+                       "radius): update -> prepare_frame -> shade_surface -> composite as separate calls vs update "
+                       "-> render_frame (lighting, shading and composite fused); CUDA graphs"}
+    steps = 10
+    for name, fn in (("separate", separate), ("fused", fused)):
+        for label, surrogate in (("plain", None), ("mlp", sg)):
+            if surrogate is None and label == "mlp":
+                continue
+            graphs = _capture_fn(shaded, device, lambda *f: fn(*f, surrogate))
+            for _ in range(3):
+                for g in graphs:
+                    g.replay()
+            out[f"{name}_{label}_ms"] = _timed_graph_region(graphs, steps, device) / steps / 3.0
+            del graphs
+    r.check()
+    r.close()
+    del shaded, frames
+    torch.cuda.empty_cache()
+    return out
+
+
 SKY_ALTITUDES_M = (2_000.0, 20_000.0, 60_000.0)
 
 

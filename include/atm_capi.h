@@ -379,6 +379,10 @@ typedef struct AtmSurrogate {
                             surface pixels, MLP surface pixels, MLP sky pixels,
                             sky-view-LUT sky pixels, 128-pixel tiles whose
                             tensor-core MMA did not complete in time (0)       */
+  int32_t gate_terminator; /* non-zero: a surface segment whose sun cosine has
+                            different signs at its start, middle and end (it
+                            crosses the terminator) takes the plain path too */
+  int32_t reserved;
 } AtmSurrogate;
 
 /* COMPOSITE view of atm_composite with the per-pixel limb integrator replaced

@@ -1033,6 +1033,7 @@ int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m
   nets.sky_floor = float(sg->sky_floor);
   if (sg->tc_wait_polls < -1) return fail(ATM_E_INVALID, "tc_wait_polls must be -1, 0 or positive");
   nets.wait_tries = sg->tc_wait_polls == 0 ? atm::kTcWaitTries : sg->tc_wait_polls < 0 ? 0 : sg->tc_wait_polls;
+  nets.gate_crossing = sg->gate_terminator != 0;
   if (!h->queue) {
     const size_t cap = size_t(h->width) * size_t(h->height);
     ATM_CUDA(cudaMalloc(&h->queue, (cap + 4) * sizeof(uint32_t)), "fallback queue");

@@ -117,6 +117,7 @@ struct SurrogateNets {
   float sky_twilight_cos;    // gate: |sun cosine| at the camera below this -> sky-view LUT
   float limb_rad;            // gate: view ray within this of the limb -> plain path
   int wait_tries;            // bound of each tensor-core completion wait (mbarrier polls)
+  int gate_crossing;         // gate: the sun cosine changes sign along a surface segment -> plain path
 };
 // Pixels the surrogate composite hands to the plain integrator: entry =
 // kind << 30 | (y * width + x).  count and next are reset by each frame.

@@ -27,6 +27,9 @@ constexpr int kThreads = 256;
 constexpr int kStride = kH + 1; // padded smem row of a 64-wide activation
 
 __device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + expf(-z)); }
+// The training kernel's sigmoid: the hardware exponential and reciprocal
+// (a few ulp; the gradients are checked against the FP64 oracle at 1e-4).
+__device__ __forceinline__ float sigmoid_fast(float z) { return __fdividef(1.0f, 1.0f + __expf(-z)); }
 
 // Shared-memory layout of the training kernel (float offsets).
 struct TrainSmem {
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_grad(MlpShape m, const float* 
       for (int i = t; i < kS * kH; i += kThreads) {
         const int s = i / kH, j = i % kH;
         const float z = sm[L.z[l] + s * kStride + j];
-        sm[L.a[l] + s * kStride + j] = z * sigmoid(z);
+        sm[L.a[l] + s * kStride + j] = z * sigmoid_fast(z);
       }
       __syncthreads();
     }
@@ -162,37 +165,75 @@ __global__ void __launch_bounds__(kThreads) k_mlp_grad(MlpShape m, const float* 
     const float* a_prev = l == 0 ? sm + L.x : sm + L.a[l - 1];
     const int a_stride = l == 0 ? m.n_in + 1 : kStride;
     // dW[j][k] = sum_s dz[s][j] a_prev[s][k];  db[j] = sum_s dz[s][j]
-    for (int idx = t; idx < out * in; idx += kThreads) {
-      const int j = idx / in, k = idx % in;
-      float acc = 0.0f;
-      for (int s = 0; s < kS; ++s) acc = fmaf(dz[s * dz_stride + j], a_prev[s * a_stride + k], acc);
-      gp[m.off_w[l] + idx] = acc;
-    }
-    for (int j = t; j < out; j += kThreads) {
-      float acc = 0.0f;
-      for (int s = 0; s < kS; ++s) acc += dz[s * dz_stride + j];
-      gp[m.off_b[l] + j] = acc;
+    if (out == kH) {
+      // register tiles: 4 neurons j = 4 (t >> 4) + r by in/16 inputs
+      // k = (t & 15) + 16 c; per sample 8 shared loads feed 16 FMAs
+      const int j0 = (t >> 4) * 4, kk = t & 15;
+      float acc[4][4] = {};
+      float bacc = 0.0f;
+      for (int s = 0; s < kS; ++s) {
+        float dv[4], av[4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) dv[r] = dz[s * dz_stride + j0 + r];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) av[c] = kk + 16 * c < in ? a_prev[s * a_stride + kk + 16 * c] : 0.0f;
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(dv[r], av[c], acc[r][c]);
+        bacc += kk == 0 ? dv[0] : kk == 1 ? dv[1] : kk == 2 ? dv[2] : dv[3];  // used by kk < 4
+      }
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+          if (kk + 16 * c < in) gp[m.off_w[l] + (j0 + r) * in + kk + 16 * c] = acc[r][c];
+      if (kk < 4) gp[m.off_b[l] + j0 + kk] = bacc;
+    } else {
+      for (int idx = t; idx < out * in; idx += kThreads) {
+        const int j = idx / in, k = idx % in;
+        float acc = 0.0f;
+        for (int s = 0; s < kS; ++s) acc = fmaf(dz[s * dz_stride + j], a_prev[s * a_stride + k], acc);
+        gp[m.off_w[l] + idx] = acc;
+      }
+      for (int j = t; j < out; j += kThreads) {
+        float acc = 0.0f;
+        for (int s = 0; s < kS; ++s) acc += dz[s * dz_stride + j];
+        gp[m.off_b[l] + j] = acc;
+      }
     }
     if (l == 0) break;
-    // dZ_{l-1}[s][k] = (sum_j dz[s][j] W[j][k]) * silu'(Z_{l-1}[s][k]), in place of Z_{l-1}
+    // dZ_{l-1}[s][k] = (sum_j dz[s][j] W[j][k]) * silu'(Z_{l-1}[s][k]), in
+    // place of Z_{l-1} (in == 64 here): register tiles of 4 samples
+    // s = 4 (t >> 4) + r by 4 inputs k = (t & 15) + 16 c
     const float* W = sm + L.w[l];
     float* zp = sm + L.z[l - 1];
-    float upd[kS * kH / kThreads];
-    int n_upd = 0;
-    for (int idx = t; idx < kS * in; idx += kThreads) {
-      const int s = idx / in, k = idx % in;
-      float acc = 0.0f;
-      for (int j = 0; j < out; ++j) acc = fmaf(dz[s * dz_stride + j], W[j * (in + 1) + k], acc);
-      const float z = zp[s * kStride + k];
-      const float sg = sigmoid(z);
-      upd[n_upd++] = acc * sg * (1.0f + z * (1.0f - sg));
+    const int s0 = (t >> 4) * 4, kk = t & 15;
+    float acc[4][4] = {};
+    for (int j = 0; j < out; ++j) {
+      float dv[4], wv[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) dv[r] = dz[(s0 + r) * dz_stride + j];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) wv[c] = W[j * (in + 1) + kk + 16 * c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = fmaf(dv[r], wv[c], acc[r][c]);
     }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float z = zp[(s0 + r) * kStride + kk + 16 * c];
+        const float sg = sigmoid_fast(z);
+        acc[r][c] = acc[r][c] * sg * (1.0f + z * (1.0f - sg));
+      }
     __syncthreads();  // all reads of Z_{l-1} (and of dZ_l by the dW loop) are done
-    n_upd = 0;
-    for (int idx = t; idx < kS * in; idx += kThreads) {
-      const int s = idx / in, k = idx % in;
-      zp[s * kStride + k] = upd[n_upd++];
-    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) zp[(s0 + r) * kStride + kk + 16 * c] = acc[r][c];
     __syncthreads();
   }
   // squared-error sum of the tile

@@ -59,12 +59,14 @@ __device__ __forceinline__ float point_features(const DevParams& P, float bottom
   return mu;
 }
 // Aerial x[7..10]: the segment's end, then its middle.  Returns the smaller
-// |sun cosine| of the two (the twilight gate).
+// |sun cosine| of the two (the twilight gate); `mu_end`, `mu_mid` receive
+// the cosines themselves.
 __device__ __forceinline__ float segment_features(const DevParams& P, float bottom, const RayGeom& G, f3 ray,
-                                                  float o_y, f3 sun, float start, float end, float* x) {
-  const float a = point_features(P, bottom, G, ray, o_y, sun, end, x + 7);
-  const float b = point_features(P, bottom, G, ray, o_y, sun, 0.5f * (start + end), x + 9);
-  return mn(fabsf(a), fabsf(b));
+                                                  float o_y, f3 sun, float start, float end, float* x,
+                                                  float& mu_end, float& mu_mid) {
+  mu_end = point_features(P, bottom, G, ray, o_y, sun, end, x + 7);
+  mu_mid = point_features(P, bottom, G, ray, o_y, sun, 0.5f * (start + end), x + 9);
+  return mn(fabsf(mu_end), fabsf(mu_mid));
 }
 // Sky x[6..9]: the end of the ray's march (the shell top or the ground),
 // then its lowest point (the closest approach, clamped to the march).
@@ -180,7 +182,8 @@ __global__ void __launch_bounds__(128) k_gen_samples(const SurrogateSetDev* __re
       } else {
         start = end = 0.0f;
       }
-      segment_features(P, R, G, ray, R + h, sun, start, end, x);
+      float mu_end, mu_mid;
+      segment_features(P, R, G, ray, R + h, sun, start, end, x, mu_end, mu_mid);
       for (int k = 0; k < kSurrogateApIn; ++k) features[i * kSurrogateApIn + k] = x[k];
       targets[i * 6 + 0] = logf(L.x + kSurrogateFloor);
       targets[i * 6 + 1] = logf(L.y + kSurrogateFloor);
@@ -281,9 +284,13 @@ __global__ void __launch_bounds__(256, 3) k_composite_surrogate(
         fx[4] = nets.lhr_n;
         fx[5] = nets.lhm_n;
         fx[6] = 2.0f * __logf(clampf(end - start, 1.0f, kSurrogateMaxLength)) / logf(kSurrogateMaxLength) - 1.0f;
-        // twilight gate: the sun cosine small at the start, middle or end
-        const float mu_min = mn(fabsf(mu_s), segment_features(P, A.bottom, G, ray, o_y, F.sun, start, end, fx));
-        kind = mu_min < nets.twilight_cos ? kSurfPlain : kSurfMlp;
+        // twilight gate: the sun cosine small at the start, middle or end, or
+        // of different signs there (the segment crosses the terminator)
+        float mu_end, mu_mid;
+        const float mu_min =
+            mn(fabsf(mu_s), segment_features(P, A.bottom, G, ray, o_y, F.sun, start, end, fx, mu_end, mu_mid));
+        const bool crosses = nets.gate_crossing && ((mu_s > 0.0f) != (mu_end > 0.0f) || (mu_s > 0.0f) != (mu_mid > 0.0f));
+        kind = (mu_min < nets.twilight_cos || crosses) ? kSurfPlain : kSurfMlp;
       }
     } else if (nets.sky != nullptr && A.cam_alt <= P.top && fabsf(F.sun.y) >= nets.sky_twilight_cos && !near_limb) {
       kind = kSkyMlp;

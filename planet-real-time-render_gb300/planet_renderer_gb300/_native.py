@@ -172,6 +172,8 @@ class AtmSurrogate(ctypes.Structure):
         ("seed", ctypes.c_uint32),
         ("tc_wait_polls", ctypes.c_int32),
         ("stats", ctypes.c_void_p),
+        ("gate_terminator", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

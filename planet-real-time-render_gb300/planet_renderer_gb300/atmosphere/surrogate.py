@@ -342,6 +342,9 @@ class Surrogate:
     # bound of each tensor-core completion wait: 0 = the library's; -1 = none
     # (every wait gives up at once, the MLP pixels take the plain path)
     tc_wait_polls = 0
+    # gate -> plain path: a surface segment crossing the terminator (its sun
+    # cosine changes sign between its start, middle and end)
+    gate_terminator = False
 
     def native(self, check_fraction: float = 0.01, seed: int = 0, stats=None,
                camera_altitude_m: float | None = None) -> _native.AtmSurrogate:
@@ -362,6 +365,7 @@ class Surrogate:
         s.limb_degrees = float(self.limb_degrees)
         s.seed = int(seed) & 0xFFFFFFFF
         s.tc_wait_polls = int(self.tc_wait_polls)
+        s.gate_terminator = 1 if self.gate_terminator else 0
         s.stats = stats
         return s
 

@@ -156,7 +156,21 @@ def _full_resolution_frame(cfg, view, width=1920, height=1080):
             return rep
         if not f64:
             f64.update(oracle_frame("f64"))
-        return assert_exact_parity(got, f32[key], f64[key], f"{key} {view.altitude_m:.0f} m")
+        return assert_exact_parity(got, f32[key], f64[key], f"{key} {view.altitude_m:.0f} m {_worst(got, key)}")
+
+    def _worst(got, key):
+        # the five elements furthest outside the criterion, for the message
+        g, r32, r64 = (np.asarray(a, np.float64) for a in (got, f32[key], f64[key]))
+        peak = np.abs(r64).reshape(-1, r64.shape[-1]).max(axis=0)
+        tol = 1e-3 * np.abs(r64) + 1e-5 * peak + np.abs(r32 - r64)
+        excess = np.abs(g - r64) / np.maximum(tol, 1e-300)
+        idx = np.argsort(excess, axis=None)[-5:]
+        rows = []
+        for i in idx:
+            at = np.unravel_index(i, g.shape)
+            sid = int(host["surface_id"][at[0], at[1]]) if g.ndim == 3 and key in ("hdr", "sun_t", "sky") else None
+            rows.append((tuple(int(a) for a in at), sid, float(g[at]), float(r32[at]), float(r64[at])))
+        return rows
 
     check(r.sky_view_lut.to_numpy(), "sky_view_lut")
     check(r.aerial_scattering_lut.to_numpy(), "aerial_scattering_lut")
