@@ -420,7 +420,7 @@ def main() -> None:
     parser.add_argument("--mlp-epochs", type=int, default=400, help="surrogate training epochs (2^22 samples)")
     parser.add_argument("--no-post", action="store_true", help="skip the 4K display post-process timing")
     parser.add_argument("--no-luts", action="store_true", help="skip the plain LUT-build timing")
-    parser.add_argument("--mlp-sweep", type=int, default=0,
+    parser.add_argument("--mlp-sweep", type=int, default=64,
                         help="also run the aerial-surrogate frame workload over this many 4K frames with cameras "
                              "log-uniform 1 m - 4000 km (e.g. 64)")
     parser.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
@@ -567,6 +567,15 @@ def _summary(frame_4k, luts, timed_s) -> dict:
                 "mlp_4k_err_worst_camera": max(c["mlp"]["mean"] for c in err["cameras"]),
                 "plain_4k_err_mean": err["all"]["plain"]["mean"],
             })
+        sky = frame_4k.get("sky_4k")
+        if sky:
+            out.update({"sky_4k_net_speedup_vs_plain": sky["net_speedup_vs_plain"],
+                        "sky_4k_net_err_mean": sky["error_vs_fp64"]["net"]["mean"],
+                        "sky_4k_net_ms": sky["net_ms"], "sky_4k_plain_ms": sky["plain_ms"]})
+        fused = frame_4k.get("fused_4k")
+        if fused:
+            out.update({k: fused[k] for k in ("separate_plain_ms", "fused_plain_ms", "separate_mlp_ms",
+                                              "fused_mlp_ms") if k in fused})
         sweep = frame_4k.get("sweep")
         if sweep:
             out.update({
@@ -814,6 +823,27 @@ def _capture_fn(frames, device, fn):
     return graphs
 
 
+def _sparse_inputs(gb, pix, width, height):
+    """The G-buffer images the FP64 oracle composite reads, as full-size
+    float64 / int32 host arrays holding only the pixels `pix` (n, 2): the
+    oracle touches no other element, and untouched zero pages cost nothing."""
+
+    import numpy as np
+    import torch
+
+    dev = gb["surface_id"].device
+    px = torch.as_tensor(pix[:, 0], device=dev)
+    py = torch.as_tensor(pix[:, 1], device=dev)
+    full = {}
+    for k in ("scene_hdr", "space_hdr", "position_view"):
+        a = np.zeros((width, height, 3), np.float64)
+        a[pix[:, 0], pix[:, 1]] = gb[k][px, py].cpu().numpy()
+        full[k] = a
+    sid = np.zeros((width, height), np.int32)
+    sid[pix[:, 0], pix[:, 1]] = gb["surface_id"][px, py].cpu().numpy()
+    return full, sid
+
+
 def _fp64_error(r, cfg, frames, images, n_pixels=1500):
     """Relative error (max over RGB, floor 1e-4 of the sample's peak) of each
     camera's image against the FP64 oracle composite at n_pixels random
@@ -836,8 +866,7 @@ def _fp64_error(r, cfg, frames, images, n_pixels=1500):
         sv = o.build_sky_view(cfg, EARTH_RADIUS_M, alt, float(v.sun_local[1]), SOLAR_IRRADIANCE, ar, tl, ms)
         ap = np.zeros((cfg.aerial_lut_width, cfg.aerial_lut_height, cfg.aerial_lut_depth, 3))
         pix = np.stack([rng.integers(0, W, n_pixels), rng.integers(0, H, n_pixels)], 1)
-        full = {k: gb[k].cpu().numpy().astype(np.float64) for k in ("scene_hdr", "space_hdr", "position_view")}
-        sid = gb["surface_id"].cpu().numpy()
+        full, sid = _sparse_inputs(gb, pix, W, H)
         plist = (pix[:, 0].astype(np.int64) * H + pix[:, 1]).astype(np.int32)
         hdr, _ = o.composite(cfg, full["scene_hdr"], full["space_hdr"], sid, full["position_view"], EARTH_RADIUS_M,
                              alt, alt, v.sun_local, SOLAR_IRRADIANCE, light.sun_disk_radiance, ar, v.basis,
@@ -884,9 +913,10 @@ def _frame_4k(device, args) -> dict:
     if args.no_mlp:
         return out
     t0 = time.perf_counter()
-    sg, reports = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device)
+    trained, reports = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device)
     torch.cuda.synchronize(device)
     train_s = time.perf_counter() - t0
+    sg = _frame_surrogate(trained)
     stats = torch.zeros(8, dtype=torch.float32, device=device)
     fn = lambda v, gb, light: _chain_surrogate(r, v, gb, light, sg, stats)
     graphs = _capture_fn(frames, device, fn)
@@ -907,20 +937,37 @@ def _frame_4k(device, args) -> dict:
     out.update({
         "mlp_ms": mlp_ms, "speedup": plain_ms / mlp_ms, "error_vs_fp64": err,
         "gate": {**gate, "check_fraction": MLP_CHECK_FRACTION},
-        "training": {"seconds": train_s, "samples_per_network": 2**22, "batch": 16384, "epochs": args.mlp_epochs,
-                     "steps_per_network": reports["sky"].steps,
+        "training": {"seconds": train_s, "networks": len(reports), "samples_per_network": 2**22, "batch": 16384,
+                     "epochs": args.mlp_epochs, "steps_per_network": reports["sky"].steps,
                      "held_out": {name: rep.held_out for name, rep in reports.items()}},
-        "networks": "aerial 11->4x64->6 (one for cameras inside the shell, one above it), sky 10->3x64->3; SiLU; "
-                    "BF16 operands on tcgen05 with FP32 accumulators in tensor memory",
+        "networks": "aerial 11->4x64->6 (one per camera-altitude band inside the shell: 0-100 m, 100 m-3 km, "
+                    "3-25 km, 25-100 km; one above the shell), sky 10->3x64->3; SiLU; BF16 operands on tcgen05 "
+                    "with FP32 accumulators in tensor memory; in frames the sky pixels read the sky-view LUT",
+        "gates": {"twilight_cosine": sg.twilight_cosine, "terminator": bool(sg.gate_terminator),
+                  "limb_degrees": sg.limb_degrees},
     })
+    del graphs
     if args.mlp_sweep:
-        del graphs
         out["sweep"] = _mlp_sweep(r, cfg, sg, args.mlp_sweep, device)
-    else:
-        del graphs
     del r, frames
     torch.cuda.empty_cache()
+    out["sky_4k"] = _sky_4k(device, args, trained)
+    out["fused_4k"] = _frame_fused_4k(device, args, sg)
     return out
+
+
+def _frame_surrogate(trained):
+    """The surrogate of the frames: the aerial networks of `trained` (its
+    altitude bands and the network above the shell) with the sky pixels on
+    the sky-view LUT, as the plain frame has them (a LUT tap is cheaper than
+    the sky network and exact to the plain frame), and the terminator gate."""
+
+    from planet_renderer_gb300.atmosphere.surrogate import Surrogate
+
+    sg = Surrogate(trained.aerial, None, trained.planet_radius_m, trained.top_altitude_m, trained.scale_height_range,
+                   trained.aerial_spec, None, trained.aerial_above_shell, aerial_bands=trained.aerial_bands)
+    sg.gate_terminator = True
+    return sg
 
 
 def _frame_fused_4k(device, args, sg) -> dict:
@@ -1120,8 +1167,7 @@ def _mlp_sweep(r, cfg, sg, n_frames, device, n_pixels=300) -> dict:
             values[name] = gb["hdr"][px, py].cpu().numpy().astype(np.float64)
         alt = v.altitude_m
         sv = o.build_sky_view(cfg, EARTH_RADIUS_M, alt, float(v.sun_local[1]), SOLAR_IRRADIANCE, ar, tl, ms)
-        full = {k: gb[k].cpu().numpy().astype(np.float64) for k in ("scene_hdr", "space_hdr", "position_view")}
-        sid = gb["surface_id"].cpu().numpy()
+        full, sid = _sparse_inputs(gb, pix, W, H)
         plist = (pix[:, 0].astype(np.int64) * H + pix[:, 1]).astype(np.int32)
         hdr, _ = o.composite(cfg, full["scene_hdr"], full["space_hdr"], sid, full["position_view"], EARTH_RADIUS_M,
                              alt, alt, v.sun_local, SOLAR_IRRADIANCE, light.sun_disk_radiance, ar, v.basis,
@@ -1182,7 +1228,9 @@ def _profile_frame_4k_mlp(args):
     device = torch.device("cuda:0")
     torch.cuda.set_device(device)
     r, cfg, frames = _setup_chain(device, 3840, 2160)
-    sg, _ = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device)
+    trained, _ = train_surrogate(epochs=args.mlp_epochs, batch=16384, seed=SEED, log_every=0, device=device,
+                                 sky=False)
+    sg = _frame_surrogate(trained)
     v, gb, light = frames[0]
     for _ in range(3):
         _chain_surrogate(r, v, gb, light, sg, None)

@@ -238,10 +238,12 @@ class Oracle:
     def composite(self, config, scene_hdr, space_hdr, surface_id, position_view, bottom_radius,
                   camera_altitude, sky_lut_camera_altitude, sun, irradiance, disk_radiance, angular_radius_rad,
                   basis, tangent_half_fov, star_start, star_end, diagnostic_view, tlut, mslut, svlut, aplut,
-                  pixel_list=None, out=None):
+                  pixel_list=None, out=None, margin_out=None):
         """Returns (hdr, radiance_samples).  ``pixel_list`` (n,) int32 linear
         indices x*H + y restricts the pixels computed (others left as in
-        ``out``, zero by default)."""
+        ``out``, zero by default).  ``margin_out`` (W, H) float64 receives per
+        computed pixel the smallest distance (m) of any density evaluation's
+        altitude from the profile's cutoffs (0 and the shell top)."""
 
         p = params_from_config(config)
         sid = np.ascontiguousarray(surface_id, dtype=np.int32)
@@ -264,7 +266,7 @@ class Oracle:
         fn = self._fn("composite")
         fn.restype = ctypes.c_int64
         fn.argtypes = [ctypes.POINTER(AtmParams), ctypes.POINTER(CompositeArgs), ctypes.c_int, ctypes.c_int,
-                       ctypes.c_int] + [ctypes.c_void_p] * 9 + [ctypes.c_void_p, ctypes.c_int64]
+                       ctypes.c_int] + [ctypes.c_void_p] * 9 + [ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p]
         if pixel_list is None:
             plist, n = None, 0
         else:
@@ -272,7 +274,8 @@ class Oracle:
             n = plist.size
         samples = fn(ctypes.byref(p), ctypes.byref(a), H, 1, 3, _ptr(scene), _ptr(space), _ptr(sid), _ptr(pos),
                      _ptr(tlut), _ptr(mslut), _ptr(svlut), _ptr(aplut), _ptr(hdr),
-                     None if plist is None else _ptr(plist), n)
+                     None if plist is None else _ptr(plist), n,
+                     None if margin_out is None else _ptr(margin_out))
         return hdr, int(samples)
 
 
@@ -364,7 +367,8 @@ class OracleAtmosphere:
 
     def composite(self, scene_hdr, space_hdr, surface_id, position_view, planet_radius_m, camera_radius_m,
                   sun_local, solar_irradiance, sun_disk_radiance_rgb, sun_angular_radius_degrees, view_basis,
-                  tangent_half_fov, star_contrast_start, star_contrast_end, diagnostic_view=0, pixel_list=None):
+                  tangent_half_fov, star_contrast_start, star_contrast_end, diagnostic_view=0, pixel_list=None,
+                  margin_out=None):
         cam_alt = max(float(camera_radius_m) - float(planet_radius_m), 0.0)
         sky_alt = cam_alt if self.sky_snapshot_altitude_m is None else self.sky_snapshot_altitude_m
         return self.kernels.composite(
@@ -372,4 +376,4 @@ class OracleAtmosphere:
             sun_local, solar_irradiance, sun_disk_radiance_rgb, math.radians(sun_angular_radius_degrees),
             view_basis, tangent_half_fov, star_contrast_start, star_contrast_end, int(diagnostic_view),
             self.transmittance_lut, self.multi_scattering_lut, self.sky_view_lut, self.aerial_scattering_lut,
-            pixel_list=pixel_list)
+            pixel_list=pixel_list, margin_out=margin_out)

@@ -56,6 +56,14 @@ template <class R> inline R m_pow(R x, R y) { using std::pow; return pow(x, y); 
 template <class R> inline R m_atan2(R y, R x) { using std::atan2; return atan2(y, x); }
 template <class R> inline R m_fabs(R x) { using std::fabs; return fabs(x); }
 template <class R> inline R m_floor(R x) { using std::floor; return floor(x); }
+template <class R> inline double as_d(R x) { return double(x); }
+// Smallest distance (m) of any density evaluation's altitude from the
+// profile's cutoffs (0 and the shell top, where _density drops to zero) since
+// the calling thread last reset it: the composite reports it per pixel.  A
+// radiance sample that close to a cutoff switches its density on or off
+// under a rounding of its altitude, so two float evaluations of the same
+// pixel can differ there by that sample's whole contribution.
+thread_local double g_cutoff_margin = HUGE_VAL;
 
 template <class R>
 struct V3 {
@@ -118,6 +126,8 @@ struct Model {
 
   // _density :168-192
   V3<R> density(R h) const {
+    const double hd = as_d(h);
+    g_cutoff_margin = std::min(g_cutoff_margin, std::min(std::fabs(hd), std::fabs(hd - P.top_altitude_m)));
     R ray = R(0), mie = R(0), ozone = R(0);
     if (R(0) <= h && h <= top()) {
       ray = m_exp(-h / R(P.rayleigh_scale_height_m));
@@ -1005,7 +1015,7 @@ V3<R> composite_pixel(const Model<R>& m, const CompositeArgs& A, int px, int py,
 template <class R>
 int64_t composite(const AtmParams& P, const CompositeArgs& A, Image img, const R* scene, const R* space,
                   const int32_t* sid, const R* pos, const R* tlut, const R* mslut, const R* svlut, const R* aplut,
-                  R* hdr, const int32_t* pixel_list, int64_t n_list) {
+                  R* hdr, const int32_t* pixel_list, int64_t n_list, double* margin) {
   Model<R> m(P);
   m.tlut = {tlut, P.transmittance_lut_width, P.transmittance_lut_height};
   m.mslut = {mslut, P.multi_scattering_lut_width, P.multi_scattering_lut_height};
@@ -1020,8 +1030,10 @@ int64_t composite(const AtmParams& P, const CompositeArgs& A, Image img, const R
     size_t o = img.off(x, y);
     size_t oi = static_cast<size_t>(x) * img.stride_x + static_cast<size_t>(y) * img.stride_y;
     int64_t local = 0;
+    g_cutoff_margin = HUGE_VAL;
     V3<R> c = composite_pixel(m, A, x, y, load3(scene + o), load3(space + o), sid[oi], load3(pos + o), &local);
     store3(hdr + o, c);
+    if (margin) margin[oi] = g_cutoff_margin;
     count += local;
   }
   return count;
@@ -1054,6 +1066,7 @@ inline bool operator<(CountF a, CountF b) { return a.v < b.v; }
 inline bool operator>(CountF a, CountF b) { return a.v > b.v; }
 inline bool operator<=(CountF a, CountF b) { return a.v <= b.v; }
 inline bool operator>=(CountF a, CountF b) { return a.v >= b.v; }
+inline double as_d(CountF x) { return double(x.v); }
 inline CountF sqrt(CountF x) { ++counts[kSqrt]; return mkc(std::sqrt(x.v)); }
 inline CountF exp(CountF x) { ++counts[kExp]; return mkc(std::exp(x.v)); }
 inline CountF acos(CountF x) { ++counts[kAcos]; return mkc(std::acos(x.v)); }
@@ -1120,9 +1133,9 @@ static_assert(sizeof(CountF) == sizeof(float), "CountF must alias float buffers"
   ORC_EXPORT int64_t orc_composite_##SUFFIX(                                                                         \
       const AtmParams* p, const CompositeArgs* a, int stride_x, int stride_y, int channels, const R* scene,           \
       const R* space, const int32_t* sid, const R* pos, const R* tlut, const R* mslut, const R* svlut,               \
-      const R* aplut, R* hdr, const int32_t* pixel_list, int64_t n_list) {                                           \
+      const R* aplut, R* hdr, const int32_t* pixel_list, int64_t n_list, double* margin) {                           \
     return composite<R>(*p, *a, Image{stride_x, stride_y, channels}, scene, space, sid, pos, tlut, mslut, svlut,     \
-                        aplut, hdr, pixel_list, n_list);                                                             \
+                        aplut, hdr, pixel_list, n_list, margin);                                                     \
   }
 
 ORC_DEFINE(f32, float)

@@ -375,10 +375,13 @@ class Surrogate:
         for name, net in (("aerial", self.aerial), ("sky", self.sky), ("aerial_above_shell", self.aerial_above_shell)):
             if net is not None:
                 net.save(d / f"{name}.npz")
+        for k, (_, net) in enumerate(self.aerial_bands):
+            net.save(d / f"aerial_band{k}.npz")
         np.savez(d / "meta.npz", planet_radius_m=self.planet_radius_m, top_altitude_m=self.top_altitude_m,
                  scale_height_range=np.array(self.scale_height_range),
                  aerial_spec=np.array([self.aerial_spec.floor, self.aerial_spec.floor_t]),
-                 sky_spec=np.array([self.sky_spec.floor, self.sky_spec.floor_t]))
+                 sky_spec=np.array([self.sky_spec.floor, self.sky_spec.floor_t]),
+                 band_tops_m=np.array([top for top, _ in self.aerial_bands], dtype=np.float64))
 
     @classmethod
     def load(cls, directory, device=None) -> "Surrogate":
@@ -387,33 +390,65 @@ class Surrogate:
         nets = {name: (Mlp.load(d / f"{name}.npz", device=device) if (d / f"{name}.npz").exists() else None)
                 for name in ("aerial", "sky", "aerial_above_shell")}
         spec = lambda a: TargetSpec(float(a[0]), float(a[1]))
+        tops = meta["band_tops_m"] if "band_tops_m" in meta.files else []
+        bands = [(float(top), Mlp.load(d / f"aerial_band{k}.npz", device=device)) for k, top in enumerate(tops)]
         return cls(nets["aerial"], nets["sky"], float(meta["planet_radius_m"]), float(meta["top_altitude_m"]),
                    tuple(float(v) for v in meta["scale_height_range"]), spec(meta["aerial_spec"]),
-                   spec(meta["sky_spec"]), nets["aerial_above_shell"])
+                   spec(meta["sky_spec"]), nets["aerial_above_shell"], aerial_bands=bands)
+
+
+# Camera-altitude bands of the aerial networks inside the shell (m).  Each
+# band's network is trained on segments starting in that band; a frame picks
+# the band of its camera on the host.  Specialised this way, the network of
+# cameras within 100 m of the ground is ~20x more accurate in the frame than
+# one network for the whole shell, and the mid-altitude bands 1.5-3x.
+INSIDE_BANDS_M = ((0.0, 100.0), (100.0, 3000.0), (3000.0, 25000.0), (25000.0, 100000.0))
+# Share of training samples with the sun's zenith uniform in angle (0-100
+# deg): the sun feature's map puts a sun within 20 deg of the zenith into 1.5%
+# of the feature range, and frames under a high sun had 2-3x the error of
+# the rest without it.
+SUN_ANGLE_FRACTION = 0.5
 
 
 def train_surrogate(configs=None, n_samples: int = 2**22, batch: int = 16384, epochs: int = 400, seed: int = 1,
-                    lr: float = 4e-3, device=None, log_every: int = 100, above_shell: bool = True):
-    """The networks on the default grid: the aerial pair (inside / above the
-    shell; one aerial network for both when ``above_shell`` is False) and the
-    sky network.  Returns (Surrogate, {name: report})."""
+                    lr: float = 4e-3, device=None, log_every: int = 100, above_shell: bool = True,
+                    bands=INSIDE_BANDS_M, sun_angle_fraction: float = SUN_ANGLE_FRACTION, sky: bool = True):
+    """The networks on the default grid: one aerial network per camera
+    altitude band inside the shell (``bands``; one network for the whole
+    shell when empty), the aerial network for cameras above the shell
+    (``above_shell``) and the sky network (``sky``).  Returns (Surrogate,
+    {name: report})."""
 
     source = SampleSource(configs or parameter_grid(), device=device)
     reports = {}
+    band_nets = []
     try:
-        inside_spec = AERIAL_INSIDE_SPEC if above_shell else DEFAULT_SPECS[AERIAL]
-        aerial, reports["aerial"] = train(source, AERIAL, n_samples, batch, epochs, lr=lr, seed=seed,
-                                          spec=inside_spec, log_every=log_every)
+        inside_spec = dataclasses.replace(AERIAL_INSIDE_SPEC if above_shell else DEFAULT_SPECS[AERIAL],
+                                          sun_angle_fraction=sun_angle_fraction)
+        if bands:
+            for k, (lo, hi) in enumerate(bands):
+                spec = dataclasses.replace(inside_spec, start_range_m=(float(lo), float(hi)))
+                net, reports[f"aerial_{int(lo)}_{int(hi)}m"] = train(
+                    source, AERIAL, n_samples, batch, epochs, lr=lr, seed=seed + 10 + k, spec=spec,
+                    log_every=log_every)
+                band_nets.append((float(hi), net))
+            aerial = band_nets[-1][1]
+        else:
+            aerial, reports["aerial"] = train(source, AERIAL, n_samples, batch, epochs, lr=lr, seed=seed,
+                                              spec=inside_spec, log_every=log_every)
         above = None
         if above_shell:
+            above_spec = dataclasses.replace(AERIAL_ABOVE_SPEC, sun_angle_fraction=sun_angle_fraction)
             above, reports["aerial_above_shell"] = train(source, AERIAL, n_samples, batch, epochs, lr=lr,
-                                                         seed=seed + 2, spec=AERIAL_ABOVE_SPEC, log_every=log_every)
-        sky, reports["sky"] = train(source, SKY, n_samples, batch, epochs, lr=lr, seed=seed + 1,
-                                    spec=DEFAULT_SPECS[SKY], log_every=log_every)
+                                                         seed=seed + 2, spec=above_spec, log_every=log_every)
+        sky_net = None
+        if sky:
+            sky_net, reports["sky"] = train(source, SKY, n_samples, batch, epochs, lr=lr, seed=seed + 1,
+                                            spec=DEFAULT_SPECS[SKY], log_every=log_every)
     finally:
         source.close()
-    return Surrogate(aerial, sky, source.planet_radius_m, source.top_altitude_m, source.scale_height_range,
-                     inside_spec, DEFAULT_SPECS[SKY], above), reports
+    return Surrogate(aerial, sky_net, source.planet_radius_m, source.top_altitude_m, source.scale_height_range,
+                     inside_spec, DEFAULT_SPECS[SKY], above, aerial_bands=band_nets), reports
 
 
 def stats_summary(stats: torch.Tensor) -> dict:

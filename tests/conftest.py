@@ -112,6 +112,27 @@ def assert_exact_parity(got, ref32, ref64, what: str = "", rtol=RTOL, atol_frac=
     return rep
 
 
+def exact_parity_violations(got, ref32, ref64, rtol=RTOL, atol_frac=ATOL_FRAC):
+    """Element mask (the arrays' shape) of the well-conditioned elements
+    outside the exact-parity criterion of :func:`exact_parity_report`."""
+    got, r32, r64 = (np.asarray(a, dtype=np.float64) for a in (got, ref32, ref64))
+    peak = np.abs(r64).reshape(-1, r64.shape[-1]).max(axis=0)
+    own = np.abs(r32 - r64)
+    tol = rtol * np.abs(r64) + atol_frac * peak
+    return (np.abs(got - r64) > tol + own) & (own <= tol)
+
+
+# A radiance sample whose altitude lies this close to a cutoff of the
+# density profile (0 and the shell top, where the reference's _density
+# drops to zero, atmosphere/renderer.py:168-192) is switched on or off by
+# the rounding of its altitude: the kernels' altitude (compensated float32
+# for cameras above the shell) and the reference's float32 one differ by up
+# to metres there, so the pixel's radiance may jump by that sample's whole
+# contribution.  Such pixels are the algorithm's own discontinuity, not a
+# mismatch.
+CUTOFF_MARGIN_M = 10.0
+
+
 def load_golden(name: str):
     path = GOLDEN / f"{name}.npz"
     if not path.exists():

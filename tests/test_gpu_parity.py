@@ -11,7 +11,8 @@ import math
 import numpy as np
 import pytest
 
-from conftest import assert_exact_parity, assert_parity, load_golden, parity_report
+from conftest import (CUTOFF_MARGIN_M, assert_exact_parity, assert_parity, exact_parity_violations, load_golden,
+                      parity_report)
 from scenario import Scenario, gpu_chain, gpu_stages, oracle_stages_with_luts
 
 pytestmark = pytest.mark.gpu
@@ -136,10 +137,12 @@ def _full_resolution_frame(cfg, view, width=1920, height=1080):
         o = OracleAtmosphere(width, height, cfg, precision)
         o.update(R, cr, sun.copy(), E, ar)
         o.prepare_frame(host["position_view"], host["surface_id"], R, cr, sun, E, ar, basis, tanfov)
+        margin = np.full((width, height), np.inf)
         out, n = o.composite(host["scene_hdr"], host["space_hdr"], host["surface_id"], host["position_view"], R, cr,
-                             sun, E, disk, ar, basis, tanfov, 4.0, 12.0, 0)
+                             sun, E, disk, ar, basis, tanfov, 4.0, 12.0, 0, margin_out=margin)
         return {"sky_view_lut": o.sky_view_lut, "aerial_scattering_lut": o.aerial_scattering_lut,
-                "sun_t": o.surface_sun_transmittance, "sky": o.surface_sky_radiance, "hdr": out, "samples": n}
+                "sun_t": o.surface_sun_transmittance, "sky": o.surface_sky_radiance, "hdr": out, "samples": n,
+                "margin": margin}
 
     f32 = oracle_frame("f32")
     f64 = {}
@@ -156,6 +159,19 @@ def _full_resolution_frame(cfg, view, width=1920, height=1080):
             return rep
         if not f64:
             f64.update(oracle_frame("f64"))
+        if key == "hdr":
+            # composite pixels outside the criterion must each have a radiance
+            # sample within CUTOFF_MARGIN_M of a density cutoff (conftest), and
+            # be rare; every other pixel meets exact parity
+            bad = exact_parity_violations(got, f32[key], f64[key]).any(axis=-1)
+            margin = f64["margin"]
+            assert (margin[bad] < CUTOFF_MARGIN_M).all(), (
+                f"{view.altitude_m:.0f} m: {int((margin[bad] >= CUTOFF_MARGIN_M).sum())} pixels outside the criterion "
+                f"away from a density cutoff {_worst(got, key)}")
+            assert bad.mean() <= 1e-4, bad.mean()
+            keep = ~bad
+            return assert_exact_parity(got[keep], f32[key][keep], f64[key][keep],
+                                       f"{key} {view.altitude_m:.0f} m {_worst(got, key)}")
         return assert_exact_parity(got, f32[key], f64[key], f"{key} {view.altitude_m:.0f} m {_worst(got, key)}")
 
     def _worst(got, key):
