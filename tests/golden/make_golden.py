@@ -427,6 +427,147 @@ def shading_reference(reference: Path) -> dict:
     return out
 
 
+RASTER_CASES = [
+    # (width, height, patches, resolution, active slots, mode, tangent_half_fov, near, seed, skirt masks)
+    (40, 24, 3, 4, (2, 0, 1), 0, 0.57735, 0.5, 21, (0b0101, 0, 0b1111)),
+    (33, 19, 2, 3, (1, 0), 1, 0.45, 2.0, 22, (0, 0)),     # height-band view, narrower field of view
+    (40, 24, 3, 4, (0, 2), 2, 0.57735, 0.5, 23, (0b0010, 0b1000, 0)),  # LOD-level hue view, one slot inactive
+    (24, 24, 2, 5, (0, 1), 3, 0.8, 1.0, 24, (0b1111, 0b1111)),      # slot-hash view
+]
+
+
+def raster_mesh(w, h, patches, resolution, seed):
+    """Seeded terrain patches in view space (x right, y up, z forward): a
+    heightfield grid of (resolution + 1)^2 vertices per patch in front of
+    and below the camera, wide enough to cross every frustum plane and the
+    near plane; odd patches wound the other way (culled as back faces)."""
+
+    rng = np.random.default_rng(seed)
+    side = resolution + 1
+    n_vert = side * side
+    view = np.zeros((patches, n_vert, 3), np.float32)
+    for p in range(patches):
+        x0, z0 = rng.uniform(-90.0, -40.0), rng.uniform(-6.0, 4.0) + 20.0 * p
+        span = rng.uniform(90.0, 140.0)
+        for j in range(side):
+            for i in range(side):
+                x = x0 + span * i / resolution
+                z = z0 + span * j / resolution
+                y = -12.0 + 0.02 * z + rng.normal(0.0, 0.4)
+                view[p, j * side + i] = (x, y, z)
+    normal = np.zeros_like(view)
+    normal[..., 1] = 1.0
+    normal += rng.normal(0.0, 0.2, normal.shape).astype(np.float32)
+    material = rng.dirichlet(np.ones(4), (patches, n_vert)).astype(np.float32)
+    height = rng.uniform(-1500.0, 4500.0, (patches, n_vert)).astype(np.float32)
+    cell = rng.integers(0, 10_000, (patches, n_vert)).astype(np.int32)
+    tris = []
+    for j in range(resolution):
+        for i in range(resolution):
+            a, b, c, d = j * side + i, j * side + i + 1, (j + 1) * side + i, (j + 1) * side + i + 1
+            tris += [(a, b, c), (b, d, c)]
+    # skirts: four edges of 2 * resolution triangles each, double-sided (here
+    # the surface triangles re-wound, so that culled ones render as skirts)
+    for k in range(8 * resolution):
+        a, b, c = tris[k % len(tris)]
+        tris.append((a, c, b))
+    triangles = np.array(tris, np.int32)
+    for p in range(1, patches, 2):  # a back-facing patch: swap the winding of its vertices' rows
+        view[p] = view[p].reshape(side, side, 3)[:, ::-1].reshape(n_vert, 3)
+    return view, normal, material, height, cell, triangles
+
+
+def raster_reference(reference: Path) -> dict:
+    """The reference's terrain raster (PlanetRenderer._clip, _emit,
+    _raster_depth_direct, _resolve_raster, _surface_color;
+    src/planet_renderer/renderer.py:628-1269) run unmodified on seeded view-space
+    patches: triangles inside the frustum, crossing its side planes and the
+    near plane (Sutherland-Hodgman), trivially rejected and back-facing ones,
+    the atomic depth-key raster and the resolve into the G-buffer, in the lit
+    albedo mode and the three debug colourings."""
+
+    shim.install()
+    sys.path.insert(0, str(reference / "src"))
+    from planet_renderer.renderer import DEPTH_KEY_SENTINEL, MAX_CLIPPED_TRIANGLES, PlanetRenderer  # type: ignore
+
+    out = {}
+    for k, (w, h, patches, resolution, active, mode, tf, near, seed, skirts) in enumerate(RASTER_CASES):
+        view, normal, material, height, cell, triangles = raster_mesh(w, h, patches, resolution, seed)
+        n_vert = view.shape[1]
+        r = PlanetRenderer.__new__(PlanetRenderer)  # fields only: the kernels read nothing else
+        r.width, r.height = w, h
+        r.resolution = resolution
+        r.local_triangle_count = len(triangles)
+        r.surface_triangle_count = 2 * resolution * resolution
+        r.local_triangles = shim.Vector.field(3, dtype=shim.i32, shape=len(triangles))
+        r.local_triangles.from_numpy(triangles)
+        r.active_slot_ids = shim.field(dtype=shim.i32, shape=patches)
+        r.active_slot_ids.from_numpy(np.array(list(active) + [0] * (patches - len(active)), np.int32))
+        r.active_slot_count = shim.field(dtype=shim.i32, shape=())
+        r.active_slot_count[None] = len(active)
+        r.slot_skirt_mask = shim.field(dtype=shim.i32, shape=patches)
+        r.slot_skirt_mask.from_numpy(np.array(skirts, np.int32))
+        for name, values, n in (("view", view, 3), ("frame_normal", normal, 3), ("frame_material", material, 4)):
+            fld = shim.Vector.field(n, dtype=shim.f32, shape=(patches, n_vert))
+            fld.from_numpy(values)
+            setattr(r, name, fld)
+        r.frame_height_m = shim.field(dtype=shim.f32, shape=(patches, n_vert))
+        r.frame_height_m.from_numpy(height)
+        r.frame_cell = shim.field(dtype=shim.i32, shape=(patches, n_vert))
+        r.frame_cell.from_numpy(cell)
+        cap = patches * len(triangles) * MAX_CLIPPED_TRIANGLES
+        r.raster_capacity = cap
+        for name, n, dt in (("rv", 3, shim.f32), ("rn", 3, shim.f32), ("rm", 4, shim.f32), ("screen", 3, shim.f32),
+                            ("edge_equation", 3, shim.f32)):
+            setattr(r, name, shim.Vector.field(n, dtype=dt, shape=(cap, 3)))
+        r.rh = shim.field(dtype=shim.f32, shape=(cap, 3))
+        r.rc = shim.field(dtype=shim.i32, shape=(cap, 3))
+        r.source = shim.field(dtype=shim.i32, shape=cap)
+        r.inv_area = shim.field(dtype=shim.f32, shape=cap)
+        r.edge_top_left = shim.Vector.field(3, dtype=shim.i32, shape=cap)
+        r.clipped_count = shim.field(dtype=shim.i32, shape=())
+        r.depth_key = shim.field(dtype=shim.u64, shape=(w, h))
+        r.depth_key.fill(DEPTH_KEY_SENTINEL)
+        r.depth = shim.field(dtype=shim.f32, shape=(w, h))
+        for name, n in (("gbuffer_position", 3), ("gbuffer_normal", 3), ("gbuffer_albedo", 3),
+                        ("gbuffer_material_weights", 4)):
+            setattr(r, name, shim.Vector.field(n, dtype=shim.f32, shape=(w, h)))
+        r.gbuffer_height_m = shim.field(dtype=shim.f32, shape=(w, h))
+        r.gbuffer_surface_id = shim.field(dtype=shim.i32, shape=(w, h))
+        r.gbuffer_surface_id.fill(-1)
+        r.gbuffer_surface_cell_id = shim.field(dtype=shim.i32, shape=(w, h))
+        r.gbuffer_surface_cell_id.fill(-1)
+        slot_level = np.arange(patches, dtype=np.int32) * 3 + 1
+
+        class _Terrain:  # the only TerrainRenderer field _surface_color reads (LOD-level view)
+            pass
+
+        r.terrain_renderer = _Terrain()
+        r.terrain_renderer.slot_level = shim.field(dtype=shim.i32, shape=patches)
+        r.terrain_renderer.slot_level.from_numpy(slot_level)
+        r._clip(near, tf)
+        r._raster_depth_direct(False)
+        r._resolve_raster(mode, False)
+        pre = f"case{k}_"
+        for name, values in (("view", view), ("normal", normal), ("material", material), ("height", height),
+                             ("cell", cell), ("triangles", triangles), ("slot_level", slot_level),
+                             ("skirt_mask", np.array(skirts, np.int32))):
+            out[pre + name] = values
+        out[pre + "clipped_count"] = np.array(int(r.clipped_count[None]))
+        for name, fld in (("depth", r.depth), ("position", r.gbuffer_position), ("gb_normal", r.gbuffer_normal),
+                          ("albedo", r.gbuffer_albedo), ("material_weights", r.gbuffer_material_weights),
+                          ("height_m", r.gbuffer_height_m), ("surface_id", r.gbuffer_surface_id),
+                          ("cell_id", r.gbuffer_surface_cell_id)):
+            out[pre + name] = fld.to_numpy()
+        out[pre + "args"] = np.array(json.dumps({"width": w, "height": h, "patches": patches,
+                                                 "resolution": resolution, "active": list(active), "mode": mode,
+                                                 "tangent_half_fov": tf, "near": near, "seed": seed}))
+    out["meta"] = np.array(json.dumps({"name": "raster", "cases": len(RASTER_CASES),
+                                       "generator": "reference renderer.py _clip/_raster_depth_direct/_resolve_raster "
+                                                    "through taichi_f32_shim"}))
+    return out
+
+
 def earth_config1_kwargs():
     return dict(
         mie_extinction_per_m=(3.996e-6 + 4.4e-6,) * 3,
@@ -472,6 +613,8 @@ def main() -> None:
         np.savez_compressed(HERE / "model_reference.npz", **model_reference(args.reference))
     if want("shading") and args.precision == "f32":
         np.savez_compressed(HERE / "shading.npz", **shading_reference(args.reference))
+    if want("raster") and args.precision == "f32":
+        np.savez_compressed(HERE / "raster.npz", **raster_reference(args.reference))
     if want("postprocess") and args.precision == "f32":
         np.savez_compressed(HERE / "postprocess.npz", **postprocess_reference(args.reference))
     renderer = None

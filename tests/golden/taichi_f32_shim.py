@@ -44,7 +44,15 @@ f64 = np.float64
 u8 = np.uint8
 u16 = np.uint16
 u32 = np.uint32
-u64 = np.uint64
+class _U64:
+    """ti.u64: a field dtype, and as a call a Python integer (numpy uint64
+    does not mix with Python integers in bit operations)."""
+
+    def __call__(self, value):
+        return int(value) & 0xFFFFFFFFFFFFFFFF
+
+
+u64 = _U64()
 i8 = np.int8
 i16 = np.int16
 i64 = np.int64
@@ -111,6 +119,11 @@ class Vec(np.ndarray):
             acc = acc + self[k] * other[k]
         return acc
 
+    def cross(self, other):
+        a, b = self, other
+        return Vec([a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]],
+                   dtype=self.dtype)
+
     def norm_sqr(self):
         return self.dot(self)
 
@@ -165,17 +178,37 @@ def clear_restrictions() -> None:
     _RESTRICT.clear()
 
 
+class IntRef(int):
+    """An integer read from a scalar field element that remembers where it
+    came from, so that ``ti.atomic_add(field[i], v)`` can update the field
+    (Python passes the value, not the element)."""
+
+    def __new__(cls, value, field, key):
+        obj = int.__new__(cls, int(value))
+        obj.field, obj.key = field, key
+        return obj
+
+
 class Field:
     """Dense field: vector elements (n>0) or scalars (n=0)."""
 
     def __init__(self, n, dtype, shape):
         self.n = int(n)
-        self.dtype = _FLOAT if dtype in (f32, float) else np.int32
+        if dtype in (f32, float):
+            self.dtype = _FLOAT
+        elif dtype is u64:
+            self.dtype = np.uint64
+        elif dtype in (u32, i64):
+            self.dtype = np.dtype(dtype).type
+        else:
+            self.dtype = np.int32
         self.shape = tuple(int(s) for s in (shape if isinstance(shape, tuple) else (shape,)))
         full = self.shape + ((self.n,) if self.n else ())
         self.data = np.zeros(full, dtype=self.dtype)
 
     def _key(self, idx):
+        if idx is None:
+            return ()
         if isinstance(idx, (tuple, list, np.ndarray)):
             return tuple(int(v) for v in idx)
         return (int(idx),)
@@ -183,13 +216,19 @@ class Field:
     def __getitem__(self, idx):
         key = self._key(idx)
         if self.n:
-            return Vec(self.data[key])
-        return self.data[key]
+            return Vec(self.data[key], dtype=self.dtype)
+        value = self.data[key]
+        if np.issubdtype(self.dtype, np.integer):
+            return IntRef(value, self, key)
+        return value
 
     def __setitem__(self, idx, value):
         key = self._key(idx)
         _check_f32(value)
-        self.data[key] = np.asarray(value, dtype=self.dtype)
+        if np.issubdtype(self.dtype, np.integer) and not self.n:
+            self.data[key] = self.dtype(int(value))
+        else:
+            self.data[key] = np.asarray(value, dtype=self.dtype)
 
     def _indices(self):
         if id(self) in _RESTRICT:
@@ -218,6 +257,8 @@ class _VectorNamespace:
 
     @staticmethod
     def zero(dtype, n):
+        if dtype is i32:
+            return Vec(np.zeros(n, dtype=np.int64), dtype=np.int64)
         return Vec(np.zeros(n, dtype=_FLOAT))
 
     @staticmethod
@@ -226,6 +267,63 @@ class _VectorNamespace:
 
 
 Vector = _VectorNamespace()
+
+
+class Mat(np.ndarray):
+    """Small matrix with value semantics; ``m[k, :]`` is a row vector."""
+
+    def __setitem__(self, item, value):
+        # write through the base array (numpy routes a subclass's slice
+        # assignment through its __getitem__, which returns copies here)
+        np.ndarray.__setitem__(self.view(np.ndarray), item, np.asarray(value))
+
+    def __getitem__(self, item):
+        value = np.ndarray.__getitem__(self, item)
+        if isinstance(value, np.ndarray):
+            if value.ndim == 0:
+                return value[()]
+            if value.ndim == 1:
+                return Vec(np.array(value), dtype=value.dtype)
+        return value
+
+
+class _MatrixNamespace:
+    @staticmethod
+    def rows(rows):
+        return np.array([np.asarray(r) for r in rows]).view(Mat)
+
+    @staticmethod
+    def zero(dtype, r, c):
+        return np.zeros((r, c), dtype=np.int64 if dtype is i32 else _FLOAT).view(Mat)
+
+
+Matrix = _MatrixNamespace()
+
+
+def atomic_add(ref, value):
+    """Add to the field element ``ref`` was read from; returns the old value."""
+
+    old = int(ref.field.data[ref.key])
+    ref.field.data[ref.key] = ref.field.dtype(old + int(value))
+    return old
+
+
+def atomic_min(ref, value):
+    old = int(ref.field.data[ref.key])
+    ref.field.data[ref.key] = ref.field.dtype(_builtins.min(old, int(value)))
+    return old
+
+
+def bit_cast(value, dtype):
+    if dtype is u32:
+        return int(np.array(value, dtype=np.float32).view(np.uint32))
+    if dtype is f32:
+        return np.array(int(value), dtype=np.uint32).view(np.float32)[()]
+    raise TypeError(f"bit_cast to {dtype} not supported")
+
+
+def loop_config(**kwargs):
+    return None
 
 
 def field(dtype=f32, shape=()):
@@ -238,7 +336,10 @@ def grouped(fld):
 
 
 def ndrange(*sizes):
-    return itertools.product(*(range(int(s)) for s in sizes))
+    """Sizes are extents or (start, stop) pairs."""
+
+    ranges = [range(int(s[0]), int(s[1])) if isinstance(s, (tuple, list)) else range(int(s)) for s in sizes]
+    return itertools.product(*ranges)
 
 
 def static(value):
@@ -246,6 +347,8 @@ def static(value):
 
 
 def cast(value, dtype):
+    if dtype in (u64, u32):
+        return int(value)
     if dtype is i32:
         if isinstance(value, (np.ndarray, tuple, list)):  # vectors: element-wise, truncating
             return Vec(np.trunc(np.asarray(value, dtype=np.float64)).astype(np.int64), dtype=np.int64)
@@ -283,6 +386,7 @@ cos = _unary(np.cos, _pymath.cos)
 sin = _unary(np.sin, _pymath.sin)
 abs = _unary(np.abs, _builtins.abs)  # noqa: A001 - mirrors ti.abs
 floor = _unary(np.floor, _pymath.floor)
+ceil = _unary(np.ceil, _pymath.ceil)
 tan = _unary(np.tan, _pymath.tan)
 
 
@@ -298,13 +402,17 @@ def atan2(y, x):
     return np.arctan2(y, x)
 
 
-def max(a, b):  # noqa: A001 - mirrors ti.max
+def max(a, b, *more):  # noqa: A001 - mirrors ti.max
+    if more:
+        return max(max(a, b), *more)
     if _is_py(a) and _is_py(b):
         return _builtins.max(a, b)
     return np.maximum(a, b)
 
 
-def min(a, b):  # noqa: A001 - mirrors ti.min
+def min(a, b, *more):  # noqa: A001 - mirrors ti.min
+    if more:
+        return min(min(a, b), *more)
     if _is_py(a) and _is_py(b):
         return _builtins.min(a, b)
     return np.minimum(a, b)
@@ -314,6 +422,10 @@ class _Math:
     @staticmethod
     def clamp(x, lo, hi):
         return min(max(x, lo), hi)
+
+    @staticmethod
+    def fract(x):
+        return x - floor(x)
 
     pi = _pymath.pi
 
