@@ -573,6 +573,65 @@ int atm_render_frame(AtmHandle* handle, const AtmShadeParams* shade, const AtmSh
                      double tangent_half_fov, double star_contrast_start, double star_contrast_end,
                      const AtmSurrogate* surrogate, void* stream);
 
+/* ---- terrain raster: the G-buffer producer ----------------------------------
+ * PlanetRenderer's terrain raster (src/planet_renderer/renderer.py :628-1269),
+ * the step before the atmosphere stage: _clip (back-face culling of surface
+ * triangles, skirts double-sided, trivial reject, Sutherland-Hodgman against
+ * the near plane and the frustum sides), _emit (projection snapped to 1/256
+ * pixel, edge equations, top-left rule), _raster_depth_direct (an atomic
+ * 64-bit minimum of depth bits << 32 | triangle per covered pixel centre) and
+ * _resolve_raster with _surface_color (perspective-correct attributes of the
+ * nearest triangle, the albedo of the view mode).  The patches' vertex
+ * streams are the camera-view-space output of the terrain's LOD system,
+ * which is not part of this library. */
+typedef struct AtmRasterMesh {
+  const float* view;        /* [patches][vertices_per_patch][3] view space (right, up, forward), m */
+  const float* normal;      /* [patches][vertices_per_patch][3] */
+  const float* material;    /* [patches][vertices_per_patch][4] material weights */
+  const float* height_m;    /* [patches][vertices_per_patch] terrain height */
+  const int32_t* cell;      /* [patches][vertices_per_patch] cell ids */
+  const int32_t* triangles; /* [triangles_per_patch][3] vertex indices within a patch: the
+                               surface triangles, then the skirts (4 edges x 2 resolution) */
+  const int32_t* active_slots; /* [n_active] the patches (slots) to draw, in order */
+  const int32_t* skirt_mask;   /* [patches] bit e enables skirt edge e, or null: no skirts */
+  const int32_t* slot_level;   /* [patches] LOD level (view mode 2), or null */
+  int32_t patches, vertices_per_patch, triangles_per_patch, surface_triangles_per_patch;
+  int32_t resolution;          /* cells per patch side (2 resolution skirt triangles per edge) */
+  int32_t n_active;
+} AtmRasterMesh;
+/* Device G-buffer images sharing `image`'s shape and element strides:
+ * position (view space), normal, albedo with image->channels floats per
+ * element, material_weights 4 floats, depth and height_m one float,
+ * surface_id and cell_id one int32.  Uncovered pixels get surface_id = -1
+ * and cell_id = -1; their other values are left as they were (as the
+ * reference leaves them). */
+typedef struct AtmRasterOutputs {
+  float* depth;
+  float* position;
+  float* normal;
+  float* albedo;
+  float* material_weights;
+  float* height_m;
+  int32_t* surface_id;
+  int32_t* cell_id;
+} AtmRasterOutputs;
+typedef struct AtmRaster AtmRaster;
+/* PlanetRenderer's raster buffers (renderer.py:200-236): the emitted-triangle
+ * stream (max_patches x triangles_per_patch x 6 triangles) and the depth keys
+ * of a width x height frame. */
+int atm_raster_create(int32_t width, int32_t height, int32_t max_patches, int32_t triangles_per_patch,
+                      AtmRaster** out);
+int atm_raster_destroy(AtmRaster* raster);
+/* _clip + _raster_depth_direct + _resolve_raster of one frame (view_mode: 0
+ * lit albedo, 1 height bands, 2 LOD-level hue, 3 patch hash; renderer.py
+ * :1008-1058).  Stream-ordered; allocates nothing. */
+int atm_raster_terrain(AtmRaster* raster, const AtmRasterMesh* mesh, double near_m, double tangent_half_fov,
+                       int32_t view_mode, const AtmRasterOutputs* outputs, const AtmImage* image, void* stream);
+/* Triangles the last atm_raster_terrain emitted (clipped_count; synchronises
+ * `stream`).  More than the stream's capacity means some were dropped, as
+ * the reference drops them. */
+int atm_raster_emitted(const AtmRaster* raster, int64_t* count, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

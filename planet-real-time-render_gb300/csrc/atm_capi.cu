@@ -1429,3 +1429,106 @@ ATM_API int atm_render_frame(AtmHandle* h, const AtmShadeParams* shade, const At
            "fused surrogate frame");
   return ATM_OK;
 }
+
+// ---- terrain raster ----------------------------------------------------------
+struct AtmRaster {
+  int32_t width = 0, height = 0, max_patches = 0, triangles_per_patch = 0;
+  atm::RasterTri* tris = nullptr;
+  long long capacity = 0;
+  uint32_t* count = nullptr;
+  unsigned long long* depth_key = nullptr;
+  int sm_count = 0;
+};
+
+ATM_API int atm_raster_create(int32_t width, int32_t height, int32_t max_patches, int32_t triangles_per_patch,
+                              AtmRaster** out) {
+  if (!out) return fail(ATM_E_INVALID, "null output pointer");
+  *out = nullptr;
+  if (width < 1 || height < 1 || width > 16384 || height > 16384)
+    return fail(ATM_E_INVALID, "raster size must be 1..16384 a side");
+  if (max_patches < 1 || triangles_per_patch < 1)
+    return fail(ATM_E_INVALID, "max_patches and triangles_per_patch must be positive");
+  const long long capacity = (long long)max_patches * triangles_per_patch * 6;  // MAX_CLIPPED_TRIANGLES
+  if (capacity > 0xffffffffll) return fail(ATM_E_INVALID, "triangle stream over 2^32 triangles");
+  AtmRaster* r = new (std::nothrow) AtmRaster;
+  if (!r) return fail(ATM_E_NOMEM, "host allocation failed");
+  r->width = width;
+  r->height = height;
+  r->max_patches = max_patches;
+  r->triangles_per_patch = triangles_per_patch;
+  r->capacity = capacity;
+  cudaError_t e = cudaMalloc(&r->tris, sizeof(atm::RasterTri) * size_t(capacity));
+  if (e == cudaSuccess) e = cudaMalloc(&r->count, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&r->depth_key, sizeof(unsigned long long) * size_t(width) * height);
+  int dev = 0;
+  if (e == cudaSuccess) e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&r->sm_count, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) {
+    atm_raster_destroy(r);
+    return e == cudaErrorMemoryAllocation ? fail(ATM_E_NOMEM, "raster allocation failed") : cuda_fail(e, "raster");
+  }
+  *out = r;
+  return ATM_OK;
+}
+
+ATM_API int atm_raster_destroy(AtmRaster* r) {
+  if (!r) return ATM_OK;
+  if (r->tris) cudaFree(r->tris);
+  if (r->count) cudaFree(r->count);
+  if (r->depth_key) cudaFree(r->depth_key);
+  delete r;
+  return ATM_OK;
+}
+
+ATM_API int atm_raster_terrain(AtmRaster* r, const AtmRasterMesh* m, double near_m, double tangent_half_fov,
+                               int32_t view_mode, const AtmRasterOutputs* o, const AtmImage* image, void* stream) {
+  if (!r || !m || !o || !image) return fail(ATM_E_INVALID, "null argument to atm_raster_terrain");
+  if (image->width != r->width || image->height != r->height)
+    return fail(ATM_E_INVALID, "image is %dx%d but the raster was created for %dx%d", image->width, image->height,
+                r->width, r->height);
+  if ((image->channels != 3 && image->channels != 4) || image->stride_x <= 0 || image->stride_y <= 0)
+    return fail(ATM_E_INVALID, "invalid AtmImage");
+  if (!m->view || !m->normal || !m->material || !m->height_m || !m->cell || !m->triangles ||
+      (m->n_active > 0 && !m->active_slots))
+    return fail(ATM_E_INVALID, "null mesh array");
+  if (!o->depth || !o->position || !o->normal || !o->albedo || !o->material_weights || !o->height_m ||
+      !o->surface_id || !o->cell_id)
+    return fail(ATM_E_INVALID, "null output image");
+  if (m->patches < 1 || m->patches > r->max_patches || m->triangles_per_patch != r->triangles_per_patch ||
+      m->vertices_per_patch < 3 || m->n_active < 0 || m->n_active > m->patches ||
+      m->surface_triangles_per_patch < 0 || m->surface_triangles_per_patch > m->triangles_per_patch ||
+      m->resolution < 1)
+    return fail(ATM_E_INVALID, "mesh sizes do not match the raster (patches %d of %d, triangles %d of %d)",
+                m->patches, r->max_patches, m->triangles_per_patch, r->triangles_per_patch);
+  if (m->triangles_per_patch > m->surface_triangles_per_patch &&
+      (m->triangles_per_patch - m->surface_triangles_per_patch) > 8 * m->resolution)
+    return fail(ATM_E_INVALID, "at most 4 edges x 2 resolution skirt triangles");
+  if (view_mode < 0 || view_mode > 3) return fail(ATM_E_INVALID, "view_mode must be 0..3");
+  if (view_mode == 2 && !m->slot_level) return fail(ATM_E_INVALID, "view mode 2 needs slot_level");
+  if (!(near_m > 0.0) || !(tangent_half_fov > 0.0) || !std::isfinite(near_m) || !std::isfinite(tangent_half_fov))
+    return fail(ATM_E_INVALID, "near plane and field of view must be positive and finite");
+  // host-side checks of the topology and active list (small arrays, device
+  // resident: validated once by a copy would need a sync; the kernels clamp
+  // nothing, so the caller's indices must be in range)
+  atm::RasterMeshDev M{m->view,       m->normal,     m->material,  m->height_m,
+                       m->cell,       m->triangles,  m->active_slots, m->skirt_mask,
+                       m->slot_level, m->patches,    m->vertices_per_patch, m->triangles_per_patch,
+                       m->surface_triangles_per_patch, m->resolution, m->n_active};
+  atm::RasterStream S{r->tris, r->count, r->capacity};
+  atm::RasterOutDev O{o->depth, o->position, o->normal, o->albedo, o->material_weights, o->height_m,
+                      o->surface_id, o->cell_id};
+  ATM_CUDA(atm::launch_raster(M, S, layout_of(image), r->depth_key, O, float(near_m), float(tangent_half_fov),
+                              view_mode, r->sm_count, static_cast<cudaStream_t>(stream)),
+           "terrain raster");
+  return ATM_OK;
+}
+
+ATM_API int atm_raster_emitted(const AtmRaster* r, int64_t* count, void* stream) {
+  if (!r || !count) return fail(ATM_E_INVALID, "null argument");
+  uint32_t v = 0;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ATM_CUDA(cudaMemcpyAsync(&v, r->count, sizeof(v), cudaMemcpyDeviceToHost, s), "raster count");
+  ATM_CUDA(cudaStreamSynchronize(s), "raster count");
+  *count = int64_t(v);
+  return ATM_OK;
+}

@@ -232,6 +232,53 @@ cudaError_t launch_frame(const DevParams& P, const ImageLayout& L, const Composi
                          const ShadeImages& I, const float* space, const float4* tlut, const float4* mslut,
                          const float4* svlut, float* hdr, unsigned long long* sample_counter, cudaStream_t s);
 
+// ---- terrain raster (the G-buffer producer) --------------------------------
+// One emitted (clipped) triangle: vertex view positions, normals, material
+// weights, heights and cell ids, its screen setup (pixels snapped to 1/256,
+// view depth), edge equations, top-left flags (bit k: edge k) and source id.
+struct RasterTri {
+  float v[3][3], n[3][3], m[3][4], h[3];
+  int32_t c[3];
+  float screen[3][3];
+  float eq[3][3];
+  float inv_area;
+  int32_t tl;
+  int32_t src;
+};
+struct RasterStream {
+  RasterTri* tris;
+  uint32_t* count;  // triangles emitted (may exceed capacity: only capacity are stored)
+  long long capacity;
+};
+struct RasterMeshDev {
+  const float* view;       // [patches][vertices][3]
+  const float* normal;     // [patches][vertices][3]
+  const float* material;   // [patches][vertices][4]
+  const float* height;     // [patches][vertices]
+  const int32_t* cell;     // [patches][vertices]
+  const int32_t* triangles;  // [triangles_per_patch][3]
+  const int32_t* active;     // [n_active] slots
+  const int32_t* skirt_mask; // [patches] or null
+  const int32_t* slot_level; // [patches] or null (view mode 2)
+  int patches, vertices_per_patch, triangles_per_patch, surface_triangles_per_patch, resolution, n_active;
+};
+// G-buffer outputs at the layout's element strides: position, normal and
+// albedo with L.channels floats per element, material 4 floats, depth and
+// height one float, ids one int32.
+struct RasterOutDev {
+  float* depth;
+  float* position;
+  float* normal;
+  float* albedo;
+  float* material;
+  float* height;
+  int32_t* surface_id;
+  int32_t* cell_id;
+};
+cudaError_t launch_raster(const RasterMeshDev& M, const RasterStream& S, const ImageLayout& L,
+                          unsigned long long* depth_key, const RasterOutDev& O, float near, float tf, int mode,
+                          int sm_count, cudaStream_t s);
+
 // Whether x is the image's contiguous axis (the orientation of its bloom planes).
 bool image_x_fast(const ImageLayout& L);
 // A bloom plane of orientation Q.x_fast copied into dst as float4 [y][x].

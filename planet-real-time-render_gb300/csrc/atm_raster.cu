@@ -1,0 +1,386 @@
+// atm_raster.cu - the terrain raster that produces the G-buffer the
+// atmosphere stage consumes (PlanetRenderer._clip, _emit,
+// _raster_depth_direct, _resolve_raster; src/planet_renderer/renderer.py
+// :628-1269) on sm_103a.
+//
+//  * k_raster_clip: thread per source triangle of the active patches:
+//    back-face culling of surface triangles (skirts are double-sided), the
+//    clip-code trivial reject, Sutherland-Hodgman clipping against the near
+//    plane and the four frustum sides, and the emission (an atomic append)
+//    of each resulting triangle with its screen setup: projection snapped to
+//    1/256 pixel, edge equations, top-left flags, inverse area;
+//  * k_raster_depth: warp per emitted triangle, lanes over the pixels of its
+//    bounding box: coverage by the edge equations with the top-left rule and
+//    a 64-bit atomic minimum of (depth bits << 32 | triangle) per pixel;
+//  * k_raster_resolve: thread per pixel: the winning triangle's
+//    perspective-correct position, normal, material weights and height, the
+//    dominant vertex's cell id and the albedo of the view mode.
+//
+// Arithmetic is IEEE float32 in the reference's operation order without
+// contraction (__fmul_rn / __fadd_rn / __fdiv_rn), so every written value
+// equals the reference's.  Triangles get their stream slot from an atomic
+// counter, so their order (the key's low bits) differs from the
+// reference's sequential order: only the winner of an exact depth tie can
+// differ.
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "atm_kernels.h"
+
+namespace atm {
+
+namespace {
+
+constexpr int kClipVerts = 8;      // MAX_CLIP_VERTICES
+constexpr int kClipTris = 6;       // MAX_CLIPPED_TRIANGLES
+constexpr unsigned long long kSentinel = ~0ull;
+
+struct r3 {
+  float x, y, z;
+};
+__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float dv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
+__device__ __forceinline__ float fmn(float a, float b) { return a < b ? a : b; }
+__device__ __forceinline__ r3 R3(float x, float y, float z) { return {x, y, z}; }
+__device__ __forceinline__ r3 radd(r3 a, r3 b) { return {add(a.x, b.x), add(a.y, b.y), add(a.z, b.z)}; }
+__device__ __forceinline__ r3 rsub(r3 a, r3 b) { return {sub(a.x, b.x), sub(a.y, b.y), sub(a.z, b.z)}; }
+__device__ __forceinline__ r3 rscale(r3 a, float s) { return {mul(a.x, s), mul(a.y, s), mul(a.z, s)}; }
+__device__ __forceinline__ float rdot(r3 a, r3 b) { return add(add(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z)); }
+__device__ __forceinline__ r3 rcross(r3 a, r3 b) {
+  return {sub(mul(a.y, b.z), mul(a.z, b.y)), sub(mul(a.z, b.x), mul(a.x, b.z)), sub(mul(a.x, b.y), mul(a.y, b.x))};
+}
+// Taichi's normalized(): (1 / (|v| + 0)) * v
+__device__ __forceinline__ r3 rnormalized(r3 v) {
+  const float inv = dv(1.0f, add(__fsqrt_rn(rdot(v, v)), 0.0f));
+  return {mul(inv, v.x), mul(inv, v.y), mul(inv, v.z)};
+}
+struct r4 {
+  float v[4];
+};
+
+// One clip-space vertex with its attributes.
+struct CVert {
+  r3 p, n;
+  r4 m;
+  float h;
+  int32_t c;
+};
+
+__device__ __forceinline__ int clip_code(r3 p, float near, float tx, float ty) {
+  int code = 0;
+  if (p.z < near) code |= 1;
+  if (p.x < mul(-p.z, tx)) code |= 2;
+  if (p.x > mul(p.z, tx)) code |= 4;
+  if (p.y < mul(-p.z, ty)) code |= 8;
+  if (p.y > mul(p.z, ty)) code |= 16;
+  return code;
+}
+__device__ __forceinline__ float clip_distance(r3 p, int plane, float near, float tx, float ty) {
+  if (plane == 1) return add(p.x, mul(p.z, tx));
+  if (plane == 2) return add(-p.x, mul(p.z, tx));
+  if (plane == 3) return add(p.y, mul(p.z, ty));
+  if (plane == 4) return add(-p.y, mul(p.z, ty));
+  return sub(p.z, near);
+}
+__device__ __forceinline__ r3 edge_coeff(float ax, float ay, float bx, float by) {
+  return {sub(ay, by), sub(bx, ax), sub(mul(sub(by, ay), ax), mul(sub(bx, ax), ay))};
+}
+__device__ __forceinline__ int top_left(float ax, float ay, float bx, float by, float o) {
+  const float dx = mul(sub(bx, ax), o), dy = mul(sub(by, ay), o);
+  return (dy > 0.0f) || (dy == 0.0f && dx < 0.0f);
+}
+
+// _emit :628-686
+__device__ void emit(const RasterMeshDev& M, RasterStream S, int32_t src, const CVert (&v)[3], float tf,
+                     float aspect, int width, int height) {
+  const uint32_t s = atomicAdd(S.count, 1u);
+  if (s >= uint32_t(S.capacity)) return;  // counted, not stored (the reference's s >= capacity)
+  RasterTri& T = S.tris[s];
+  float sp[3][3];
+  for (int k = 0; k < 3; ++k) {
+    const r3 p = v[k].p;
+    T.v[k][0] = p.x;
+    T.v[k][1] = p.y;
+    T.v[k][2] = p.z;
+    T.n[k][0] = v[k].n.x;
+    T.n[k][1] = v[k].n.y;
+    T.n[k][2] = v[k].n.z;
+    for (int i = 0; i < 4; ++i) T.m[k][i] = v[k].m.v[i];
+    T.h[k] = v[k].h;
+    T.c[k] = v[k].c;
+    float px = mul(add(mul(dv(p.x, mul(mul(p.z, tf), aspect)), 0.5f), 0.5f), float(width));
+    float py = mul(add(mul(dv(p.y, mul(p.z, tf)), 0.5f), 0.5f), float(height));
+    px = dv(floorf(add(mul(px, 256.0f), 0.5f)), 256.0f);
+    py = dv(floorf(add(mul(py, 256.0f), 0.5f)), 256.0f);
+    sp[k][0] = px;
+    sp[k][1] = py;
+    sp[k][2] = p.z;
+    T.screen[k][0] = px;
+    T.screen[k][1] = py;
+    T.screen[k][2] = p.z;
+  }
+  const float ax = sp[0][0], ay = sp[0][1], bx = sp[1][0], by = sp[1][1], cx = sp[2][0], cy = sp[2][1];
+  const float area = sub(mul(sub(bx, ax), sub(cy, ay)), mul(sub(by, ay), sub(cx, ax)));  // _edge(a, b, c)
+  const float abs_area = fabsf(area);
+  const float sg = area > 0.0f ? 1.0f : -1.0f;
+  T.inv_area = abs_area > 1e-8f ? dv(1.0f, abs_area) : 0.0f;
+  const r3 e0 = rscale(edge_coeff(bx, by, cx, cy), sg);
+  const r3 e1 = rscale(edge_coeff(cx, cy, ax, ay), sg);
+  const r3 e2 = rscale(edge_coeff(ax, ay, bx, by), sg);
+  T.eq[0][0] = e0.x, T.eq[0][1] = e0.y, T.eq[0][2] = e0.z;
+  T.eq[1][0] = e1.x, T.eq[1][1] = e1.y, T.eq[1][2] = e1.z;
+  T.eq[2][0] = e2.x, T.eq[2][1] = e2.y, T.eq[2][2] = e2.z;
+  T.tl = top_left(bx, by, cx, cy, sg) | (top_left(cx, cy, ax, ay, sg) << 1) | (top_left(ax, ay, bx, by, sg) << 2);
+  T.src = src;
+}
+
+// _clip :731-901
+__global__ void __launch_bounds__(128) k_raster_clip(RasterMeshDev M, RasterStream S, float near, float tf,
+                                                     int width, int height) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int ltc = M.triangles_per_patch;
+  if (i >= (long long)M.n_active * ltc) return;
+  const float aspect = dv(float(width), float(height));
+  const float tx = mul(tf, aspect), ty = tf;
+  const int slot = M.active[i / ltc];
+  if (slot < 0 || slot >= M.patches) return;  // not a patch: nothing to draw
+  const int local_id = int(i % ltc);
+  const int32_t source_id = slot * ltc + local_id;
+  const int stc = M.surface_triangles_per_patch;
+  if (local_id >= stc) {  // a skirt: enabled per patch edge
+    const int edge = (local_id - stc) / (M.resolution * 2);
+    if (M.skirt_mask == nullptr || (M.skirt_mask[slot] & (1 << edge)) == 0) return;
+  }
+  const int32_t* ids = M.triangles + 3 * local_id;
+  for (int k = 0; k < 3; ++k)
+    if (ids[k] < 0 || ids[k] >= M.vertices_per_patch) return;  // a vertex outside the patch: dropped
+  CVert v[3];
+  for (int k = 0; k < 3; ++k) {
+    const long long e = (long long)slot * M.vertices_per_patch + ids[k];
+    v[k].p = R3(M.view[3 * e], M.view[3 * e + 1], M.view[3 * e + 2]);
+    v[k].n = R3(M.normal[3 * e], M.normal[3 * e + 1], M.normal[3 * e + 2]);
+    for (int j = 0; j < 4; ++j) v[k].m.v[j] = M.material[4 * e + j];
+    v[k].h = M.height[e];
+    v[k].c = M.cell[e];
+  }
+  // ordinary terrain back faces are culled; skirts stay double-sided
+  if (local_id < stc) {
+    const r3 p0 = v[0].p;
+    if (!(rdot(rcross(rsub(v[1].p, p0), rsub(v[2].p, p0)), R3(-p0.x, -p0.y, -p0.z)) < 0.0f)) return;
+  }
+  const int c0 = clip_code(v[0].p, near, tx, ty), c1 = clip_code(v[1].p, near, tx, ty),
+            c2 = clip_code(v[2].p, near, tx, ty);
+  if (c0 & c1 & c2) return;  // all three outside one plane
+  if ((c0 | c1 | c2) == 0) {
+    emit(M, S, source_id, v, tf, aspect, width, height);
+    return;
+  }
+  // Sutherland-Hodgman over the five planes, ping-ponging two vertex buffers
+  CVert buf[2][kClipVerts];
+  for (int k = 0; k < 3; ++k) buf[0][k] = v[k];
+  int count = 3, rd = 0;
+  for (int plane = 0; plane < 5; ++plane) {
+    const int wr = 1 - rd;
+    int oc = 0;
+    for (int vertex = 0; vertex < kClipVerts; ++vertex) {
+      if (vertex >= count) break;
+      const int prev = (vertex + count - 1) % count;
+      const CVert& cur = buf[rd][vertex];
+      const CVert& pre = buf[rd][prev];
+      const float cd = clip_distance(cur.p, plane, near, tx, ty);
+      const float pd = clip_distance(pre.p, plane, near, tx, ty);
+      const bool ci = cd >= 0.0f, pi = pd >= 0.0f;
+      if (ci != pi && oc < kClipVerts) {
+        const float den = sub(pd, cd);
+        const float t = fabsf(den) > 1e-20f ? dv(pd, den) : 0.0f;
+        CVert& o = buf[wr][oc];
+        o.p = radd(pre.p, rscale(rsub(cur.p, pre.p), t));
+        o.n = rnormalized(radd(pre.n, rscale(rsub(cur.n, pre.n), t)));
+        for (int j = 0; j < 4; ++j) o.m.v[j] = add(pre.m.v[j], mul(sub(cur.m.v[j], pre.m.v[j]), t));
+        o.h = add(pre.h, mul(sub(cur.h, pre.h), t));
+        o.c = ci ? cur.c : pre.c;
+        ++oc;
+      }
+      if (ci && oc < kClipVerts) buf[wr][oc++] = cur;
+    }
+    count = oc;
+    rd = wr;
+  }
+  for (int tri = 0; tri < kClipTris; ++tri) {
+    if (tri >= count - 2) break;
+    const CVert t3[3] = {buf[rd][0], buf[rd][tri + 1], buf[rd][tri + 2]};
+    emit(M, S, source_id, t3, tf, aspect, width, height);
+  }
+}
+
+__device__ __forceinline__ r3 edge_values(const RasterTri& T, float px, float py) {
+  return {add(add(mul(T.eq[0][0], px), mul(T.eq[0][1], py)), T.eq[0][2]),
+          add(add(mul(T.eq[1][0], px), mul(T.eq[1][1], py)), T.eq[1][2]),
+          add(add(mul(T.eq[2][0], px), mul(T.eq[2][1], py)), T.eq[2][2])};
+}
+__device__ __forceinline__ bool inside_edges(const RasterTri& T, r3 e) {
+  return (e.x > 0.0f || (e.x == 0.0f && (T.tl & 1))) && (e.y > 0.0f || (e.y == 0.0f && (T.tl & 2))) &&
+         (e.z > 0.0f || (e.z == 0.0f && (T.tl & 4)));
+}
+
+// _raster_depth_direct :1158-1206.  A warp per triangle (grid-stride over
+// the emitted stream); lanes over the bounding box's pixels.
+__global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayout L,
+                                                      unsigned long long* __restrict__ depth_key) {
+  const int lane = threadIdx.x & 31;
+  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
+  const long long n = min((long long)*S.count, (long long)S.capacity);
+  for (long long q = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); q < n; q += warps) {
+    const RasterTri& T = S.tris[q];
+    if (!(T.inv_area > 0.0f)) continue;
+    const float ax = T.screen[0][0], bx = T.screen[1][0], cx = T.screen[2][0];
+    const float ay = T.screen[0][1], by = T.screen[1][1], cy = T.screen[2][1];
+    const int x0 = max(int(floorf(fmn(fmn(ax, bx), cx))), 0);
+    const int x1 = min(int(ceilf(fmx(fmx(ax, bx), cx))), L.width - 1);
+    const int y0 = max(int(floorf(fmn(fmn(ay, by), cy))), 0);
+    const int y1 = min(int(ceilf(fmx(fmx(ay, by), cy))), L.height - 1);
+    if (x0 > x1 || y0 > y1) continue;
+    const int bw = x1 - x0 + 1;
+    const long long area = (long long)bw * (y1 - y0 + 1);
+    const float az = T.screen[0][2], bz = T.screen[1][2], cz = T.screen[2][2];
+    for (long long k = lane; k < area; k += 32) {
+      const int x = x0 + int(k % bw), y = y0 + int(k / bw);
+      const r3 e = edge_values(T, add(float(x), 0.5f), add(float(y), 0.5f));
+      if (!inside_edges(T, e)) continue;
+      const r3 l = rscale(e, T.inv_area);
+      const float z = dv(1.0f, fmx(add(add(dv(l.x, az), dv(l.y, bz)), dv(l.z, cz)), 1e-20f));
+      const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | (unsigned long long)q;
+      atomicMin(depth_key + (size_t(x) * L.height + y), key);
+    }
+  }
+}
+
+__device__ __forceinline__ r3 mix3(r3 a, r3 b, float t) { return radd(rscale(a, sub(1.0f, t)), rscale(b, t)); }
+__device__ __forceinline__ float clamp01(float x) { return fmn(fmx(x, 0.0f), 1.0f); }
+
+// _height_band :976-1006
+__device__ r3 height_band(float h) {
+  const r3 deep = R3(0.015f, 0.12f, 0.34f), shallow = R3(0.02f, 0.63f, 0.82f), beach = R3(0.82f, 0.78f, 0.48f);
+  const r3 lowland = R3(0.16f, 0.58f, 0.22f), upland = R3(0.48f, 0.42f, 0.16f), rock = R3(0.43f, 0.39f, 0.35f);
+  const r3 snow = R3(0.94f, 0.96f, 0.98f);
+  if (h < -250.0f) return mix3(deep, shallow, clamp01(dv(add(h, 5000.0f), 4750.0f)));
+  if (h < 0.0f) return shallow;
+  if (h < 120.0f) return mix3(beach, lowland, clamp01(dv(h, 120.0f)));
+  if (h < 1400.0f) return mix3(lowland, upland, clamp01(dv(sub(h, 120.0f), 1280.0f)));
+  if (h < 3000.0f) return mix3(upland, rock, clamp01(dv(sub(h, 1400.0f), 1600.0f)));
+  return mix3(rock, snow, clamp01(dv(sub(h, 3000.0f), 1400.0f)));
+}
+
+// _surface_color :1008-1058
+__device__ r3 surface_color(float h, const float (&m)[4], int slot, int mode, const int32_t* slot_level) {
+  const r3 fertile = R3(0.10f, 0.34f, 0.075f), arid = R3(0.44f, 0.31f, 0.13f), rock = R3(0.34f, 0.32f, 0.30f);
+  const r3 snow = R3(0.92f, 0.95f, 0.98f), sand = R3(0.72f, 0.60f, 0.34f);
+  const r3 deep_ocean = R3(0.012f, 0.055f, 0.16f), shallow_ocean = R3(0.015f, 0.34f, 0.46f);
+  r3 color = radd(radd(radd(rscale(fertile, m[0]), rscale(arid, m[1])), rscale(rock, m[2])), rscale(snow, m[3]));
+  if (h < 0.0f) {
+    color = mix3(shallow_ocean, deep_ocean, clamp01(dv(-h, 4200.0f)));
+  } else if (h < 140.0f) {
+    color = mix3(sand, color, clamp01(dv(h, 140.0f)));
+  }
+  if (mode == 1) {
+    color = height_band(h);
+  } else if (mode == 2) {
+    const float hue = dv(float(slot_level[slot] % 6), 6.0f);
+    const float h6 = mul(hue, 6.0f);
+    color = R3(clamp01(sub(fabsf(sub(h6, 3.0f)), 1.0f)), clamp01(sub(2.0f, fabsf(sub(h6, 2.0f)))),
+               clamp01(sub(2.0f, fabsf(sub(h6, 4.0f)))));
+  } else if (mode == 3) {
+    const float value = dv(float((int32_t(uint32_t(slot) * 1103515245u + 12345u)) & 255), 255.0f);
+    const float a = add(mul(value, 0.73f), 0.21f), b = add(mul(value, 0.37f), 0.61f);
+    color = R3(value, sub(a, floorf(a)), sub(b, floorf(b)));
+  }
+  return color;
+}
+
+// _resolve_raster :1208-1267
+__global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLayout L,
+                                                        const unsigned long long* __restrict__ depth_key,
+                                                        RasterOutDev O, int mode, int triangles_per_patch,
+                                                        const int32_t* __restrict__ slot_level) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)L.width * L.height) return;
+  int x, y;
+  if (L.sy <= L.sx) {  // y contiguous: the reference's (W, H, ...) layout
+    x = int(i / L.height);
+    y = int(i % L.height);
+  } else {
+    y = int(i / L.width);
+    x = int(i % L.width);
+  }
+  const long long e = (long long)x * L.sx + (long long)y * L.sy;
+  const unsigned long long key = depth_key[size_t(x) * L.height + y];
+  if (key == kSentinel) {
+    O.surface_id[e] = -1;
+    O.cell_id[e] = -1;
+    return;
+  }
+  const float z = __uint_as_float(uint32_t(key >> 32));
+  const RasterTri& T = S.tris[key & 0xffffffffull];
+  const r3 l = rscale(edge_values(T, add(float(x), 0.5f), add(float(y), 0.5f)), T.inv_area);
+  const float w0 = dv(mul(l.x, z), T.screen[0][2]), w1 = dv(mul(l.y, z), T.screen[1][2]),
+              w2 = dv(mul(l.z, z), T.screen[2][2]);
+  auto lerp3 = [&](const float (&a)[3][3]) {
+    return radd(radd(rscale(R3(a[0][0], a[0][1], a[0][2]), w0), rscale(R3(a[1][0], a[1][1], a[1][2]), w1)),
+                rscale(R3(a[2][0], a[2][1], a[2][2]), w2));
+  };
+  const r3 bp = lerp3(T.v);
+  const r3 bn = rnormalized(lerp3(T.n));
+  float bm[4];
+  for (int j = 0; j < 4; ++j) bm[j] = add(add(mul(T.m[0][j], w0), mul(T.m[1][j], w1)), mul(T.m[2][j], w2));
+  const float bh = add(add(mul(T.h[0], w0), mul(T.h[1], w1)), mul(T.h[2], w2));
+  int vi = 0;
+  float wv = w0;
+  if (w1 > w0) vi = 1, wv = w1;
+  if (w2 > wv) vi = 2;
+  const int32_t src = T.src;
+  const r3 albedo = surface_color(bh, bm, src / triangles_per_patch, mode, slot_level);
+  const int c = L.channels;
+  O.depth[e] = z;
+  O.surface_id[e] = src;
+  O.cell_id[e] = T.c[vi];
+  O.position[e * c + 0] = bp.x, O.position[e * c + 1] = bp.y, O.position[e * c + 2] = bp.z;
+  O.normal[e * c + 0] = bn.x, O.normal[e * c + 1] = bn.y, O.normal[e * c + 2] = bn.z;
+  O.albedo[e * c + 0] = albedo.x, O.albedo[e * c + 1] = albedo.y, O.albedo[e * c + 2] = albedo.z;
+  for (int j = 0; j < 4; ++j) O.material[e * 4 + j] = bm[j];
+  O.height[e] = bh;
+}
+
+__global__ void k_raster_clear(unsigned long long* __restrict__ depth_key, long long n, uint32_t* count) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i == 0) *count = 0u;
+  if (i < n) depth_key[i] = kSentinel;
+}
+
+}  // namespace
+
+cudaError_t launch_raster(const RasterMeshDev& M, const RasterStream& S, const ImageLayout& L,
+                          unsigned long long* depth_key, const RasterOutDev& O, float near, float tf, int mode,
+                          int sm_count, cudaStream_t s) {
+  const long long pixels = (long long)L.width * L.height;
+  k_raster_clear<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(depth_key, pixels, S.count);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const long long sources = (long long)M.n_active * M.triangles_per_patch;
+  if (sources > 0) {
+    k_raster_clip<<<unsigned((sources + 127) / 128), 128, 0, s>>>(M, S, near, tf, L.width, L.height);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  k_raster_depth<<<unsigned(sm_count * 8), 256, 0, s>>>(S, L, depth_key);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_raster_resolve<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(S, L, depth_key, O, mode, M.triangles_per_patch,
+                                                                  M.slot_level);
+  return cudaGetLastError();
+}
+
+}  // namespace atm

@@ -226,6 +226,20 @@ class AtmPostConfig(ctypes.Structure):
         ("bloom_passes", ctypes.c_int32),
     ]
 
+class AtmRasterMesh(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in ("view", "normal", "material", "height_m", "cell", "triangles",
+                                                     "active_slots", "skirt_mask", "slot_level")] + [
+        (name, ctypes.c_int32) for name in ("patches", "vertices_per_patch", "triangles_per_patch",
+                                            "surface_triangles_per_patch", "resolution", "n_active")]
+
+
+RASTER_OUTPUTS = ("depth", "position", "normal", "albedo", "material_weights", "height_m", "surface_id", "cell_id")
+
+
+class AtmRasterOutputs(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in RASTER_OUTPUTS]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _D = ctypes.c_double
@@ -295,6 +309,11 @@ SIGNATURES = {
         [_P, ctypes.POINTER(AtmShadeParams), ctypes.POINTER(AtmShadeImages), _P, _P, ctypes.POINTER(AtmImage), _D, _D,
          c_double3, c_double3, c_double3, _D, c_double9, _D, _D, _D, ctypes.POINTER(AtmSurrogate), _P],
     ),
+    "atm_raster_create": (ctypes.c_int, [_I32, _I32, _I32, _I32, ctypes.POINTER(_P)]),
+    "atm_raster_destroy": (ctypes.c_int, [_P]),
+    "atm_raster_terrain": (ctypes.c_int, [_P, ctypes.POINTER(AtmRasterMesh), _D, _D, _I32,
+                                          ctypes.POINTER(AtmRasterOutputs), ctypes.POINTER(AtmImage), _P]),
+    "atm_raster_emitted": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), _P]),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,

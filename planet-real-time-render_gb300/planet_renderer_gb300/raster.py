@@ -1,0 +1,178 @@
+"""The terrain raster that produces the atmosphere stage's G-buffer: the
+reference's ``PlanetRenderer`` triangle path (``src/planet_renderer/renderer.py
+:628-1269``) over ``atm_raster_terrain``.
+
+One frame is ``_clip`` (back-face culling of surface triangles, skirts drawn
+from both sides, trivial reject, Sutherland-Hodgman against the near plane
+and the four frustum sides, fan triangulation into the emitted stream),
+``_raster_depth_direct`` (each covered pixel centre takes the atomic 64-bit
+minimum of ``depth bits << 32 | triangle``) and ``_resolve_raster`` (the
+nearest triangle's perspective-correct view position, normal, material
+weights and height, the dominant vertex's cell id and the albedo of the
+debug view).  The reference's tiled pixel path (``_bin`` / ``_raster_pixel``)
+chooses the same nearest triangle per pixel; this class runs the
+triangle-driven path for every frame.
+
+Images are torch CUDA tensors ``(W, H, ...)`` - the layout of the reference's
+Taichi fields - or ``(H, W, ...)`` with ``layout="hw"``; work is enqueued on
+the current CUDA stream.
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _native
+
+MAX_CLIPPED_TRIANGLES = 6  # renderer.py:37
+# G-buffer images the raster writes, with (dtype, floats per element; 0 = one scalar)
+OUTPUTS = {"depth": (torch.float32, 0), "position": (torch.float32, -1), "normal": (torch.float32, -1),
+           "albedo": (torch.float32, -1), "material_weights": (torch.float32, 4), "height_m": (torch.float32, 0),
+           "surface_id": (torch.int32, 0), "cell_id": (torch.int32, 0)}
+
+
+def _element_strides(t: torch.Tensor, per_element: int, layout: str) -> tuple:
+    sx, sy = (t.stride(0), t.stride(1)) if layout == "wh" else (t.stride(1), t.stride(0))
+    if sx % per_element or sy % per_element:
+        raise ValueError("image strides must be whole elements")
+    return sx // per_element, sy // per_element
+
+
+class TerrainRaster:
+    """The raster buffers of one frame size (``renderer.py:200-236``): the
+    emitted-triangle stream of ``max_patches * triangles_per_patch * 6``
+    triangles and the per-pixel depth keys."""
+
+    def __init__(self, width: int, height: int, max_patches: int, triangles_per_patch: int,
+                 layout: str = "wh", device: str | torch.device = "cuda"):
+        if layout not in ("wh", "hw"):
+            raise ValueError("layout must be 'wh' (Taichi field layout) or 'hw'")
+        self.width, self.height = int(width), int(height)
+        self.max_patches, self.triangles_per_patch = int(max_patches), int(triangles_per_patch)
+        self.layout = layout
+        self.device = torch.device(device)
+        self._lib = _native.library()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            _native.check(self._lib.atm_raster_create(self.width, self.height, self.max_patches,
+                                                      self.triangles_per_patch, ctypes.byref(h)))
+        self._handle = h
+
+    @property
+    def capacity(self) -> int:
+        return self.max_patches * self.triangles_per_patch * MAX_CLIPPED_TRIANGLES
+
+    def allocate_gbuffer(self, channels: int = 3) -> dict:
+        """Empty G-buffer images of this raster's size and layout."""
+
+        dims = (self.width, self.height) if self.layout == "wh" else (self.height, self.width)
+        out = {}
+        for name, (dtype, per) in OUTPUTS.items():
+            per = channels if per < 0 else per
+            shape = dims + ((per,) if per else ())
+            out[name] = torch.zeros(shape, dtype=dtype, device=self.device)
+        out["surface_id"].fill_(-1)
+        out["cell_id"].fill_(-1)
+        return out
+
+    def _image(self, gbuffer: dict) -> _native.AtmImage:
+        missing = [n for n in OUTPUTS if n not in gbuffer]
+        if missing:
+            raise ValueError(f"missing G-buffer images: {missing}")
+        ref = gbuffer["position"]
+        if not isinstance(ref, torch.Tensor) or ref.dim() != 3 or ref.shape[2] not in (3, 4) or ref.stride(2) != 1:
+            raise ValueError("position must be a float32 CUDA tensor (W, H, 3|4) with contiguous channels")
+        channels = int(ref.shape[2])
+        dims = (int(ref.shape[0]), int(ref.shape[1])) if self.layout == "wh" else (int(ref.shape[1]),
+                                                                                  int(ref.shape[0]))
+        if dims != (self.width, self.height):
+            raise ValueError(f"G-buffer is {dims[0]}x{dims[1]}, the raster {self.width}x{self.height}")
+        strides = _element_strides(ref, channels, self.layout)
+        for name, (dtype, per) in OUTPUTS.items():
+            t = gbuffer[name]
+            per = channels if per < 0 else per
+            if not isinstance(t, torch.Tensor) or t.dtype != dtype or t.device != self.device:
+                raise ValueError(f"{name} must be a {dtype} tensor on {self.device}")
+            shape = tuple(t.shape[:2]) if self.layout == "wh" else (int(t.shape[1]), int(t.shape[0]))
+            if shape != dims or t.dim() != (3 if per else 2) or (per and (t.shape[2] != per or t.stride(2) != 1)):
+                raise ValueError(f"{name} must have the frame's shape with {per or 1} values per pixel")
+            if _element_strides(t, per or 1, self.layout) != strides:
+                raise ValueError(f"{name} must share the G-buffer's element strides")
+        return _native.AtmImage(self.width, self.height, strides[0], strides[1], channels)
+
+    def render(self, mesh: dict, near: float, tangent_half_fov: float, gbuffer: dict, view_mode: int = 0) -> None:
+        """One frame's _clip + _raster_depth_direct + _resolve_raster into
+        ``gbuffer`` (images named as ``OUTPUTS``).  ``mesh`` holds CUDA
+        tensors: ``view``, ``normal`` (patches, vertices, 3), ``material``
+        (patches, vertices, 4), ``height_m`` (patches, vertices) float32,
+        ``cell`` (patches, vertices), ``triangles`` (triangles, 3) and
+        ``active_slots`` int32, optional ``skirt_mask`` and ``slot_level``
+        (patches,) int32, and the ints ``surface_triangles`` and
+        ``resolution``.  ``view_mode``: 0 lit albedo, 1 height bands, 2 LOD
+        level, 3 patch hash."""
+
+        image = self._image(gbuffer)
+        view = mesh["view"]
+        patches, vertices = int(view.shape[0]), int(view.shape[1])
+        tri = mesh["triangles"]
+
+        def arr(name, dtype, shape, optional=False):
+            t = mesh.get(name)
+            if t is None:
+                if optional:
+                    return None
+                raise ValueError(f"mesh needs {name}")
+            if not isinstance(t, torch.Tensor) or t.dtype != dtype or t.device != self.device:
+                raise ValueError(f"mesh {name} must be a {dtype} tensor on {self.device}")
+            if tuple(t.shape) != shape or not t.is_contiguous():
+                raise ValueError(f"mesh {name} must be a contiguous {shape} tensor")
+            return t
+
+        f32, i32 = torch.float32, torch.int32
+        active = mesh["active_slots"]
+        n_active = int(active.numel())
+        tensors = {
+            "view": arr("view", f32, (patches, vertices, 3)),
+            "normal": arr("normal", f32, (patches, vertices, 3)),
+            "material": arr("material", f32, (patches, vertices, 4)),
+            "height_m": arr("height_m", f32, (patches, vertices)),
+            "cell": arr("cell", i32, (patches, vertices)),
+            "triangles": arr("triangles", i32, (int(tri.shape[0]), 3)),
+            "active_slots": arr("active_slots", i32, (n_active,)),
+            "skirt_mask": arr("skirt_mask", i32, (patches,), optional=True),
+            "slot_level": arr("slot_level", i32, (patches,), optional=True),
+        }
+        m = _native.AtmRasterMesh()
+        for name, t in tensors.items():
+            setattr(m, name, None if t is None else t.data_ptr())
+        m.patches, m.vertices_per_patch, m.triangles_per_patch = patches, vertices, int(tri.shape[0])
+        m.surface_triangles_per_patch = int(mesh.get("surface_triangles", tri.shape[0]))
+        m.resolution = int(mesh.get("resolution", 1))
+        m.n_active = n_active
+        outs = _native.AtmRasterOutputs(*[ctypes.c_void_p(gbuffer[n].data_ptr()) for n in _native.RASTER_OUTPUTS])
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        _native.check(self._lib.atm_raster_terrain(self._handle, ctypes.byref(m), float(near), float(tangent_half_fov),
+                                                   int(view_mode), ctypes.byref(outs), ctypes.byref(image),
+                                                   ctypes.c_void_p(stream)))
+
+    def emitted(self) -> int:
+        """Triangles the last frame emitted (``clipped_count``; synchronises
+        the current stream).  Above ``capacity`` means some were dropped."""
+
+        n = ctypes.c_int64()
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        _native.check(self._lib.atm_raster_emitted(self._handle, ctypes.byref(n), ctypes.c_void_p(stream)))
+        return int(n.value)
+
+    def close(self) -> None:
+        if self._handle:
+            self._lib.atm_raster_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
