@@ -420,6 +420,7 @@ def main() -> None:
     parser.add_argument("--mlp-epochs", type=int, default=400, help="surrogate training epochs (2^22 samples)")
     parser.add_argument("--no-post", action="store_true", help="skip the 4K display post-process timing")
     parser.add_argument("--no-luts", action="store_true", help="skip the plain LUT-build timing")
+    parser.add_argument("--no-raster", action="store_true", help="skip the 4K terrain raster timing")
     parser.add_argument("--mlp-sweep", type=int, default=64,
                         help="also run the aerial-surrogate frame workload over this many 4K frames with cameras "
                              "log-uniform 1 m - 4000 km (e.g. 64)")
@@ -497,6 +498,7 @@ def main() -> None:
     batch = None if args.no_batch else _batch(device, args)
     post = None if args.no_post else _postprocess_4k(device, args)
     shade = None if args.no_post else _shading_4k(device, args)
+    raster = None if args.no_raster else _raster_4k(device, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -522,6 +524,7 @@ def main() -> None:
             "batch": batch,
             "postprocess_4k": post,
             "shading_4k": shade,
+            "raster_4k": raster,
             "samples_per_step": samples_per_step,
             "e2e": {"value": world * e2e_samples / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / e2e_steps,
@@ -738,6 +741,58 @@ def _shading_4k(device, args, steps=20) -> dict:
     del gb, inputs, out
     torch.cuda.empty_cache()
     return res
+
+
+RASTER_TRI_BYTES = 228  # one emitted triangle record (atm::RasterTri)
+RASTER_VERTEX_BYTES = 48  # view 12, normal 12, material 16, height 4, cell 4
+RASTER_COVERED_BYTES = 68  # depth, position, normal, albedo (3 floats), material (4), height, ids
+RASTER_KEY_BYTES = 16  # the depth key's clear and its read by the resolve
+
+
+def _raster_4k(device, args, steps=20) -> dict:
+    """The terrain raster (clip, depth keys, resolve; the atmosphere stage's
+    G-buffer producer) at 3840x2160 over the synthetic ground-camera terrain:
+    the reference renderer's default patch budget (256 patches of 12 cells)
+    and a dense one (1024 patches of 32 cells), 2 km above ground looking 8
+    degrees down to 80 km.  Device time per frame with CUDA events."""
+
+    import torch
+
+    from planet_renderer_gb300.raster import TerrainRaster, synthetic_terrain
+
+    width, height, tf = 3840, 2160, math.tan(math.radians(30.0))
+    out = {}
+    for name, rows, cols, res in (("default_256x12", 16, 16, 12), ("dense_1024x32", 32, 32, 32)):
+        mesh = synthetic_terrain(width, height, tf, rows=rows, columns=cols, resolution=res, seed=SEED, device=device)
+        patches, tpp = rows * cols, int(mesh["triangles"].shape[0])
+        r = TerrainRaster(width, height, patches, tpp, device=device)
+        g = r.allocate_gbuffer(3)
+        run = lambda: r.render(mesh, 0.5, tf, g)
+        for _ in range(args.warmup):
+            run()
+        emitted = r.emitted()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(device)
+        start.record()
+        for _ in range(steps):
+            run()
+        end.record()
+        torch.cuda.synchronize(device)
+        ms = start.elapsed_time(end) / steps
+        covered = int((g["surface_id"] >= 0).sum())
+        pixels = width * height
+        algo = (patches * int(mesh["view"].shape[1]) * RASTER_VERTEX_BYTES + 2 * emitted * RASTER_TRI_BYTES
+                + pixels * RASTER_KEY_BYTES + covered * RASTER_COVERED_BYTES + (pixels - covered) * 8)
+        peaks = _peaks()
+        out[name] = {"ms": ms, "source_triangles": patches * tpp, "emitted": emitted, "covered_px": covered,
+                     "algorithmic_bytes": algo, "achieved_gbs": algo / (ms / 1e3) / 1e9,
+                     "frac": algo / (ms / 1e3) / 1e9 / peaks["hbm_gbs"]}
+        r.close()
+        del mesh, g
+        torch.cuda.empty_cache()
+    out["workload"] = ("3840x2160 terrain raster (clip + depth keys + resolve) of a 2 km ground camera's synthetic "
+                       "terrain, 60 degree vertical field of view, near 0.5 m")
+    return out
 
 
 def _batch(device, args) -> dict:
@@ -1311,7 +1366,15 @@ def _profile_shade(args):
     print("profile case shade4k:", round(out["ms"], 3), "ms")
 
 
+def _profile_raster(args):
+    """The terrain raster at 4K, both patch budgets, three frames each."""
+
+    out = _raster_4k(__import__("torch").device("cuda:0"), argparse.Namespace(warmup=3), steps=3)
+    print("profile case raster4k:", {k: round(v["ms"], 3) for k, v in out.items() if isinstance(v, dict)})
+
+
 PROFILE_CASES = {
+    "raster4k": _profile_raster,
     "frame1080p": _profile_frame_1080p,
     "frame4k_mlp": _profile_frame_4k_mlp,
     "luts": _profile_luts,

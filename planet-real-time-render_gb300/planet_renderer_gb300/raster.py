@@ -21,7 +21,9 @@ the current CUDA stream.
 from __future__ import annotations
 
 import ctypes
+import math
 
+import numpy as np
 import torch
 
 from . import _native
@@ -31,6 +33,106 @@ MAX_CLIPPED_TRIANGLES = 6  # renderer.py:37
 OUTPUTS = {"depth": (torch.float32, 0), "position": (torch.float32, -1), "normal": (torch.float32, -1),
            "albedo": (torch.float32, -1), "material_weights": (torch.float32, 4), "height_m": (torch.float32, 0),
            "surface_id": (torch.int32, 0), "cell_id": (torch.int32, 0)}
+
+
+def shared_topology(resolution: int) -> np.ndarray:
+    """The patch topology the raster draws (``_shared_topology``,
+    renderer.py:78-100): two triangles per grid cell of the (resolution + 1)^2
+    surface vertices, then per edge (bottom, right, top, left, walked so the
+    skirt faces outwards) two triangles per segment joining the edge's surface
+    vertices to that edge's row of skirt vertices, which follow the surface
+    vertices in the patch's vertex stream."""
+
+    n = int(resolution)
+    side = n + 1
+    cells = np.arange(n)
+    a = (cells[:, None] * side + cells[None, :]).ravel()  # row-major cells: a = y * side + x
+    surface = np.stack([np.stack([a, a + 1, a + side], 1), np.stack([a + 1, a + side + 1, a + side], 1)],
+                       1).reshape(-1, 3)
+    i = np.arange(side)
+    edges = (i, i * side + n, (n * side + i)[::-1], (i * side)[::-1])
+    skirts = []
+    for k, edge in enumerate(edges):
+        base = side * side + k * side
+        s0, s1 = edge[:-1], edge[1:]
+        c0, c1 = base + cells, base + cells + 1
+        skirts.append(np.stack([np.stack([s0, c0, s1], 1), np.stack([s1, c0, c1], 1)], 1).reshape(-1, 3))
+    return np.concatenate([surface] + skirts).astype(np.int32)
+
+
+def synthetic_terrain(width: int, height: int, tangent_half_fov: float, altitude_m: float = 2000.0,
+                      pitch_degrees: float = 8.0, rows: int = 16, columns: int = 16, resolution: int = 12,
+                      far_m: float = 80_000.0, planet_radius_m: float = 6_371_000.0, seed: int = 0,
+                      device: str | torch.device = "cuda") -> dict:
+    """A seeded terrain frame in camera view space for ``render``: rows x
+    columns patches of ``resolution`` cells a side tiling the ground in the
+    view frustum from the camera's foot to ``far_m`` (rows growing
+    geometrically with distance, as a distance-based LOD does), heights from
+    a few octaves of sinusoids over the planet's curvature drop, outward
+    skirts below every edge, material weights by height and slope.  Stands in
+    for the terrain backend's patch stream (the LOD system is not part of
+    this library)."""
+
+    rng = np.random.default_rng(seed)
+    n, side = int(resolution), int(resolution) + 1
+    near_z = max(altitude_m / math.tan(math.radians(pitch_degrees) + math.atan(tangent_half_fov)), 1.0)
+    growth = (far_m / near_z) ** (1.0 / rows)
+    tx = tangent_half_fov * width / height
+    t = np.linspace(0.0, 1.0, side)
+    phases = rng.uniform(0.0, 2.0 * math.pi, (6, 2))
+    waves = [(1.0 / (900.0 * 2.2 ** -k), 380.0 * 0.5 ** k) for k in range(6)]
+
+    def ground(x, z):
+        h = np.zeros_like(x)
+        dhx, dhz = np.zeros_like(x), np.zeros_like(x)
+        for k, (f, amp) in enumerate(waves):
+            u, v = f * x + phases[k, 0], f * z * 0.83 + phases[k, 1]
+            h += amp * np.sin(u) * np.cos(v)
+            dhx += amp * f * np.cos(u) * np.cos(v)
+            dhz -= amp * f * 0.83 * np.sin(u) * np.sin(v)
+        return h + 150.0, dhx, dhz
+
+    view, normal, material, hgt, cell = [], [], [], [], []
+    pitch = math.radians(pitch_degrees)
+    up = np.array([0.0, math.cos(pitch), math.sin(pitch)])
+    fwd = np.array([0.0, -math.sin(pitch), math.cos(pitch)])
+    for r in range(rows):
+        z0, z1 = near_z * growth ** r * (0.0 if r == 0 else 1.0), near_z * growth ** (r + 1)
+        half = 1.15 * tx * z1 + 200.0
+        for c in range(columns):
+            x0, x1 = -half + 2.0 * half * c / columns, -half + 2.0 * half * (c + 1) / columns
+            X, Z = np.meshgrid(x0 + (x1 - x0) * t, z0 + (z1 - z0) * t)
+            h, dhx, dhz = ground(X, Z)
+            drop = (X * X + Z * Z) / (2.0 * planet_radius_m)
+            Y = h - altitude_m - drop
+            nrm = np.stack([-dhx, np.ones_like(X), -dhz], -1)
+            nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+            pts = np.stack([X, Y, Z], -1).reshape(-1, 3)
+            nr = nrm.reshape(-1, 3)
+            hh = h.reshape(-1)
+            skirt_depth = 0.02 * (z1 - z0) + 5.0
+            ring = np.concatenate([np.arange(side), np.arange(side) * side + n, n * side + np.arange(side),
+                                   np.arange(side) * side])
+            pts = np.concatenate([pts, pts[ring] - [0.0, skirt_depth, 0.0]])
+            nr = np.concatenate([nr, nr[ring]])
+            hh = np.concatenate([hh, hh[ring] - skirt_depth])
+            slope = 1.0 - nr[:, 1]
+            snow = np.clip((hh - 450.0) / 150.0, 0.0, 1.0)
+            rock = np.clip(slope * 6.0, 0.0, 1.0) * (1.0 - snow)
+            arid = np.clip(hh / 600.0, 0.0, 1.0) * (1.0 - rock - snow)
+            fertile = np.clip(1.0 - arid - rock - snow, 0.0, 1.0)
+            view.append(np.stack([pts[:, 0], pts @ up, pts @ fwd], -1))
+            normal.append(np.stack([nr[:, 0], nr @ up, nr @ fwd], -1))
+            material.append(np.stack([fertile, arid, rock, snow], -1))
+            hgt.append(hh)
+            cell.append((r * columns + c) * 4096 + np.arange(len(hh)))
+    patches = rows * columns
+    f32 = lambda a: torch.as_tensor(np.asarray(a, np.float32), device=device)
+    i32 = lambda a: torch.as_tensor(np.asarray(a, np.int32), device=device)
+    return {"view": f32(view), "normal": f32(normal), "material": f32(material), "height_m": f32(hgt),
+            "cell": i32(cell), "triangles": i32(shared_topology(n)), "active_slots": i32(np.arange(patches)),
+            "skirt_mask": i32(np.full(patches, 15)), "slot_level": i32(rows - 1 - np.arange(patches) // columns),
+            "surface_triangles": 2 * n * n, "resolution": n}
 
 
 def _element_strides(t: torch.Tensor, per_element: int, layout: str) -> tuple:

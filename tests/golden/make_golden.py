@@ -436,6 +436,9 @@ RASTER_CASES = [
 ]
 
 
+RASTER_TOPOLOGIES = (2, 5, 12, 32)
+
+
 def raster_mesh(w, h, patches, resolution, seed):
     """Seeded terrain patches in view space (x right, y up, z forward): a
     heightfield grid of (resolution + 1)^2 vertices per patch in front of
@@ -488,9 +491,12 @@ def raster_reference(reference: Path) -> dict:
 
     shim.install()
     sys.path.insert(0, str(reference / "src"))
-    from planet_renderer.renderer import DEPTH_KEY_SENTINEL, MAX_CLIPPED_TRIANGLES, PlanetRenderer  # type: ignore
+    from planet_renderer.renderer import (DEPTH_KEY_SENTINEL, MAX_CLIPPED_TRIANGLES,  # type: ignore
+                                          PlanetRenderer, _shared_topology)
 
     out = {}
+    for n in RASTER_TOPOLOGIES:  # the patch topology the terrain backend's patches are drawn with
+        out[f"topology{n}"] = np.asarray(_shared_topology(n), np.int32)
     for k, (w, h, patches, resolution, active, mode, tf, near, seed, skirts) in enumerate(RASTER_CASES):
         view, normal, material, height, cell, triangles = raster_mesh(w, h, patches, resolution, seed)
         n_vert = view.shape[1]
