@@ -632,6 +632,67 @@ int atm_raster_terrain(AtmRaster* raster, const AtmRasterMesh* mesh, double near
  * the reference drops them. */
 int atm_raster_emitted(const AtmRaster* raster, int64_t* count, void* stream);
 
+/* ---- ocean coverage: the sea-level part of the G-buffer -----------------------
+ * OceanRenderer (src/planet_renderer/ocean.py:193-771): per frame the
+ * directional wave spectrum (_build_directional_spectrum :260-337, three
+ * periodic cascades) and the coverage pass (_rasterize :517-684): each view
+ * ray against the sea-level sphere, near-field wave geometry by fixed-point
+ * sphere solves, and where the sea is nearer than the terrain the water
+ * surface's G-buffer values (view position, footprint-filtered wave normal,
+ * slope variance, seabed colour / normal / water depth from the terrain pixel
+ * it covers, surface_id = OCEAN_SURFACE_ID, cell_id = -1). */
+typedef struct AtmOceanConfig { /* OceanConfig's fields the pass reads (ocean.py:38-110) */
+  int32_t surface_enabled;      /* 0: the pass writes nothing */
+  int32_t enabled;              /* advanced waves; 0: flat sea level, no spectrum */
+  double albedo[3];
+  double normal_strength;       /* 0..1 */
+  double max_visible_depth_m;   /* > 0 */
+  int32_t spectrum_resolution;  /* 32, 64, 128 or 256 */
+  int32_t geometry_cascades;    /* 0..3 */
+  double wind_speed_mps;        /* 0.1..40 */
+  double wind_direction_degrees;
+  double wave_height_scale;     /* 0..4 */
+  double choppiness;            /* 0..1 */
+  double geometry_max_distance_m; /* >= 0 */
+} AtmOceanConfig;
+/* Device G-buffer images sharing `image`'s shape and element strides:
+ * position (view space), normal, albedo, seabed_albedo and seabed_normal
+ * with image->channels floats per element, material_weights 4 floats, the
+ * rest one value.  Read where the terrain was drawn (surface_id >= 0), and
+ * overwritten at the pixels the sea covers. */
+typedef struct AtmOceanImages {
+  float* depth;
+  float* position;
+  float* normal;
+  float* albedo;
+  float* material_weights;
+  float* height_m;
+  float* water_depth_m;
+  float* seabed_albedo;
+  float* seabed_normal;
+  float* slope_variance;
+  int32_t* surface_id;
+  int32_t* cell_id;
+} AtmOceanImages;
+typedef struct AtmOcean AtmOcean;
+/* OceanRenderer.__init__ (:197-230): validates the configuration and
+ * allocates the spectrum (3 cascades x resolution^2 texels). */
+int atm_ocean_create(const AtmOceanConfig* config, AtmOcean** out);
+int atm_ocean_destroy(AtmOcean* ocean);
+/* OceanRenderer.rasterize (:686-762) after PlanetRenderer's terrain raster
+ * (renderer.py:1643-1663): planet_frame = (east, up, north) of the camera's
+ * local frame in planet coordinates, view_basis = (right, up, forward) in the
+ * local frame, 9 doubles each.  Stream-ordered; allocates nothing. */
+int atm_ocean_rasterize(AtmOcean* ocean, const AtmOceanImages* images, const AtmImage* image, double planet_radius_m,
+                        double camera_altitude_m, const double planet_frame[9], const double view_basis[9],
+                        double tangent_half_fov, double time_seconds, int32_t debug_mode, void* stream);
+/* The last frame's spectrum copied to host memory (tests; synchronises):
+ * each array is [3][resolution][resolution] (cascade, x, y) of 1, 2, 2 and
+ * 4 floats: height, gradient, displacement, displacement Jacobian.  Any
+ * pointer may be null. */
+int atm_ocean_read_spectrum(AtmOcean* ocean, float* height, float* gradient, float* displacement, float* jacobian,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

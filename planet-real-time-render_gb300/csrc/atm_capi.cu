@@ -1532,3 +1532,205 @@ ATM_API int atm_raster_emitted(const AtmRaster* r, int64_t* count, void* stream)
   *count = int64_t(v);
   return ATM_OK;
 }
+
+// ---- ocean coverage ----------------------------------------------------------
+struct AtmOcean {
+  AtmOceanConfig config{};
+  atm::OceanSpectrum spectrum{};
+  double variances[atm::kOceanCascades] = {};
+};
+
+namespace {
+
+// The spectrum's table (ocean.py:18-25) for the host-side (float64) set-up.
+constexpr double kOceanPeriods[atm::kOceanCascades] = {2048.0, 256.0, 32.0};
+constexpr double kOceanHeights[atm::kOceanCascades] = {0.62, 0.14, 0.025};
+constexpr int kOceanModeX[12] = {3, 4, 4, 5, 5, 3, 2, 1, -1, -2, -3, -4};
+constexpr int kOceanModeY[12] = {1, 1, 2, 1, 2, 2, 3, 4, 4, 3, 2, 1};
+constexpr double kOceanWeights[12] = {1.0, 0.82, 0.72, 0.60, 0.52, 0.68, 0.55, 0.42, 0.36, 0.31, 0.27, 0.22};
+
+double wind_amplitude_scale(const AtmOceanConfig& c) {  // _wind_amplitude_scale :232-233
+  return std::min(std::max(c.wind_speed_mps / 8.0, 0.25), 2.0);
+}
+
+// Python's float modulo by a positive divisor: the result takes the
+// divisor's sign (x % 1.0 lies in [0, 1)).
+double py_mod1(double x) {
+  double m = std::fmod(x, 1.0);
+  if (m != 0.0) {
+    if (m < 0.0) m += 1.0;
+  } else {
+    m = 0.0;
+  }
+  return m;
+}
+
+}  // namespace
+
+ATM_API int atm_ocean_create(const AtmOceanConfig* config, AtmOcean** out) {
+  if (!config || !out) return fail(ATM_E_INVALID, "null argument to atm_ocean_create");
+  *out = nullptr;
+  const AtmOceanConfig& c = *config;
+  for (double a : c.albedo)
+    if (!(a >= 0.0 && a <= 1.0)) return fail(ATM_E_INVALID, "ocean.albedo components must be in 0..1");
+  if (!(c.normal_strength >= 0.0 && c.normal_strength <= 1.0))
+    return fail(ATM_E_INVALID, "ocean.normal_strength must be in 0..1");
+  if (!(c.max_visible_depth_m > 0.0) || !std::isfinite(c.max_visible_depth_m))
+    return fail(ATM_E_INVALID, "ocean.max_visible_depth_m must be positive");
+  if (c.spectrum_resolution != 32 && c.spectrum_resolution != 64 && c.spectrum_resolution != 128 &&
+      c.spectrum_resolution != 256)
+    return fail(ATM_E_INVALID, "ocean.spectrum_resolution must be 32, 64, 128 or 256");
+  if (!(c.wind_speed_mps >= 0.1 && c.wind_speed_mps <= 40.0))
+    return fail(ATM_E_INVALID, "ocean.wind_speed_mps must be in 0.1..40");
+  if (!std::isfinite(c.wind_direction_degrees)) return fail(ATM_E_INVALID, "ocean.wind_direction_degrees must be finite");
+  if (!(c.wave_height_scale >= 0.0 && c.wave_height_scale <= 4.0))
+    return fail(ATM_E_INVALID, "ocean.wave_height_scale must be in 0..4");
+  if (!(c.choppiness >= 0.0 && c.choppiness <= 1.0)) return fail(ATM_E_INVALID, "ocean.choppiness must be in 0..1");
+  if (c.geometry_cascades < 0 || c.geometry_cascades > atm::kOceanCascades)
+    return fail(ATM_E_INVALID, "ocean.geometry_cascades must be in 0..3");
+  if (!(c.geometry_max_distance_m >= 0.0) || !std::isfinite(c.geometry_max_distance_m))
+    return fail(ATM_E_INVALID, "ocean.geometry_max_distance_m must be non-negative");
+  AtmOcean* o = new (std::nothrow) AtmOcean;
+  if (!o) return fail(ATM_E_NOMEM, "host allocation failed");
+  o->config = c;
+  const int n = c.spectrum_resolution;
+  const size_t texels = size_t(atm::kOceanCascades) * n * n;
+  o->spectrum.n = n;
+  cudaError_t e = cudaMalloc(&o->spectrum.height_gradient, texels * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&o->spectrum.displacement, texels * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&o->spectrum.jacobian, texels * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMemset(o->spectrum.height_gradient, 0, texels * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMemset(o->spectrum.displacement, 0, texels * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMemset(o->spectrum.jacobian, 0, texels * sizeof(float4));
+  if (e != cudaSuccess) {
+    atm_ocean_destroy(o);
+    return e == cudaErrorMemoryAllocation ? fail(ATM_E_NOMEM, "ocean spectrum allocation failed")
+                                          : cuda_fail(e, "ocean spectrum");
+  }
+  // per-cascade slope variance of the spectrum (_compute_slope_variance :235-258)
+  double weight_sum = 0.0;
+  for (double w : kOceanWeights) weight_sum += w;
+  const double amplitude_scale = c.wave_height_scale * wind_amplitude_scale(c);
+  for (int k = 0; k < atm::kOceanCascades; ++k) {
+    double variance = 0.0;
+    for (int m = 0; m < 12; ++m) {
+      const double amplitude = kOceanHeights[k] * amplitude_scale * kOceanWeights[m] / weight_sum;
+      const double wave_number = 2.0 * M_PI * std::hypot(double(kOceanModeX[m]), double(kOceanModeY[m])) /
+                                 kOceanPeriods[k];
+      const double slope = amplitude * wave_number;
+      variance += 0.5 * (slope * slope);
+    }
+    o->variances[k] = variance;
+  }
+  *out = o;
+  return ATM_OK;
+}
+
+ATM_API int atm_ocean_destroy(AtmOcean* o) {
+  if (!o) return ATM_OK;
+  if (o->spectrum.height_gradient) cudaFree(o->spectrum.height_gradient);
+  if (o->spectrum.displacement) cudaFree(o->spectrum.displacement);
+  if (o->spectrum.jacobian) cudaFree(o->spectrum.jacobian);
+  delete o;
+  return ATM_OK;
+}
+
+ATM_API int atm_ocean_rasterize(AtmOcean* o, const AtmOceanImages* im, const AtmImage* image, double planet_radius_m,
+                                double camera_altitude_m, const double planet_frame[9], const double view_basis[9],
+                                double tangent_half_fov, double time_seconds, int32_t debug_mode, void* stream) {
+  if (!o || !im || !image || !planet_frame || !view_basis) return fail(ATM_E_INVALID, "null argument to atm_ocean_rasterize");
+  if (image->width < 1 || image->height < 1 || (image->channels != 3 && image->channels != 4) ||
+      image->stride_x <= 0 || image->stride_y <= 0)
+    return fail(ATM_E_INVALID, "invalid AtmImage");
+  if (!im->depth || !im->position || !im->normal || !im->albedo || !im->material_weights || !im->height_m ||
+      !im->water_depth_m || !im->seabed_albedo || !im->seabed_normal || !im->slope_variance || !im->surface_id ||
+      !im->cell_id)
+    return fail(ATM_E_INVALID, "null G-buffer image");
+  if (!(planet_radius_m > 0.0) || !std::isfinite(planet_radius_m) || !std::isfinite(camera_altitude_m) ||
+      !(tangent_half_fov > 0.0) || !std::isfinite(tangent_half_fov) || !std::isfinite(time_seconds))
+    return fail(ATM_E_INVALID, "planet radius, field of view and time must be finite (radius, fov positive)");
+  for (int k = 0; k < 9; ++k)
+    if (!std::isfinite(planet_frame[k]) || !std::isfinite(view_basis[k]))
+      return fail(ATM_E_INVALID, "planet frame and view basis must be finite");
+  const AtmOceanConfig& c = o->config;
+  if (!c.surface_enabled) return ATM_OK;  // rasterize :709-710
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (c.enabled)
+    ATM_CUDA(atm::launch_ocean_spectrum(o->spectrum, float(time_seconds), float(c.wave_height_scale *
+                                                                                 wind_amplitude_scale(c)),
+                                        float(c.choppiness), s),
+             "ocean spectrum");
+  const double wind = c.wind_direction_degrees * (M_PI / 180.0);  // math.radians
+  atm::OceanFrame F{};
+  F.radius = float(planet_radius_m);
+  F.altitude = float(std::max(camera_altitude_m, 0.0));
+  F.tf = float(tangent_half_fov);
+  F.wind = float(wind);
+  double max_displacement = 0.0;
+  for (int k = 0; k < c.geometry_cascades; ++k) max_displacement += kOceanHeights[k];
+  max_displacement = max_displacement * c.wave_height_scale * wind_amplitude_scale(c);
+  F.max_displacement = float(c.enabled ? max_displacement : 0.0);
+  F.geometry_max_distance = float(c.enabled ? c.geometry_max_distance_m : 0.0);
+  F.normal_strength = float(c.normal_strength);
+  F.max_visible_depth = float(c.max_visible_depth_m);
+  for (int k = 0; k < 3; ++k) {
+    F.east[k] = float(planet_frame[k]);
+    F.up[k] = float(planet_frame[3 + k]);
+    F.north[k] = float(planet_frame[6 + k]);
+    F.right[k] = float(view_basis[k]);
+    F.vup[k] = float(view_basis[3 + k]);
+    F.fwd[k] = float(view_basis[6 + k]);
+    F.albedo[k] = float(c.albedo[k]);
+  }
+  // texture offsets of the sea anchor below the camera (rasterize :709-726), float64
+  const double cw = std::cos(wind), sw = std::sin(wind);
+  static const double base[3][2][3] = {{{1, 0, 0}, {0, 0, 1}}, {{0, 1, 0}, {1, 0, 0}}, {{0, 0, 1}, {0, 1, 0}}};
+  for (int k = 0; k < atm::kOceanCascades; ++k) {
+    double au[3], av[3], du = 0.0, dvv = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      au[j] = base[k][0][j] * cw + base[k][1][j] * sw;
+      av[j] = -base[k][0][j] * sw + base[k][1][j] * cw;
+    }
+    for (int j = 0; j < 3; ++j) {
+      const double anchor = planet_frame[3 + j] * planet_radius_m;
+      du += anchor * au[j];
+      dvv += anchor * av[j];
+    }
+    F.offsets[k][0] = float(py_mod1(du / kOceanPeriods[k]));
+    F.offsets[k][1] = float(py_mod1(dvv / kOceanPeriods[k]));
+    F.variances[k] = float(o->variances[k]);
+  }
+  F.geometry_cascades = c.geometry_cascades;
+  F.enabled = c.enabled ? 1 : 0;
+  F.debug_mode = debug_mode;
+  atm::OceanImages G{im->depth,      im->position,      im->normal,        im->albedo,
+                     im->material_weights, im->height_m, im->water_depth_m, im->seabed_albedo,
+                     im->seabed_normal, im->slope_variance, im->surface_id, im->cell_id};
+  ATM_CUDA(atm::launch_ocean_coverage(o->spectrum, F, layout_of(image), G, s), "ocean coverage");
+  return ATM_OK;
+}
+
+ATM_API int atm_ocean_read_spectrum(AtmOcean* o, float* height, float* gradient, float* displacement, float* jacobian,
+                                    void* stream) {
+  if (!o) return fail(ATM_E_INVALID, "null ocean");
+  const int n = o->spectrum.n;
+  const size_t texels = size_t(atm::kOceanCascades) * n * n;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::vector<float4> hg(texels), jac(texels);
+  std::vector<float2> disp(texels);
+  ATM_CUDA(cudaMemcpyAsync(hg.data(), o->spectrum.height_gradient, texels * sizeof(float4), cudaMemcpyDeviceToHost, s),
+           "spectrum read");
+  ATM_CUDA(cudaMemcpyAsync(disp.data(), o->spectrum.displacement, texels * sizeof(float2), cudaMemcpyDeviceToHost, s),
+           "spectrum read");
+  ATM_CUDA(cudaMemcpyAsync(jac.data(), o->spectrum.jacobian, texels * sizeof(float4), cudaMemcpyDeviceToHost, s),
+           "spectrum read");
+  ATM_CUDA(cudaStreamSynchronize(s), "spectrum read");
+  for (size_t t = 0; t < texels; ++t) {
+    if (height) height[t] = hg[t].x;
+    if (gradient) gradient[2 * t] = hg[t].y, gradient[2 * t + 1] = hg[t].z;
+    if (displacement) displacement[2 * t] = disp[t].x, displacement[2 * t + 1] = disp[t].y;
+    if (jacobian)
+      for (int k = 0; k < 4; ++k) jacobian[4 * t + k] = (&jac[t].x)[k];
+  }
+  return ATM_OK;
+}

@@ -279,6 +279,48 @@ cudaError_t launch_raster(const RasterMeshDev& M, const RasterStream& S, const I
                           unsigned long long* depth_key, const RasterOutDev& O, float near, float tf, int mode,
                           int sm_count, cudaStream_t s);
 
+// ---- ocean coverage (the sea-level part of the G-buffer) --------------------
+constexpr int kOceanCascades = 3;
+constexpr int32_t kOceanSurfaceId = 2147000000;  // OCEAN_SURFACE_ID
+// The per-frame wave spectrum: kOceanCascades x n x n texels indexed
+// [cascade][x][y] (x along the cascade's u axis): (height, dh/du, dh/dv, 0),
+// the horizontal displacement and its 2x2 Jacobian (row-major).
+struct OceanSpectrum {
+  float4* height_gradient;
+  float2* displacement;
+  float4* jacobian;
+  int n;
+};
+// One frame's scalars, rounded to float32 as the reference's kernel arguments.
+struct OceanFrame {
+  float radius, altitude, tf, wind, max_displacement, geometry_max_distance, normal_strength, max_visible_depth;
+  float east[3], up[3], north[3], right[3], vup[3], fwd[3], albedo[3];
+  float offsets[kOceanCascades][2];
+  float variances[kOceanCascades];
+  int geometry_cascades, enabled, debug_mode;
+};
+// The G-buffer images it reads and overwrites, at the layout's element
+// strides: position, normal, albedo, seabed albedo and normal with
+// L.channels floats, material 4 floats, the rest one value.
+struct OceanImages {
+  float* depth;
+  float* position;
+  float* normal;
+  float* albedo;
+  float* material;
+  float* height;
+  float* water_depth;
+  float* seabed_albedo;
+  float* seabed_normal;
+  float* slope_variance;
+  int32_t* surface_id;
+  int32_t* cell_id;
+};
+cudaError_t launch_ocean_spectrum(const OceanSpectrum& S, float time_s, float amplitude_scale, float choppiness,
+                                  cudaStream_t s);
+cudaError_t launch_ocean_coverage(const OceanSpectrum& S, const OceanFrame& F, const ImageLayout& L,
+                                  const OceanImages& G, cudaStream_t s);
+
 // Whether x is the image's contiguous axis (the orientation of its bloom planes).
 bool image_x_fast(const ImageLayout& L);
 // A bloom plane of orientation Q.x_fast copied into dst as float4 [y][x].

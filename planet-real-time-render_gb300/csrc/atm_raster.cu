@@ -26,38 +26,19 @@
 
 #include <cstdint>
 
+#include "atm_f32.cuh"
 #include "atm_kernels.h"
 
 namespace atm {
 
 namespace {
 
+using namespace f32;
+
 constexpr int kClipVerts = 8;      // MAX_CLIP_VERTICES
 constexpr int kClipTris = 6;       // MAX_CLIPPED_TRIANGLES
 constexpr unsigned long long kSentinel = ~0ull;
 
-struct r3 {
-  float x, y, z;
-};
-__device__ __forceinline__ float mul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float add(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float sub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float dv(float a, float b) { return __fdiv_rn(a, b); }
-__device__ __forceinline__ float fmx(float a, float b) { return a > b ? a : b; }
-__device__ __forceinline__ float fmn(float a, float b) { return a < b ? a : b; }
-__device__ __forceinline__ r3 R3(float x, float y, float z) { return {x, y, z}; }
-__device__ __forceinline__ r3 radd(r3 a, r3 b) { return {add(a.x, b.x), add(a.y, b.y), add(a.z, b.z)}; }
-__device__ __forceinline__ r3 rsub(r3 a, r3 b) { return {sub(a.x, b.x), sub(a.y, b.y), sub(a.z, b.z)}; }
-__device__ __forceinline__ r3 rscale(r3 a, float s) { return {mul(a.x, s), mul(a.y, s), mul(a.z, s)}; }
-__device__ __forceinline__ float rdot(r3 a, r3 b) { return add(add(mul(a.x, b.x), mul(a.y, b.y)), mul(a.z, b.z)); }
-__device__ __forceinline__ r3 rcross(r3 a, r3 b) {
-  return {sub(mul(a.y, b.z), mul(a.z, b.y)), sub(mul(a.z, b.x), mul(a.x, b.z)), sub(mul(a.x, b.y), mul(a.y, b.x))};
-}
-// Taichi's normalized(): (1 / (|v| + 0)) * v
-__device__ __forceinline__ r3 rnormalized(r3 v) {
-  const float inv = dv(1.0f, add(__fsqrt_rn(rdot(v, v)), 0.0f));
-  return {mul(inv, v.x), mul(inv, v.y), mul(inv, v.z)};
-}
 struct r4 {
   float v[4];
 };

@@ -240,6 +240,31 @@ class AtmRasterOutputs(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in RASTER_OUTPUTS]
 
 
+class AtmOceanConfig(ctypes.Structure):
+    _fields_ = [
+        ("surface_enabled", ctypes.c_int32),
+        ("enabled", ctypes.c_int32),
+        ("albedo", ctypes.c_double * 3),
+        ("normal_strength", ctypes.c_double),
+        ("max_visible_depth_m", ctypes.c_double),
+        ("spectrum_resolution", ctypes.c_int32),
+        ("geometry_cascades", ctypes.c_int32),
+        ("wind_speed_mps", ctypes.c_double),
+        ("wind_direction_degrees", ctypes.c_double),
+        ("wave_height_scale", ctypes.c_double),
+        ("choppiness", ctypes.c_double),
+        ("geometry_max_distance_m", ctypes.c_double),
+    ]
+
+
+OCEAN_IMAGES = ("depth", "position", "normal", "albedo", "material_weights", "height_m", "water_depth",
+                "seabed_albedo", "seabed_normal", "slope_variance", "surface_id", "cell_id")
+
+
+class AtmOceanImages(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in OCEAN_IMAGES]
+
+
 _P = ctypes.c_void_p
 _I32 = ctypes.c_int32
 _D = ctypes.c_double
@@ -314,6 +339,11 @@ SIGNATURES = {
     "atm_raster_terrain": (ctypes.c_int, [_P, ctypes.POINTER(AtmRasterMesh), _D, _D, _I32,
                                           ctypes.POINTER(AtmRasterOutputs), ctypes.POINTER(AtmImage), _P]),
     "atm_raster_emitted": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64), _P]),
+    "atm_ocean_create": (ctypes.c_int, [ctypes.POINTER(AtmOceanConfig), ctypes.POINTER(_P)]),
+    "atm_ocean_destroy": (ctypes.c_int, [_P]),
+    "atm_ocean_rasterize": (ctypes.c_int, [_P, ctypes.POINTER(AtmOceanImages), ctypes.POINTER(AtmImage), _D, _D,
+                                           c_double9, c_double9, _D, _D, _I32, _P]),
+    "atm_ocean_read_spectrum": (ctypes.c_int, [_P, _P, _P, _P, _P, _P]),
     "atm_composite_noalloc": (
         ctypes.c_int,
         [ctypes.POINTER(AtmParams), _P, _P, _P, _P, _P, _P, _P, _P, ctypes.POINTER(AtmImage), _D, _D, _D, c_double3,

@@ -436,6 +436,95 @@ RASTER_CASES = [
 ]
 
 
+# (width, height, seed, camera altitude m, pitch deg, yaw deg, time s, debug mode, OceanConfig overrides)
+OCEAN_CASES = [
+    (40, 24, 21, 30.0, -4.0, 20.0, 3.7, 0, dict(spectrum_resolution=32)),  # waves displace the near field
+    (36, 20, 22, 5000.0, -2.0, -50.0, 11.0, 1, dict(spectrum_resolution=32)),  # reseeded grazing rays
+    (32, 18, 23, 120.0, -8.0, 140.0, 0.0, 3, dict(enabled=False, spectrum_resolution=32)),  # flat sea level
+    (30, 18, 24, 0.5, -1.0, 75.0, 42.5, 2, dict(spectrum_resolution=64, wind_direction_degrees=-120.0,
+                                               choppiness=1.0, geometry_cascades=3, wind_speed_mps=14.0,
+                                               wave_height_scale=1.6, normal_strength=0.8)),
+]
+
+
+def ocean_reference(reference: Path) -> dict:
+    """The reference's ocean coverage pass (OceanRenderer.rasterize with
+    _build_directional_spectrum and _rasterize, src/planet_renderer/ocean.py
+    :193-771) run unmodified on seeded G-buffers holding terrain pixels in
+    front of and behind the sea surface and sky: near-field wave geometry by
+    fixed-point sphere solves, the reseeded outer sphere for a high camera's
+    grazing rays, the flat sea level with the advanced path off, a camera
+    below the crests, the debug colourings."""
+
+    shim.install()
+    sys.path.insert(0, str(reference / "src"))
+    from planet_renderer.ocean import OCEAN_SURFACE_ID, OceanConfig, OceanRenderer  # type: ignore
+
+    from planet_renderer_gb300 import camera as cam
+
+    out = {}
+    for k, (w, h, seed, altitude, pitch, yaw, time_s, mode, overrides) in enumerate(OCEAN_CASES):
+        rng = np.random.default_rng(seed)
+        f32 = np.float32
+        config = OceanConfig(**overrides)
+        ocean = OceanRenderer(w, h, config)
+        tanfov = cam.tangent_half_fov(60.0)
+        basis = cam.view_basis(yaw, pitch)
+        # the camera's local frame in planet coordinates: a seeded rotation
+        q = np.linalg.qr(rng.normal(size=(3, 3)))[0]
+        frame = (q[:, 0], q[:, 1], np.cross(q[:, 0], q[:, 1]))
+        xs = (np.arange(w) + 0.5) / w * 2.0 - 1.0
+        ys = (np.arange(h) + 0.5) / h * 2.0 - 1.0
+        rays = np.stack(np.broadcast_arrays(xs[:, None] * tanfov * w / h, ys[None, :] * tanfov,
+                                            np.ones((w, h))), -1)
+        depth = rng.uniform(1.0, 4.0, (w, h)) * np.exp(rng.uniform(0.0, 9.0, (w, h)))
+        sid = np.where(rng.random((w, h)) < 0.6, rng.integers(0, 5000, (w, h)), -1).astype(np.int32)
+        g = {
+            "depth": depth.astype(f32),
+            "position": (rays * depth[..., None]).astype(f32),
+            "normal": (np.array([0.0, 1.0, 0.0]) + rng.normal(0.0, 0.3, (w, h, 3))).astype(f32),
+            "albedo": rng.uniform(0.02, 0.6, (w, h, 3)).astype(f32),
+            "material_weights": rng.dirichlet(np.ones(4), (w, h)).astype(f32),
+            "height_m": rng.uniform(-200.0, 900.0, (w, h)).astype(f32),
+            "water_depth": rng.uniform(0.0, 50.0, (w, h)).astype(f32),
+            "seabed_albedo": rng.uniform(0.0, 0.3, (w, h, 3)).astype(f32),
+            "seabed_normal": rng.normal(0.0, 1.0, (w, h, 3)).astype(f32),
+            "slope_variance": rng.uniform(0.0, 0.1, (w, h)).astype(f32),
+            "surface_id": sid,
+            "cell_id": rng.integers(0, 1 << 20, (w, h)).astype(np.int32),
+        }
+        fields = {}
+        for name, values in g.items():
+            if values.ndim == 3:
+                fld = shim.Vector.field(values.shape[-1], dtype=shim.f32, shape=(w, h))
+            else:
+                fld = shim.field(dtype=shim.i32 if values.dtype == np.int32 else shim.f32, shape=(w, h))
+            fld.from_numpy(values)
+            fields[name] = fld
+        radius = 6_371_000.0
+        ocean.rasterize(*(fields[n] for n in ("depth", "position", "normal", "albedo", "material_weights",
+                                               "height_m", "water_depth", "seabed_albedo", "seabed_normal",
+                                               "slope_variance", "surface_id", "cell_id")),
+                        radius, altitude, frame, basis, tanfov, time_s, mode)
+        pre = f"case{k}_"
+        for name, values in g.items():
+            out[pre + "in_" + name] = values
+            out[pre + name] = fields[name].to_numpy()
+        if config.enabled:
+            out[pre + "spectrum_height"] = ocean.spectrum_height.to_numpy()
+            out[pre + "spectrum_gradient"] = ocean.spectrum_gradient.to_numpy()
+            out[pre + "spectrum_displacement"] = ocean.spectrum_displacement.to_numpy()
+            out[pre + "spectrum_jacobian"] = ocean.spectrum_displacement_jacobian.to_numpy()
+        out[pre + "args"] = np.array(json.dumps({
+            "width": w, "height": h, "planet_radius_m": radius, "camera_altitude_m": altitude,
+            "planet_frame": [list(map(float, v)) for v in frame], "view_basis": [list(map(float, v)) for v in basis],
+            "tangent_half_fov": float(tanfov), "time_seconds": time_s, "debug_mode": mode, "config": overrides}))
+    out["meta"] = np.array(json.dumps({"name": "ocean", "cases": len(OCEAN_CASES), "ocean_surface_id": OCEAN_SURFACE_ID,
+                                       "generator": "reference ocean.py OceanRenderer.rasterize through "
+                                                    "taichi_f32_shim"}))
+    return out
+
+
 RASTER_TOPOLOGIES = (2, 5, 12, 32)
 
 
@@ -619,6 +708,8 @@ def main() -> None:
         np.savez_compressed(HERE / "model_reference.npz", **model_reference(args.reference))
     if want("shading") and args.precision == "f32":
         np.savez_compressed(HERE / "shading.npz", **shading_reference(args.reference))
+    if want("ocean") and args.precision == "f32":
+        np.savez_compressed(HERE / "ocean.npz", **ocean_reference(args.reference))
     if want("raster") and args.precision == "f32":
         np.savez_compressed(HERE / "raster.npz", **raster_reference(args.reference))
     if want("postprocess") and args.precision == "f32":

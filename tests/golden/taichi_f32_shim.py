@@ -107,6 +107,10 @@ class Vec(np.ndarray):
     def z(self):
         return self[2]
 
+    @property
+    def w(self):
+        return self[3]
+
     def __getitem__(self, item):
         value = np.ndarray.__getitem__(self, item)
         if isinstance(value, np.ndarray) and value.ndim == 0:

@@ -1,0 +1,138 @@
+"""The ocean coverage pass (atm_ocean_rasterize through OceanRenderer)
+against the reference's own kernels (golden vectors, tests/golden/ocean.npz)
+and the float32 oracle (oracle/ocean.py) on larger seeded frames.
+
+Bar: float32 rounding.  Every operation follows the reference's order
+without contraction, but the wave spectrum's sines and cosines are CUDA's
+sinf / cosf, whose last bit can differ from the reference runtime's, so each
+value must agree within 1e-4 relative plus 1e-5 of the image's largest
+magnitude (1e-3 for the wave-slope quantities, which divide by the map's
+determinant), and the covered pixels must be the same."""
+
+from __future__ import annotations
+
+import json
+
+import numpy as np
+import pytest
+import torch
+
+from test_ocean import IMAGES, golden_case
+
+pytestmark = pytest.mark.gpu
+LOOSE = ("normal", "slope_variance")
+
+
+def _check(got, ref, label=""):
+    np.testing.assert_array_equal(got["surface_id"], ref["surface_id"], err_msg=label + "surface_id")
+    np.testing.assert_array_equal(got["cell_id"], ref["cell_id"], err_msg=label + "cell_id")
+    for name in IMAGES:
+        if name in ("surface_id", "cell_id"):
+            continue
+        a, b = got[name].astype(np.float64), ref[name].astype(np.float64)
+        rtol = 1e-3 if name in LOOSE else 1e-4
+        tol = rtol * np.abs(b) + 1e-5 * max(float(np.abs(b).max()), 1e-30)
+        bad = np.abs(a - b) > tol
+        assert not bad.any(), f"{label}{name}: {bad.sum()} values off, worst {np.abs(a - b).max():.3g}"
+
+
+def _run(inputs, cfg_kwargs, a, layout="wh", channels=3):
+    from planet_renderer_gb300.ocean import OceanConfig, OceanRenderer
+
+    W, H = inputs["surface_id"].shape
+    g = {}
+    for name in IMAGES:
+        x = inputs[name]
+        if x.ndim == 3 and x.shape[-1] == 3 and channels == 4:
+            x = np.concatenate([x, np.zeros(x.shape[:2] + (1,), x.dtype)], -1)
+        if layout == "hw":
+            x = np.swapaxes(x, 0, 1)
+        g[name] = torch.as_tensor(np.ascontiguousarray(x), device="cuda")
+    r = OceanRenderer(W, H, OceanConfig(**cfg_kwargs), layout=layout)
+    r.rasterize_gbuffer(g, a["planet_radius_m"], a["camera_altitude_m"], a["planet_frame"], a["view_basis"],
+                        a["tangent_half_fov"], a["time_seconds"], a["debug_mode"])
+    out = {k: v.cpu().numpy() for k, v in g.items()}
+    if layout == "hw":
+        out = {k: np.swapaxes(v, 0, 1) for k, v in out.items()}
+    out = {k: (v[..., :3] if v.ndim == 3 and k != "material_weights" else v) for k, v in out.items()}
+    spectrum = r.spectrum() if r.config.enabled else None
+    r.close()
+    return out, spectrum
+
+
+@pytest.mark.parametrize("case", [0, 1, 2, 3])
+def test_ocean_matches_the_reference_golden(case):
+    a, inputs, ref, ref_spectrum = golden_case(case)
+    got, spectrum = _run(inputs, a["config"], a)
+    if ref_spectrum is not None:
+        for name, y in zip(("height", "gradient", "displacement", "jacobian"), ref_spectrum):
+            x = spectrum[name]
+            np.testing.assert_allclose(x, y, rtol=1e-4, atol=1e-5 * float(np.abs(y).max()), err_msg=name)
+    _check(got, ref, f"case {case}: ")
+
+
+def _frame(W, H, seed):
+    """A seeded G-buffer of terrain (nearer and farther than the sea) and sky."""
+
+    rng = np.random.default_rng(seed)
+    depth = (rng.uniform(1.0, 4.0, (W, H)) * np.exp(rng.uniform(0.0, 10.0, (W, H)))).astype(np.float32)
+    rays = np.stack(np.broadcast_arrays(np.linspace(-1, 1, W)[:, None], np.linspace(-0.6, 0.6, H)[None, :],
+                                        np.ones((W, H))), -1)
+    return {"depth": depth, "position": (rays * depth[..., None]).astype(np.float32),
+            "normal": rng.normal(0.0, 1.0, (W, H, 3)).astype(np.float32),
+            "albedo": rng.uniform(0.0, 1.0, (W, H, 3)).astype(np.float32),
+            "material_weights": rng.uniform(0.0, 1.0, (W, H, 4)).astype(np.float32),
+            "height_m": rng.uniform(-100.0, 100.0, (W, H)).astype(np.float32),
+            "water_depth": rng.uniform(0.0, 9.0, (W, H)).astype(np.float32),
+            "seabed_albedo": rng.uniform(0.0, 1.0, (W, H, 3)).astype(np.float32),
+            "seabed_normal": rng.normal(0.0, 1.0, (W, H, 3)).astype(np.float32),
+            "slope_variance": rng.uniform(0.0, 1.0, (W, H)).astype(np.float32),
+            "surface_id": np.where(rng.random((W, H)) < 0.5, rng.integers(0, 9999, (W, H)), -1).astype(np.int32),
+            "cell_id": rng.integers(0, 1 << 24, (W, H)).astype(np.int32)}
+
+
+@pytest.mark.parametrize("altitude,pitch,config,layout,channels", [
+    (8.0, -3.0, {}, "wh", 3),
+    (1500.0, -20.0, {"spectrum_resolution": 256, "geometry_cascades": 3}, "hw", 4),
+    (0.3, 2.0, {"wind_speed_mps": 30.0, "choppiness": 1.0, "spectrum_resolution": 64}, "wh", 4),
+    (400_000.0, -60.0, {}, "hw", 3),
+])
+def test_ocean_matches_the_oracle(altitude, pitch, config, layout, channels):
+    """Default and heavier configurations at 192x108 against the oracle: a
+    near-surface camera inside the crests, a low camera, one over the
+    displaced near field, and an orbital camera (only the flat sphere)."""
+
+    from oracle import ocean
+    from planet_renderer_gb300 import camera as cam
+
+    W, H = 192, 108
+    inputs = _frame(W, H, int(altitude) + 7)
+    q = np.linalg.qr(np.random.default_rng(3).normal(size=(3, 3)))[0]
+    a = {"planet_radius_m": 6_371_000.0, "camera_altitude_m": altitude,
+         "planet_frame": (q[:, 0], q[:, 1], np.cross(q[:, 0], q[:, 1])), "view_basis": cam.view_basis(30.0, pitch),
+         "tangent_half_fov": cam.tangent_half_fov(60.0), "time_seconds": 17.25, "debug_mode": 0}
+    ref, _ = ocean.rasterize(inputs, ocean.OceanSettings(**config), a["planet_radius_m"], altitude,
+                             a["planet_frame"], a["view_basis"], a["tangent_half_fov"], a["time_seconds"], 0)
+    got, _ = _run(inputs, config, a, layout, channels)
+    assert (ref["surface_id"] == ocean.OCEAN_SURFACE_ID).mean() > 0.1
+    _check(got, ref)
+
+
+def test_ocean_surface_disabled_writes_nothing_and_rejects_bad_input():
+    from planet_renderer_gb300.ocean import OceanConfig, OceanRenderer
+
+    a, inputs, _, _ = golden_case(0)
+    got, _ = _run(inputs, dict(a["config"], surface_enabled=False), a)
+    for name in IMAGES:
+        np.testing.assert_array_equal(got[name], inputs[name][..., :3] if inputs[name].ndim == 3 and
+                                      name != "material_weights" else inputs[name])
+    W, H = inputs["surface_id"].shape
+    r = OceanRenderer(W + 1, H, OceanConfig())
+    g = {n: torch.as_tensor(v, device="cuda") for n, v in inputs.items()}
+    with pytest.raises(ValueError):
+        r.rasterize_gbuffer(g, a["planet_radius_m"], 10.0, a["planet_frame"], a["view_basis"], 0.5, 0.0, 0)
+    r.close()
+    r = OceanRenderer(W, H, OceanConfig())
+    with pytest.raises(RuntimeError):
+        r.rasterize_gbuffer(g, -1.0, 10.0, a["planet_frame"], a["view_basis"], 0.5, 0.0, 0)
+    r.close()
