@@ -614,6 +614,14 @@ typedef struct AtmRasterOutputs {
   float* height_m;
   int32_t* surface_id;
   int32_t* cell_id;
+  /* The opaque terrain snapshot the ocean shading reads
+   * (_snapshot_terrain_gbuffer, renderer.py:1270-1275), written in the same
+   * pass; null terrain_surface_id skips it.  Uncovered pixels get
+   * terrain_surface_id = -1 (the other snapshot values are not read there). */
+  float* terrain_position;
+  float* terrain_normal;
+  float* terrain_albedo;
+  int32_t* terrain_surface_id;
 } AtmRasterOutputs;
 typedef struct AtmRaster AtmRaster;
 /* PlanetRenderer's raster buffers (renderer.py:200-236): the emitted-triangle

@@ -1515,8 +1515,11 @@ ATM_API int atm_raster_terrain(AtmRaster* r, const AtmRasterMesh* m, double near
                        m->slot_level, m->patches,    m->vertices_per_patch, m->triangles_per_patch,
                        m->surface_triangles_per_patch, m->resolution, m->n_active};
   atm::RasterStream S{r->tris, r->count, r->capacity};
-  atm::RasterOutDev O{o->depth, o->position, o->normal, o->albedo, o->material_weights, o->height_m,
-                      o->surface_id, o->cell_id};
+  if (o->terrain_surface_id && (!o->terrain_position || !o->terrain_normal || !o->terrain_albedo))
+    return fail(ATM_E_INVALID, "the terrain snapshot needs position, normal and albedo images");
+  atm::RasterOutDev O{o->depth,          o->position,        o->normal,           o->albedo,
+                      o->material_weights, o->height_m,      o->surface_id,       o->cell_id,
+                      o->terrain_position, o->terrain_normal, o->terrain_albedo, o->terrain_surface_id};
   ATM_CUDA(atm::launch_raster(M, S, layout_of(image), r->depth_key, O, float(near_m), float(tangent_half_fov),
                               view_mode, r->sm_count, static_cast<cudaStream_t>(stream)),
            "terrain raster");

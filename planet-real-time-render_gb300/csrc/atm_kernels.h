@@ -274,6 +274,10 @@ struct RasterOutDev {
   float* height;
   int32_t* surface_id;
   int32_t* cell_id;
+  float* t_position;  // the terrain snapshot (null t_surface_id: not written)
+  float* t_normal;
+  float* t_albedo;
+  int32_t* t_surface_id;
 };
 cudaError_t launch_raster(const RasterMeshDev& M, const RasterStream& S, const ImageLayout& L,
                           unsigned long long* depth_key, const RasterOutDev& O, float near, float tf, int mode,

@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLay
   if (key == kSentinel) {
     O.surface_id[e] = -1;
     O.cell_id[e] = -1;
+    if (O.t_surface_id) O.t_surface_id[e] = -1;
     return;
   }
   const float z = __uint_as_float(uint32_t(key >> 32));
@@ -333,6 +334,12 @@ __global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLay
   O.albedo[e * c + 0] = albedo.x, O.albedo[e * c + 1] = albedo.y, O.albedo[e * c + 2] = albedo.z;
   for (int j = 0; j < 4; ++j) O.material[e * 4 + j] = bm[j];
   O.height[e] = bh;
+  if (O.t_surface_id) {  // _snapshot_terrain_gbuffer, fused
+    O.t_surface_id[e] = src;
+    O.t_position[e * c + 0] = bp.x, O.t_position[e * c + 1] = bp.y, O.t_position[e * c + 2] = bp.z;
+    O.t_normal[e * c + 0] = bn.x, O.t_normal[e * c + 1] = bn.y, O.t_normal[e * c + 2] = bn.z;
+    O.t_albedo[e * c + 0] = albedo.x, O.t_albedo[e * c + 1] = albedo.y, O.t_albedo[e * c + 2] = albedo.z;
+  }
 }
 
 __global__ void k_raster_clear(unsigned long long* __restrict__ depth_key, long long n, uint32_t* count) {

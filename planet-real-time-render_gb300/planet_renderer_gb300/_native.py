@@ -233,7 +233,8 @@ class AtmRasterMesh(ctypes.Structure):
                                             "surface_triangles_per_patch", "resolution", "n_active")]
 
 
-RASTER_OUTPUTS = ("depth", "position", "normal", "albedo", "material_weights", "height_m", "surface_id", "cell_id")
+RASTER_OUTPUTS = ("depth", "position", "normal", "albedo", "material_weights", "height_m", "surface_id", "cell_id",
+                  "terrain_position", "terrain_normal", "terrain_albedo", "terrain_surface_id")
 
 
 class AtmRasterOutputs(ctypes.Structure):

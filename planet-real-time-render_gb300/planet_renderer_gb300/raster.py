@@ -33,6 +33,12 @@ MAX_CLIPPED_TRIANGLES = 6  # renderer.py:37
 OUTPUTS = {"depth": (torch.float32, 0), "position": (torch.float32, -1), "normal": (torch.float32, -1),
            "albedo": (torch.float32, -1), "material_weights": (torch.float32, 4), "height_m": (torch.float32, 0),
            "surface_id": (torch.int32, 0), "cell_id": (torch.int32, 0)}
+# the opaque terrain snapshot the ocean shading reads (written when all four are given)
+SNAPSHOT = {"terrain_position": (torch.float32, -1), "terrain_normal": (torch.float32, -1),
+            "terrain_albedo": (torch.float32, -1), "terrain_surface_id": (torch.int32, 0)}
+# the rest of a frame's G-buffer, written by the ocean coverage pass
+OCEAN_EXTRA = {"water_depth": (torch.float32, 0), "seabed_albedo": (torch.float32, -1),
+               "seabed_normal": (torch.float32, -1), "slope_variance": (torch.float32, 0)}
 
 
 def shared_topology(resolution: int) -> np.ndarray:
@@ -166,17 +172,21 @@ class TerrainRaster:
     def capacity(self) -> int:
         return self.max_patches * self.triangles_per_patch * MAX_CLIPPED_TRIANGLES
 
-    def allocate_gbuffer(self, channels: int = 3) -> dict:
-        """Empty G-buffer images of this raster's size and layout."""
+    def allocate_gbuffer(self, channels: int = 3, snapshot: bool = False, ocean: bool = False) -> dict:
+        """Empty G-buffer images of this raster's size and layout; with
+        ``snapshot`` also the terrain snapshot, with ``ocean`` also the
+        images the ocean pass adds (a whole frame's G-buffer)."""
 
         dims = (self.width, self.height) if self.layout == "wh" else (self.height, self.width)
         out = {}
-        for name, (dtype, per) in OUTPUTS.items():
+        images = dict(OUTPUTS, **(SNAPSHOT if snapshot else {}), **(OCEAN_EXTRA if ocean else {}))
+        for name, (dtype, per) in images.items():
             per = channels if per < 0 else per
             shape = dims + ((per,) if per else ())
             out[name] = torch.zeros(shape, dtype=dtype, device=self.device)
-        out["surface_id"].fill_(-1)
-        out["cell_id"].fill_(-1)
+        for name in ("surface_id", "cell_id", "terrain_surface_id"):
+            if name in out:
+                out[name].fill_(-1)
         return out
 
     def _image(self, gbuffer: dict) -> _native.AtmImage:
@@ -192,7 +202,10 @@ class TerrainRaster:
         if dims != (self.width, self.height):
             raise ValueError(f"G-buffer is {dims[0]}x{dims[1]}, the raster {self.width}x{self.height}")
         strides = _element_strides(ref, channels, self.layout)
-        for name, (dtype, per) in OUTPUTS.items():
+        snapshot = [n for n in SNAPSHOT if n in gbuffer]
+        if snapshot and len(snapshot) != len(SNAPSHOT):
+            raise ValueError(f"the terrain snapshot needs all of {list(SNAPSHOT)}")
+        for name, (dtype, per) in dict(OUTPUTS, **{n: SNAPSHOT[n] for n in snapshot}).items():
             t = gbuffer[name]
             per = channels if per < 0 else per
             if not isinstance(t, torch.Tensor) or t.dtype != dtype or t.device != self.device:
@@ -213,7 +226,9 @@ class TerrainRaster:
         ``active_slots`` int32, optional ``skirt_mask`` and ``slot_level``
         (patches,) int32, and the ints ``surface_triangles`` and
         ``resolution``.  ``view_mode``: 0 lit albedo, 1 height bands, 2 LOD
-        level, 3 patch hash."""
+        level, 3 patch hash.  When ``gbuffer`` also holds the ``SNAPSHOT``
+        images the same pass writes the terrain snapshot
+        (_snapshot_terrain_gbuffer) into them."""
 
         image = self._image(gbuffer)
         view = mesh["view"]
@@ -253,7 +268,8 @@ class TerrainRaster:
         m.surface_triangles_per_patch = int(mesh.get("surface_triangles", tri.shape[0]))
         m.resolution = int(mesh.get("resolution", 1))
         m.n_active = n_active
-        outs = _native.AtmRasterOutputs(*[ctypes.c_void_p(gbuffer[n].data_ptr()) for n in _native.RASTER_OUTPUTS])
+        outs = _native.AtmRasterOutputs(*[ctypes.c_void_p(gbuffer[n].data_ptr() if n in gbuffer else None)
+                                          for n in _native.RASTER_OUTPUTS])
         stream = torch.cuda.current_stream(self.device).cuda_stream
         _native.check(self._lib.atm_raster_terrain(self._handle, ctypes.byref(m), float(near), float(tangent_half_fov),
                                                    int(view_mode), ctypes.byref(outs), ctypes.byref(image),

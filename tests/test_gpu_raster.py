@@ -37,17 +37,24 @@ def _mesh_tensors(view, normal, material, height, cell, triangles, active, skirt
 
 
 def _render(mesh, width, height, near, tf, mode, layout="wh", channels=3):
+    """One frame through TerrainRaster with the terrain snapshot written in
+    the same pass; the snapshot must equal the G-buffer it copies."""
+
     from planet_renderer_gb300.raster import TerrainRaster
 
     r = TerrainRaster(width, height, mesh["view"].shape[0], mesh["triangles"].shape[0], layout=layout)
-    g = r.allocate_gbuffer(channels)
+    g = r.allocate_gbuffer(channels, snapshot=True)
     r.render(mesh, near, tf, g, view_mode=mode)
     count = r.emitted()
     out = {k: v.cpu().numpy() for k, v in g.items()}
     if layout == "hw":
         out = {k: np.swapaxes(v, 0, 1) for k, v in out.items()}
-    for k in ("position", "normal", "albedo"):
+    for k in ("position", "normal", "albedo", "terrain_position", "terrain_normal", "terrain_albedo"):
         out[k] = out[k][..., :3]
+    np.testing.assert_array_equal(out["terrain_surface_id"], out["surface_id"])
+    cov = out["surface_id"] >= 0
+    for k in ("position", "normal", "albedo"):
+        np.testing.assert_array_equal(out["terrain_" + k][cov], out[k][cov])
     r.close()
     return out, count
 
