@@ -499,6 +499,7 @@ def main() -> None:
     post = None if args.no_post else _postprocess_4k(device, args)
     shade = None if args.no_post else _shading_4k(device, args)
     raster = None if args.no_raster else _raster_4k(device, args)
+    mesh_frame = None if args.no_raster else _frame_from_mesh_4k(device, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -525,6 +526,7 @@ def main() -> None:
             "postprocess_4k": post,
             "shading_4k": shade,
             "raster_4k": raster,
+            "frame_from_mesh_4k": mesh_frame,
             "samples_per_step": samples_per_step,
             "e2e": {"value": world * e2e_samples / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_s / e2e_steps,
@@ -792,6 +794,76 @@ def _raster_4k(device, args, steps=20) -> dict:
         torch.cuda.empty_cache()
     out["workload"] = ("3840x2160 terrain raster (clip + depth keys + resolve) of a 2 km ground camera's synthetic "
                        "terrain, 60 degree vertical field of view, near 0.5 m")
+    return out
+
+
+def _frame_from_mesh_4k(device, args, steps=10) -> dict:
+    """A whole 3840x2160 frame from terrain patches to the display image, in
+    the reference renderer's order (renderer.py:1626-1735): terrain raster
+    with the snapshot -> ocean coverage -> atmosphere update -> fused surface
+    lighting + shading + composite -> display post-process.  The ground
+    camera 30 m above sea level looks 6 degrees down over the synthetic
+    coast (the default patch budget, 256 patches of 12 cells; 200 m relief
+    rising inland, its valleys below sea level are sea), sun 35 degrees up.  One CUDA graph per frame;
+    device ms per frame and per stage."""
+
+    import numpy as np
+    import torch
+
+    from planet_renderer_gb300 import camera as cam
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.workloads import (EARTH_RADIUS_M, SOLAR_IRRADIANCE,
+                                                            SUN_ANGULAR_RADIUS_DEG)
+    from planet_renderer_gb300.lighting import LightingState
+    from planet_renderer_gb300.ocean import OCEAN_SURFACE_ID, OceanConfig, OceanRenderer
+    from planet_renderer_gb300.postprocess import PostprocessConfig, PostProcessor
+    from planet_renderer_gb300.raster import TerrainRaster, synthetic_terrain
+
+    W, H, tf, alt = 3840, 2160, math.tan(math.radians(30.0)), 30.0
+    mesh = synthetic_terrain(W, H, tf, altitude_m=alt, pitch_degrees=6.0, relief_m=200.0, base_height_m=0.0,
+                             rise_m_per_km=10.0, seed=SEED, device=device)
+    basis = mesh["view_basis"]
+    frame = (np.array([1.0, 0.0, 0.0]), np.array([0.0, 1.0, 0.0]), np.array([0.0, 0.0, 1.0]))
+    sun = cam.sun_local(150.0, 35.0)
+    light = LightingState(sun, SUN_ANGULAR_RADIUS_DEG, SOLAR_IRRADIANCE)
+    raster = TerrainRaster(W, H, int(mesh["view"].shape[0]), int(mesh["triangles"].shape[0]), device=device)
+    g = raster.allocate_gbuffer(3, snapshot=True, ocean=True)
+    sea = OceanRenderer(W, H, OceanConfig(), device=device)
+    atm = AtmosphereRenderer(W, H, earth_baseline(), device=device)
+    post = PostProcessor(W, H, PostprocessConfig(), device=device)
+    space_hdr = torch.zeros(W, H, 3, device=device)
+    hdr = torch.zeros(W, H, 3, device=device)
+    display = torch.zeros(W, H, 3, device=device)
+    R = EARTH_RADIUS_M
+    args_atm = (R, R + alt, sun, SOLAR_IRRADIANCE, light.sun_disk_radiance, SUN_ANGULAR_RADIUS_DEG, basis, tf, 4.0,
+                12.0)
+    stages = {
+        "raster": lambda: raster.render(mesh, 0.5, tf, g),
+        "ocean": lambda: sea.rasterize_gbuffer(g, R, alt, frame, basis, tf, 12.5, 0),
+        "atmosphere": lambda: (atm.update(R, R + alt, sun, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG),
+                               atm.render_frame(g, space_hdr, hdr, *args_atm)),
+        "post": lambda: post.process(hdr, display, 0.0, bloom=True, tone_map=True),
+    }
+    whole = lambda: [fn() for fn in stages.values()]
+    out = {"workload": "3840x2160 frame from terrain patches to display: raster + snapshot, ocean coverage, "
+                       "atmosphere update, fused lighting + shading + composite, bloom + tone map; ground camera "
+                       "30 m above sea level, 256 patches x 12 cells, default ocean; CUDA graphs"}
+    for name, fn in list(stages.items()) + [("frame", whole)]:
+        graphs = _capture_fn([()], device, fn)
+        for _ in range(3):
+            graphs[0].replay()
+        out[f"{name}_ms"] = _timed_graph_region(graphs, steps, device) / steps
+        del graphs
+    sid = g["surface_id"]
+    out["sea_px"] = int((sid == OCEAN_SURFACE_ID).sum())
+    out["terrain_px"] = int(((sid >= 0) & (sid != OCEAN_SURFACE_ID)).sum())
+    out["emitted_triangles"] = raster.emitted()
+    out["display_finite"] = bool(torch.isfinite(display).all())
+    for o in (raster, sea, atm, post):
+        o.close()
+    del g, mesh
+    torch.cuda.empty_cache()
     return out
 
 
@@ -1373,8 +1445,16 @@ def _profile_raster(args):
     print("profile case raster4k:", {k: round(v["ms"], 3) for k, v in out.items() if isinstance(v, dict)})
 
 
+def _profile_mesh_frame(args):
+    """The whole 4K frame from terrain patches to display, three frames."""
+
+    out = _frame_from_mesh_4k(__import__("torch").device("cuda:0"), argparse.Namespace(warmup=3), steps=3)
+    print("profile case meshframe4k:", {k: v for k, v in out.items() if k != "workload"})
+
+
 PROFILE_CASES = {
     "raster4k": _profile_raster,
+    "meshframe4k": _profile_mesh_frame,
     "frame1080p": _profile_frame_1080p,
     "frame4k_mlp": _profile_frame_4k_mlp,
     "luts": _profile_luts,

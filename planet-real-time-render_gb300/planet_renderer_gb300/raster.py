@@ -69,15 +69,21 @@ def shared_topology(resolution: int) -> np.ndarray:
 def synthetic_terrain(width: int, height: int, tangent_half_fov: float, altitude_m: float = 2000.0,
                       pitch_degrees: float = 8.0, rows: int = 16, columns: int = 16, resolution: int = 12,
                       far_m: float = 80_000.0, planet_radius_m: float = 6_371_000.0, seed: int = 0,
+                      relief_m: float = 380.0, base_height_m: float = 150.0, rise_m_per_km: float = 0.0,
                       device: str | torch.device = "cuda") -> dict:
     """A seeded terrain frame in camera view space for ``render``: rows x
     columns patches of ``resolution`` cells a side tiling the ground in the
     view frustum from the camera's foot to ``far_m`` (rows growing
     geometrically with distance, as a distance-based LOD does), heights from
-    a few octaves of sinusoids over the planet's curvature drop, outward
-    skirts below every edge, material weights by height and slope.  Stands in
-    for the terrain backend's patch stream (the LOD system is not part of
-    this library)."""
+    a few octaves of sinusoids (largest amplitude ``relief_m``, mean
+    ``base_height_m``, rising ``rise_m_per_km`` with distance) over the
+    planet's curvature drop, outward
+    skirts below every edge, material weights by height and slope.  Vertex
+    positions are in view space (x right, y up, z forward; the camera looks
+    ``pitch_degrees`` down), normals in the camera's local East-Up-North frame
+    (the global frame when the planet frame is the identity), as the
+    reference's patch streams hold them.  Stands in for the terrain backend's
+    patch stream (the LOD system is not part of this library)."""
 
     rng = np.random.default_rng(seed)
     n, side = int(resolution), int(resolution) + 1
@@ -86,7 +92,7 @@ def synthetic_terrain(width: int, height: int, tangent_half_fov: float, altitude
     tx = tangent_half_fov * width / height
     t = np.linspace(0.0, 1.0, side)
     phases = rng.uniform(0.0, 2.0 * math.pi, (6, 2))
-    waves = [(1.0 / (900.0 * 2.2 ** -k), 380.0 * 0.5 ** k) for k in range(6)]
+    waves = [(1.0 / (900.0 * 2.2 ** -k), relief_m * 0.5 ** k) for k in range(6)]
 
     def ground(x, z):
         h = np.zeros_like(x)
@@ -96,7 +102,7 @@ def synthetic_terrain(width: int, height: int, tangent_half_fov: float, altitude
             h += amp * np.sin(u) * np.cos(v)
             dhx += amp * f * np.cos(u) * np.cos(v)
             dhz -= amp * f * 0.83 * np.sin(u) * np.sin(v)
-        return h + 150.0, dhx, dhz
+        return h + base_height_m + rise_m_per_km * 1e-3 * z, dhx, dhz + rise_m_per_km * 1e-3
 
     view, normal, material, hgt, cell = [], [], [], [], []
     pitch = math.radians(pitch_degrees)
@@ -128,7 +134,7 @@ def synthetic_terrain(width: int, height: int, tangent_half_fov: float, altitude
             arid = np.clip(hh / 600.0, 0.0, 1.0) * (1.0 - rock - snow)
             fertile = np.clip(1.0 - arid - rock - snow, 0.0, 1.0)
             view.append(np.stack([pts[:, 0], pts @ up, pts @ fwd], -1))
-            normal.append(np.stack([nr[:, 0], nr @ up, nr @ fwd], -1))
+            normal.append(nr)
             material.append(np.stack([fertile, arid, rock, snow], -1))
             hgt.append(hh)
             cell.append((r * columns + c) * 4096 + np.arange(len(hh)))
@@ -138,7 +144,8 @@ def synthetic_terrain(width: int, height: int, tangent_half_fov: float, altitude
     return {"view": f32(view), "normal": f32(normal), "material": f32(material), "height_m": f32(hgt),
             "cell": i32(cell), "triangles": i32(shared_topology(n)), "active_slots": i32(np.arange(patches)),
             "skirt_mask": i32(np.full(patches, 15)), "slot_level": i32(rows - 1 - np.arange(patches) // columns),
-            "surface_triangles": 2 * n * n, "resolution": n}
+            "surface_triangles": 2 * n * n, "resolution": n,
+            "view_basis": (np.array([1.0, 0.0, 0.0]), up, fwd)}
 
 
 def _element_strides(t: torch.Tensor, per_element: int, layout: str) -> tuple:
