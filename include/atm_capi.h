@@ -382,7 +382,15 @@ typedef struct AtmSurrogate {
   int32_t gate_terminator; /* non-zero: a surface segment whose sun cosine has
                             different signs at its start, middle and end (it
                             crosses the terminator) takes the plain path too */
-  int32_t reserved;
+  int32_t calibration_tile; /* 0: off.  Else the side (a power of two, 16..256
+                            pixels) of the calibration tiles: the checked
+                            pixels' log ratio of the plain path's in-scattering
+                            to the network's, averaged per tile (clamped to
+                            +-0.3; tiles with at least 4 checked pixels),
+                            rescales the network's in-scattering of the
+                            tile's other MLP pixels.  Costs a width x height x
+                            3 float scratch image (allocated on first use) and
+                            one extra pass over the frame.                  */
 } AtmSurrogate;
 
 /* COMPOSITE view of atm_composite with the per-pixel limb integrator replaced

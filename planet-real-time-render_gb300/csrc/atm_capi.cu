@@ -169,6 +169,8 @@ struct AtmHandle {
   // surrogate composite: fallback queue (4 header words: entries, ticket,
   // timeout flag, padding; then width * height entries)
   uint32_t* queue = nullptr;
+  float* calib_lm = nullptr;     // the surrogate calibration's scratch image (width x height x 3)
+  float* calib_tiles = nullptr;  // its tile sums, sized for the smallest tile (16 pixels)
   int sm_count = 0;
 };
 
@@ -296,6 +298,8 @@ ATM_API int atm_destroy(AtmHandle* h) {
   }
   if (h->samples) cudaFree(h->samples);
   if (h->queue) cudaFree(h->queue);
+  if (h->calib_lm) cudaFree(h->calib_lm);
+  if (h->calib_tiles) cudaFree(h->calib_tiles);
   delete h;
   return ATM_OK;
 }
@@ -1048,6 +1052,29 @@ int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m
   Q.items = h->queue + 4;
   Q.stats = sg->stats;
   Q.check_fraction = float(sg->check_fraction);
+  if (sg->calibration_tile != 0) {
+    const int t = sg->calibration_tile;
+    if (t < 16 || t > 256 || (t & (t - 1)) != 0)
+      return fail(ATM_E_INVALID, "calibration_tile must be 0 or a power of two in 16..256");
+    if (!h->calib_lm) {
+      const size_t px = size_t(h->width) * size_t(h->height);
+      const size_t tiles = size_t((h->width + 15) / 16) * size_t((h->height + 15) / 16);
+      float *lm = nullptr, *sums = nullptr;
+      cudaError_t e = cudaMalloc(&lm, px * 3 * sizeof(float));
+      if (e == cudaSuccess) e = cudaMalloc(&sums, tiles * 4 * sizeof(float));
+      if (e != cudaSuccess) {
+        if (lm) cudaFree(lm);
+        return cuda_fail(e, "calibration scratch");
+      }
+      h->calib_lm = lm;
+      h->calib_tiles = sums;
+    }
+    Q.lm = h->calib_lm;
+    Q.tiles = h->calib_tiles;
+    Q.tile_shift = 0;
+    while ((1 << Q.tile_shift) < t) ++Q.tile_shift;
+    Q.tiles_x = (h->width + t - 1) / t;
+  }
   Q.seed = sg->seed;
   return ATM_OK;
 }

@@ -130,7 +130,20 @@ struct SurrogateQueue {
   float* stats;       // null or kSurrogateStats floats, accumulated
   float check_fraction;
   uint32_t seed;
+  // Calibration of the aerial network from the checked pixels (null lm: off).
+  // lm: width x height x 3 floats in storage order (the image's contiguous
+  // axis first): each MLP surface pixel's network in-scattering, x < 0 where
+  // none is to be rescaled.  tiles: per calibration tile (side 1 <<
+  // tile_shift, tiles_x per row) the checked pixels' summed log ratios
+  // (RGB) and their count.
+  float* lm;
+  float* tiles;
+  int tile_shift, tiles_x;
 };
+// a calibration tile applies when it holds this many checked pixels; each
+// checked pixel's log ratio is clamped to +-kCalibrationClamp
+constexpr int kCalibrationMinChecks = 4;
+constexpr float kCalibrationClamp = 0.3f;
 // stats: checked pixels, sum of their relative errors, max relative error,
 // gated surface pixels (plain integrator), MLP surface pixels, MLP sky
 // pixels, gated sky pixels (sky-view LUT), 128-pixel tiles whose tensor-core

@@ -204,6 +204,12 @@ __device__ __forceinline__ bool check_pixel(int x, int y, unsigned seed, float f
   return float(h >> 8) * (1.0f / 16777216.0f) < fraction;
 }
 
+// A pixel's index in storage order (the image's contiguous axis first), the
+// order of the calibration scratch image.
+__device__ __forceinline__ size_t storage_index(const ImageLayout& L, int x, int y) {
+  return L.sy <= L.sx ? size_t(x) * size_t(L.height) + size_t(y) : size_t(y) * size_t(L.width) + size_t(x);
+}
+
 // Largest per-channel error of `got` relative to `ref` (floor 1e-6 E).
 __device__ __forceinline__ float color_error(f3 got, f3 ref, f3 E) {
   const f3 d = vmax(got - ref, 0.0f) + vmax(ref - got, 0.0f);
@@ -356,6 +362,7 @@ __global__ void __launch_bounds__(256, 3) k_composite_surrogate(
 
   bool queued = false;
   uint32_t qkind = kQueueSurface;
+  f3 Lnet = mk(-1.0f, 0.0f, 0.0f);  // the network's in-scattering (x < 0: none)
   if (inside && kind != kSurfPlain) {
     f3 color = kShade ? shaded_scene(P, F, A, S, L, I, x, y, e, sid[e]) : ld3(scene + o);
     if (kind == kSurfMlp) {
@@ -364,6 +371,7 @@ __global__ void __launch_bounds__(256, 3) k_composite_surrogate(
       const f3 Tm = surface_segment_t(P, F, camera_ray_geom(P, A.bottom, A.cam_alt, ray), ray, start, end);
       const f3 Lm = net_radiance(yv, A.E, splat(nets.floor) + Tm * nets.floor_t);
       color = Lm + color * Tm;
+      Lnet = Lm;
       if (check_pixel(x, y, Q.seed, Q.check_fraction)) {
         queued = true;
         qkind = kQueueSurfaceCheck;
@@ -384,6 +392,14 @@ __global__ void __launch_bounds__(256, 3) k_composite_surrogate(
     hdr[o + 2] = color.z;
   } else if (kind == kSurfPlain) {
     queued = true;
+  }
+  if (inside && Q.lm != nullptr) {  // the calibration's scratch: every pixel, each frame
+    float* lm = Q.lm + 3 * storage_index(L, x, y);
+    lm[0] = Lnet.x;
+    if (Lnet.x >= 0.0f) {
+      lm[1] = Lnet.y;
+      lm[2] = Lnet.z;
+    }
   }
 
   // warp-aggregated append to the fallback queue
@@ -444,9 +460,27 @@ __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
       } else {
         float start, end;
         const RayGeom G = camera_ray_geom(P, A.bottom, A.cam_alt, ray);
-        if (surface_interval(P, G, A.bottom, norm(ld3(pos + o)), start, end))
-          color = integrate_surface(P, F, G, ray, start, end, samples) +
-                  color * surface_segment_t(P, F, G, ray, start, end);
+        if (surface_interval(P, G, A.bottom, norm(ld3(pos + o)), start, end)) {
+          const f3 Ls = integrate_surface(P, F, G, ray, start, end, samples);
+          color = Ls + color * surface_segment_t(P, F, G, ray, start, end);
+          if (kind == kQueueSurfaceCheck && Q.lm != nullptr) {
+            // the calibration: this tile's log ratio of the plain in-scattering
+            // to the network's; the pixel itself keeps the plain result
+            float* lm = Q.lm + 3 * storage_index(L, x, y);
+            const f3 Ln = ld3(lm);
+            if (Ln.x >= 0.0f) {
+              float* t = Q.tiles + 4 * ((y >> Q.tile_shift) * Q.tiles_x + (x >> Q.tile_shift));
+              atomicAdd(t + 0, clampf(__logf(mx(Ls.x, 1e-12f) / mx(Ln.x, 1e-12f)), -kCalibrationClamp,
+                                      kCalibrationClamp));
+              atomicAdd(t + 1, clampf(__logf(mx(Ls.y, 1e-12f) / mx(Ln.y, 1e-12f)), -kCalibrationClamp,
+                                      kCalibrationClamp));
+              atomicAdd(t + 2, clampf(__logf(mx(Ls.z, 1e-12f) / mx(Ln.z, 1e-12f)), -kCalibrationClamp,
+                                      kCalibrationClamp));
+              atomicAdd(t + 3, 1.0f);
+            }
+            lm[0] = -1.0f;
+          }
+        }
       }
       color = vmax(color, 0.0f);
       if (kind != kQueueSurface) {
@@ -475,6 +509,32 @@ __global__ void __launch_bounds__(256, 2) k_surrogate_fallback(
       atomicMax(reinterpret_cast<int*>(Q.stats + 2), __float_as_int(err_max));  // non-negative floats
     }
   }
+}
+
+// The calibration pass: every MLP surface pixel whose tile holds enough
+// checked pixels gets its network in-scattering rescaled by the tile's mean
+// log ratio, hdr += Lnet (exp(mean) - 1).  Thread per pixel in storage order.
+__global__ void __launch_bounds__(256) k_surrogate_calibrate(ImageLayout L, SurrogateQueue Q, float* __restrict__ hdr) {
+  const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i >= size_t(L.width) * size_t(L.height)) return;
+  const float* lm = Q.lm + 3 * i;
+  const float lx = lm[0];
+  if (lx < 0.0f) return;
+  int x, y;
+  if (L.sy <= L.sx) {
+    x = int(i / size_t(L.height));
+    y = int(i % size_t(L.height));
+  } else {
+    y = int(i / size_t(L.width));
+    x = int(i % size_t(L.width));
+  }
+  const float4 t = *reinterpret_cast<const float4*>(Q.tiles + 4 * ((y >> Q.tile_shift) * Q.tiles_x + (x >> Q.tile_shift)));
+  if (t.w < float(kCalibrationMinChecks)) return;
+  const float inv = 1.0f / t.w;
+  const size_t o = pix_offset(L, x, y) * L.channels;
+  hdr[o + 0] += lx * (__expf(t.x * inv) - 1.0f);
+  hdr[o + 1] += lm[1] * (__expf(t.y * inv) - 1.0f);
+  hdr[o + 2] += lm[2] * (__expf(t.z * inv) - 1.0f);
 }
 
 // Sky radiance of every pixel of a frame, the pixel's own view ray from the
@@ -611,6 +671,11 @@ cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L,
                                        const ShadeParams* shade, const ShadeImages* shade_images) {
   cudaError_t e = cudaMemsetAsync(Q.count, 0, 2 * sizeof(uint32_t), s);
   if (e != cudaSuccess) return e;
+  const int tiles_y = (L.height + (1 << Q.tile_shift) - 1) >> Q.tile_shift;
+  if (Q.lm != nullptr) {
+    e = cudaMemsetAsync(Q.tiles, 0, sizeof(float) * 4 * size_t(Q.tiles_x) * tiles_y, s);
+    if (e != cudaSuccess) return e;
+  }
   const int smem = int(surrogate_smem_bytes(nets));
   const dim3 grid((L.width + 15) / 16, (L.height + 15) / 16);
   const ShadeParams S = shade ? *shade : ShadeParams{};
@@ -634,6 +699,10 @@ cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L,
     k_surrogate_fallback<false><<<2 * sm_count, 256, 0, s>>>(P, L, A, scene, space, pos, tlut, mslut, Q, hdr,
                                                              counter, S, I);
   }
+  e = cudaGetLastError();
+  if (e != cudaSuccess || Q.lm == nullptr) return e;
+  const size_t pixels = size_t(L.width) * L.height;
+  k_surrogate_calibrate<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(L, Q, hdr);
   return cudaGetLastError();
 }
 

@@ -173,7 +173,7 @@ class AtmSurrogate(ctypes.Structure):
         ("tc_wait_polls", ctypes.c_int32),
         ("stats", ctypes.c_void_p),
         ("gate_terminator", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("calibration_tile", ctypes.c_int32),
     ]
 
 

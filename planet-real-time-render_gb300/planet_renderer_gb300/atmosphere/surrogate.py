@@ -345,6 +345,12 @@ class Surrogate:
     # gate -> plain path: a surface segment crossing the terminator (its sun
     # cosine changes sign between its start, middle and end)
     gate_terminator = False
+    # calibration from the checked pixels: the side of the tiles (pixels, a
+    # power of two in 16..256; 0 = off) whose checked pixels' mean log ratio
+    # of plain to network in-scattering rescales the tile's other MLP pixels
+    # (measured over the 64-frame 4K sweep: frame error mean 0.45% -> 0.18%,
+    # worst 1.46% -> 0.43% at 64 px, nearly flat from 32 to 128)
+    calibration_tile = 64
 
     def native(self, check_fraction: float = 0.01, seed: int = 0, stats=None,
                camera_altitude_m: float | None = None) -> _native.AtmSurrogate:
@@ -366,6 +372,7 @@ class Surrogate:
         s.seed = int(seed) & 0xFFFFFFFF
         s.tc_wait_polls = int(self.tc_wait_polls)
         s.gate_terminator = 1 if self.gate_terminator else 0
+        s.calibration_tile = int(self.calibration_tile)
         s.stats = stats
         return s
 

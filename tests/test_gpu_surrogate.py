@@ -333,33 +333,79 @@ def test_surrogate_frame_against_fp64(trained, altitude, zenith):
     (The bench states the error of the fully trained networks.)"""
 
     sg, _, _ = trained
-    r, gb, args, v = _frame(320, 180, altitude, zenith, 30.0)
+    r, gb, args, v = _frame(640, 360, altitude, zenith, 30.0)
     plain = _plain(r, gb, args).cpu().numpy()
-    got, _ = _surrogate(r, gb, args, sg)
-    got = got.cpu().numpy()
-    sid = gb["surface_id"].cpu().numpy()
-    rng = np.random.default_rng(1)
-    xs, ys = np.nonzero(sid >= 0)
-    pick = rng.choice(len(xs), size=min(400, len(xs)), replace=False)
-    pixels = np.stack([xs[pick], ys[pick]], 1)
+    sg.calibration_tile = 0
+    raw, _ = _surrogate(r, gb, args, sg, check_fraction=0.01)
+    sg.calibration_tile = 64
+    got, _ = _surrogate(r, gb, args, sg, check_fraction=0.01)
+    raw, got = raw.cpu().numpy(), got.cpu().numpy()
+    pixels = _surface_pixels(gb, 400)
     ref = _fp64_pixels(r, gb, args, v, pixels)
     floor = 1e-4 * np.abs(ref).max()
     e_mlp = _rel(got[pixels[:, 0], pixels[:, 1]], ref, floor)
+    e_raw = _rel(raw[pixels[:, 0], pixels[:, 1]], ref, floor)
     e_plain = _rel(plain[pixels[:, 0], pixels[:, 1]], ref, floor)
+    print(f"{altitude} m: plain {np.mean(e_plain):.2e} raw {np.mean(e_raw):.4f} calibrated {np.mean(e_mlp):.4f}")
     assert np.median(e_plain) < 1e-3
-    # the reduced test budget: the bench states the fully trained networks' error
-    assert np.mean(e_mlp) < 0.1, (np.mean(e_mlp), np.quantile(e_mlp, 0.99))
+    # the reduced test budget (60 epochs); the bench states the fully trained
+    # networks' error over the 64-frame sweep against the 1e-2 target
+    assert np.mean(e_mlp) <= np.mean(e_raw) * 1.05
+    assert np.mean(e_mlp) < 0.05, (np.mean(e_mlp), np.quantile(e_mlp, 0.99))
+    r.close()
+
+
+def _surface_pixels(gb, n, seed=1):
+    sid = gb["surface_id"].cpu().numpy()
+    xs, ys = np.nonzero(sid >= 0)
+    pick = np.random.default_rng(seed).choice(len(xs), size=min(n, len(xs)), replace=False)
+    return np.stack([xs[pick], ys[pick]], 1)
+
+
+def test_calibration_corrects_a_biased_network(trained):
+    """A planted bias: the aerial network's log-radiance outputs shifted by
+    ln 1.2 (in-scattering about 20% high).  The calibration from the 1%
+    checked pixels (64-pixel tiles) must take most of it out: against FP64
+    at sampled surface pixels its mean error is below a third of the
+    uncalibrated one; sky pixels are not touched."""
+
+    from planet_renderer_gb300.atmosphere.mlp import Mlp
+    from planet_renderer_gb300.atmosphere.surrogate import Surrogate
+
+    sg_full, _, _ = trained
+    biased = Mlp(11, 4, 6, device=sg_full.aerial.device)
+    p = sg_full.aerial.params()
+    p[-6:-3] += math.log(1.2)
+    biased.set_params(p)
+    sg = Surrogate(biased, None, sg_full.planet_radius_m, sg_full.top_altitude_m, sg_full.scale_height_range)
+    r, gb, args, v = _frame(640, 360, 2000.0, 40.0, 30.0)
+    sg.calibration_tile = 0
+    raw, _ = _surrogate(r, gb, args, sg, check_fraction=0.01)
+    sg.calibration_tile = 64
+    cal, stats = _surrogate(r, gb, args, sg, check_fraction=0.01)
+    raw, cal = raw.cpu().numpy(), cal.cpu().numpy()
+    sky = gb["surface_id"].cpu().numpy() < 0
+    np.testing.assert_array_equal(cal[sky], raw[sky])
+    pixels = _surface_pixels(gb, 400)
+    ref = _fp64_pixels(r, gb, args, v, pixels)
+    floor = 1e-4 * np.abs(ref).max()
+    e_raw = _rel(raw[pixels[:, 0], pixels[:, 1]], ref, floor).mean()
+    e_cal = _rel(cal[pixels[:, 0], pixels[:, 1]], ref, floor).mean()
+    print(f"planted 20% bias: raw {e_raw:.4f} calibrated {e_cal:.4f}")
+    assert e_raw > 0.05
+    assert e_cal < e_raw / 3.0, (e_raw, e_cal)
     r.close()
 
 
 def test_surrogate_frame_gains_over_the_plain_integrator(trained):
     """What the network gains over the method without it (the plain limb
     integrator of every surface pixel): the surrogate composite of a
-    1920x1080 frame from 2 km is at least twice as fast, with its error
-    against FP64 stated by test_surrogate_frame_against_fp64."""
+    3840x2160 frame from 2 km, with its 1% checks and the calibration pass,
+    is at least three times as fast (the target), with its error against
+    FP64 stated by test_surrogate_frame_against_fp64."""
 
     sg, _, _ = trained
-    r, gb, args, _ = _frame(1920, 1080, 2000.0, 40.0, 30.0)
+    r, gb, args, _ = _frame(3840, 2160, 2000.0, 40.0, 30.0)
     hdr = torch.zeros_like(gb["scene_hdr"])
 
     def timed(fn, reps=5):
@@ -378,7 +424,8 @@ def test_surrogate_frame_gains_over_the_plain_integrator(trained):
                                       *args))
     mlp = timed(lambda: r.composite_surrogate(gb["scene_hdr"], gb["space_hdr"], gb["surface_id"], gb["position_view"],
                                               hdr, *args, surrogate=sg, check_fraction=0.01, seed=1))
-    assert plain / mlp > 2.0, (plain, mlp)
+    print(f"4K composite: plain {plain:.3f} ms, surrogate {mlp:.3f} ms, {plain / mlp:.2f}x")
+    assert plain / mlp > 3.0, (plain, mlp)
     r.close()
 
 
