@@ -638,7 +638,17 @@ ATM_API int atm_batch_build(AtmBatch* b, const AtmBatchJob* jobs, int32_t n_jobs
   b->h_jobs.assign(size_t(n_jobs) * jsz, 0);
   b->h_prefix.assign(size_t(n_jobs) + 1, 0);
   float4* base = static_cast<float4*>(arena);
-  for (int i = 0; i < n_jobs; ++i) {
+  // Processing order: the sky-view jobs, then the aerial volumes (each job
+  // writes only its own output range, so the order changes no result).
+  // Neighbouring work tickets then run the same LUT kind's warp functions,
+  // which keeps the persistent kernel's hot code in the instruction cache.
+  std::vector<int> order(static_cast<size_t>(n_jobs));
+  for (int i = 0; i < n_jobs; ++i) order[size_t(i)] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) {
+    return (jobs[a].kind == ATM_LUT_AERIAL) < (jobs[c].kind == ATM_LUT_AERIAL);
+  });
+  for (int slot = 0; slot < n_jobs; ++slot) {
+    const int i = order[size_t(slot)];
     const AtmBatchJob& j = jobs[i];
     if (j.param_set < 0 || j.param_set >= int(b->params.size()))
       return fail(ATM_E_INVALID, "job %d: parameter set %d out of range", i, j.param_set);
@@ -669,9 +679,9 @@ ATM_API int atm_batch_build(AtmBatch* b, const AtmBatchJob* jobs, int32_t n_jobs
     if (!std::isfinite(j.camera_altitude_m) || !std::isfinite(j.sun_zenith_cosine))
       return fail(ATM_E_INVALID, "job %d: non-finite camera or sun", i);
     const int p = j.param_set;
-    atm::fill_batch_job(*reinterpret_cast<atm::BatchJobDev*>(b->h_jobs.data() + size_t(i) * jsz), b->dev[p], j,
+    atm::fill_batch_job(*reinterpret_cast<atm::BatchJobDev*>(b->h_jobs.data() + size_t(slot) * jsz), b->dev[p], j,
                         base, b->tlut[p], b->mslut[p], b->radius[p], b->E, b->ar_rad, per);
-    b->h_prefix[i + 1] = b->h_prefix[i] + (units + per - 1) / per;
+    b->h_prefix[slot + 1] = b->h_prefix[slot] + (units + per - 1) / per;
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (b->jobs_bytes < b->h_jobs.size()) {

@@ -133,6 +133,6 @@ def test_ocean_surface_disabled_writes_nothing_and_rejects_bad_input():
         r.rasterize_gbuffer(g, a["planet_radius_m"], 10.0, a["planet_frame"], a["view_basis"], 0.5, 0.0, 0)
     r.close()
     r = OceanRenderer(W, H, OceanConfig())
-    with pytest.raises(RuntimeError):
+    with pytest.raises(ValueError):
         r.rasterize_gbuffer(g, -1.0, 10.0, a["planet_frame"], a["view_basis"], 0.5, 0.0, 0)
     r.close()

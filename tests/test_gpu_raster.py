@@ -181,9 +181,9 @@ def test_raster_rejects_bad_arguments():
     mesh = _mesh_tensors(view, normal, material, height, cell, tris, [0, 1], skirt, None, surface, 2)
     r = TerrainRaster(32, 16, 2, len(tris))
     g = r.allocate_gbuffer()
-    with pytest.raises(RuntimeError):
+    with pytest.raises(ValueError):
         r.render(mesh, 0.5, 0.6, g, view_mode=2)  # mode 2 without slot levels
-    with pytest.raises(RuntimeError):
+    with pytest.raises(ValueError):
         r.render(mesh, -1.0, 0.6, g)
     with pytest.raises(ValueError):
         r.render(mesh, 0.5, 0.6, {k: v for k, v in g.items() if k != "albedo"})
