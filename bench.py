@@ -499,7 +499,9 @@ def main() -> None:
     post = None if args.no_post else _postprocess_4k(device, args)
     shade = None if args.no_post else _shading_4k(device, args)
     raster = None if args.no_raster else _raster_4k(device, args)
-    mesh_frame = None if args.no_raster else _frame_from_mesh_4k(device, args)
+    mesh_frame = (frame_4k or {}).pop("mesh_4k", None)
+    if mesh_frame is None and not args.no_raster:
+        mesh_frame = _frame_from_mesh_4k(device, args)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -797,7 +799,7 @@ def _raster_4k(device, args, steps=20) -> dict:
     return out
 
 
-def _frame_from_mesh_4k(device, args, steps=10) -> dict:
+def _frame_from_mesh_4k(device, args, sg=None, steps=10) -> dict:
     """A whole 3840x2160 frame from terrain patches to the display image, in
     the reference renderer's order (renderer.py:1626-1735): terrain raster
     with the snapshot -> ocean coverage -> atmosphere update -> fused surface
@@ -805,7 +807,9 @@ def _frame_from_mesh_4k(device, args, steps=10) -> dict:
     camera 30 m above sea level looks 6 degrees down over the synthetic
     coast (the default patch budget, 256 patches of 12 cells; 200 m relief
     rising inland, its valleys below sea level are sea), sun 35 degrees up.  One CUDA graph per frame;
-    device ms per frame and per stage."""
+    device ms per frame and per stage.  With ``sg`` the atmosphere stage also
+    runs with the surrogate composite, and its frame's error against the
+    plain frame is stated."""
 
     import numpy as np
     import torch
@@ -846,10 +850,27 @@ def _frame_from_mesh_4k(device, args, steps=10) -> dict:
         "post": lambda: post.process(hdr, display, 0.0, bloom=True, tone_map=True),
     }
     whole = lambda: [fn() for fn in stages.values()]
+    timed = list(stages.items()) + [("frame", whole)]
+    if sg is not None:
+        stages_mlp = dict(stages, atmosphere=lambda: (
+            atm.update(R, R + alt, sun, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG),
+            atm.render_frame(g, space_hdr, hdr, *args_atm, surrogate=sg, check_fraction=MLP_CHECK_FRACTION,
+                             seed=SEED)))
+        timed += [("atmosphere_mlp", stages_mlp["atmosphere"]),
+                  ("frame_mlp", lambda: [fn() for fn in stages_mlp.values()])]
     out = {"workload": "3840x2160 frame from terrain patches to display: raster + snapshot, ocean coverage, "
                        "atmosphere update, fused lighting + shading + composite, bloom + tone map; ground camera "
                        "30 m above sea level, 256 patches x 12 cells, default ocean; CUDA graphs"}
-    for name, fn in list(stages.items()) + [("frame", whole)]:
+    if sg is not None:
+        whole()
+        plain_hdr = hdr.clone()
+        [fn() for fn in stages_mlp.values()]
+        surface = (g["surface_id"] >= 0)
+        ref = plain_hdr[surface].double()
+        floor = 1e-4 * float(ref.abs().max())
+        rel = ((hdr[surface].double() - ref).abs() / ref.abs().clamp_min(floor)).max(dim=-1).values
+        out["mlp_err_vs_plain"] = {"mean": float(rel.mean()), "p99": float(torch.quantile(rel.float()[::97], 0.99))}
+    for name, fn in timed:
         graphs = _capture_fn([()], device, fn)
         for _ in range(3):
             graphs[0].replay()
@@ -1080,6 +1101,8 @@ def _frame_4k(device, args) -> dict:
     torch.cuda.empty_cache()
     out["sky_4k"] = _sky_4k(device, args, trained)
     out["fused_4k"] = _frame_fused_4k(device, args, sg)
+    if not args.no_raster:
+        out["mesh_4k"] = _frame_from_mesh_4k(device, args, sg)
     return out
 
 

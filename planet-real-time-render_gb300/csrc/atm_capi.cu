@@ -1472,7 +1472,9 @@ struct AtmRaster {
   int32_t width = 0, height = 0, max_patches = 0, triangles_per_patch = 0;
   atm::RasterTri* tris = nullptr;
   long long capacity = 0;
-  uint32_t* count = nullptr;
+  uint32_t* count = nullptr;  // emitted, large, spare
+  uint32_t* large = nullptr;
+  unsigned long long* tile_prefix = nullptr;
   unsigned long long* depth_key = nullptr;
   int sm_count = 0;
 };
@@ -1495,7 +1497,9 @@ ATM_API int atm_raster_create(int32_t width, int32_t height, int32_t max_patches
   r->triangles_per_patch = triangles_per_patch;
   r->capacity = capacity;
   cudaError_t e = cudaMalloc(&r->tris, sizeof(atm::RasterTri) * size_t(capacity));
-  if (e == cudaSuccess) e = cudaMalloc(&r->count, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&r->count, 4 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&r->large, sizeof(uint32_t) * size_t(capacity));
+  if (e == cudaSuccess) e = cudaMalloc(&r->tile_prefix, sizeof(unsigned long long) * (size_t(capacity) + 1));
   if (e == cudaSuccess) e = cudaMalloc(&r->depth_key, sizeof(unsigned long long) * size_t(width) * height);
   int dev = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
@@ -1512,6 +1516,8 @@ ATM_API int atm_raster_destroy(AtmRaster* r) {
   if (!r) return ATM_OK;
   if (r->tris) cudaFree(r->tris);
   if (r->count) cudaFree(r->count);
+  if (r->large) cudaFree(r->large);
+  if (r->tile_prefix) cudaFree(r->tile_prefix);
   if (r->depth_key) cudaFree(r->depth_key);
   delete r;
   return ATM_OK;
@@ -1551,7 +1557,7 @@ ATM_API int atm_raster_terrain(AtmRaster* r, const AtmRasterMesh* m, double near
                        m->cell,       m->triangles,  m->active_slots, m->skirt_mask,
                        m->slot_level, m->patches,    m->vertices_per_patch, m->triangles_per_patch,
                        m->surface_triangles_per_patch, m->resolution, m->n_active};
-  atm::RasterStream S{r->tris, r->count, r->capacity};
+  atm::RasterStream S{r->tris, r->count, r->capacity, r->large, r->tile_prefix};
   if (o->terrain_surface_id && (!o->terrain_position || !o->terrain_normal || !o->terrain_albedo))
     return fail(ATM_E_INVALID, "the terrain snapshot needs position, normal and albedo images");
   atm::RasterOutDev O{o->depth,          o->position,        o->normal,           o->albedo,

@@ -260,8 +260,11 @@ struct RasterTri {
 };
 struct RasterStream {
   RasterTri* tris;
-  uint32_t* count;  // triangles emitted (may exceed capacity: only capacity are stored)
+  uint32_t* count;  // [0] triangles emitted (may exceed capacity: only capacity are stored),
+                    // [1] large triangles listed, [2] spare
   long long capacity;
+  uint32_t* large;                 // capacity: the emitted triangles too large for one warp
+  unsigned long long* tile_prefix; // capacity + 1: exclusive prefix of their pixel-tile counts
 };
 struct RasterMeshDev {
   const float* view;       // [patches][vertices][3]

@@ -9,9 +9,11 @@
 //    plane and the four frustum sides, and the emission (an atomic append)
 //    of each resulting triangle with its screen setup: projection snapped to
 //    1/256 pixel, edge equations, top-left flags, inverse area;
-//  * k_raster_depth: warp per emitted triangle, lanes over the pixels of its
-//    bounding box: coverage by the edge equations with the top-left rule and
-//    a 64-bit atomic minimum of (depth bits << 32 | triangle) per pixel;
+//  * k_raster_depth (+ k_raster_tile_prefix, k_raster_depth_tiles): coverage
+//    by the edge equations with the top-left rule and a 64-bit atomic
+//    minimum of (depth bits << 32 | triangle) per pixel; small triangles by
+//    one thread, medium ones by a warp, large ones cut into 8 x 32 pixel
+//    tiles spread over the whole grid;
 //  * k_raster_resolve: thread per pixel: the winning triangle's
 //    perspective-correct position, normal, material weights and height, the
 //    dominant vertex's cell id and the albedo of the view mode.
@@ -208,35 +210,141 @@ __device__ __forceinline__ bool inside_edges(const RasterTri& T, r3 e) {
          (e.z > 0.0f || (e.z == 0.0f && (T.tl & 4)));
 }
 
-// _raster_depth_direct :1158-1206.  A warp per triangle (grid-stride over
-// the emitted stream); lanes over the bounding box's pixels.
+// _raster_depth_direct :1158-1206, in three sizes of work.  Each covered
+// pixel centre (edge equations with the top-left rule) takes the atomic
+// minimum of (depth bits << 32 | triangle); the order of the atomics changes
+// no result.  Pixels are walked along y, the depth keys' contiguous axis.
+__device__ __forceinline__ void depth_pixel(const RasterTri& T, int x, int y, int H,
+                                            unsigned long long* __restrict__ depth_key, unsigned long long q) {
+  const r3 e = edge_values(T, add(float(x), 0.5f), add(float(y), 0.5f));
+  if (!inside_edges(T, e)) return;
+  const r3 l = rscale(e, T.inv_area);
+  const float z = dv(1.0f, fmx(add(add(dv(l.x, T.screen[0][2]), dv(l.y, T.screen[1][2])), dv(l.z, T.screen[2][2])),
+                               1e-20f));
+  atomicMin(depth_key + (size_t(x) * H + y), ((unsigned long long)__float_as_uint(z) << 32) | q);
+}
+struct Box {
+  int x0, x1, y0, y1;
+};
+__device__ __forceinline__ Box bbox(const RasterTri& T, const ImageLayout& L) {
+  const float ax = T.screen[0][0], bx = T.screen[1][0], cx = T.screen[2][0];
+  const float ay = T.screen[0][1], by = T.screen[1][1], cy = T.screen[2][1];
+  return {max(int(floorf(fmn(fmn(ax, bx), cx))), 0), min(int(ceilf(fmx(fmx(ax, bx), cx))), L.width - 1),
+          max(int(floorf(fmn(fmn(ay, by), cy))), 0), min(int(ceilf(fmx(fmx(ay, by), cy))), L.height - 1)};
+}
+constexpr long long kRasterThreadArea = 16;    // bounding boxes up to this many pixels: one thread
+constexpr long long kRasterWarpArea = 4096;    // up to this: one warp; larger: tiles over the whole grid
+constexpr int kRasterTileW = 8, kRasterTileH = 32;  // a large triangle's work item: 8 columns x 32 rows
+
+// Thread per emitted triangle (grid-stride, warp-aligned): small boxes are
+// walked by their own thread, medium ones by the whole warp in turn, large
+// ones are listed for k_raster_depth_tiles.
 __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayout L,
                                                       unsigned long long* __restrict__ depth_key) {
   const int lane = threadIdx.x & 31;
-  const long long warps = (long long)gridDim.x * (blockDim.x >> 5);
-  const long long n = min((long long)*S.count, (long long)S.capacity);
-  for (long long q = blockIdx.x * (long long)(blockDim.x >> 5) + (threadIdx.x >> 5); q < n; q += warps) {
-    const RasterTri& T = S.tris[q];
-    if (!(T.inv_area > 0.0f)) continue;
-    const float ax = T.screen[0][0], bx = T.screen[1][0], cx = T.screen[2][0];
-    const float ay = T.screen[0][1], by = T.screen[1][1], cy = T.screen[2][1];
-    const int x0 = max(int(floorf(fmn(fmn(ax, bx), cx))), 0);
-    const int x1 = min(int(ceilf(fmx(fmx(ax, bx), cx))), L.width - 1);
-    const int y0 = max(int(floorf(fmn(fmn(ay, by), cy))), 0);
-    const int y1 = min(int(ceilf(fmx(fmx(ay, by), cy))), L.height - 1);
-    if (x0 > x1 || y0 > y1) continue;
-    const int bw = x1 - x0 + 1;
-    const long long area = (long long)bw * (y1 - y0 + 1);
-    const float az = T.screen[0][2], bz = T.screen[1][2], cz = T.screen[2][2];
-    for (long long k = lane; k < area; k += 32) {
-      const int x = x0 + int(k % bw), y = y0 + int(k / bw);
-      const r3 e = edge_values(T, add(float(x), 0.5f), add(float(y), 0.5f));
-      if (!inside_edges(T, e)) continue;
-      const r3 l = rscale(e, T.inv_area);
-      const float z = dv(1.0f, fmx(add(add(dv(l.x, az), dv(l.y, bz)), dv(l.z, cz)), 1e-20f));
-      const unsigned long long key = ((unsigned long long)__float_as_uint(z) << 32) | (unsigned long long)q;
-      atomicMin(depth_key + (size_t(x) * L.height + y), key);
+  const long long n = min((long long)S.count[0], (long long)S.capacity);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long base = blockIdx.x * (long long)blockDim.x + (threadIdx.x & ~31); base < n; base += stride) {
+    const long long q = base + lane;
+    bool medium = false;
+    if (q < n) {
+      const RasterTri& T = S.tris[q];
+      const Box b = bbox(T, L);
+      if (T.inv_area > 0.0f && b.x0 <= b.x1 && b.y0 <= b.y1) {
+        const long long area = (long long)(b.x1 - b.x0 + 1) * (b.y1 - b.y0 + 1);
+        if (area <= kRasterThreadArea) {
+          for (int x = b.x0; x <= b.x1; ++x)
+            for (int y = b.y0; y <= b.y1; ++y) depth_pixel(T, x, y, L.height, depth_key, (unsigned long long)q);
+        } else if (area <= kRasterWarpArea) {
+          medium = true;
+        } else {
+          S.large[atomicAdd(S.count + 1, 1u)] = uint32_t(q);  // at most one entry per stored triangle
+        }
+      }
     }
+    unsigned m = __ballot_sync(0xffffffffu, medium);
+    while (m) {
+      const int leader = __ffs(m) - 1;
+      m &= m - 1;
+      const long long ql = base + leader;
+      const RasterTri& T = S.tris[ql];
+      const Box b = bbox(T, L);
+      const int bh = b.y1 - b.y0 + 1;
+      const long long area = (long long)(b.x1 - b.x0 + 1) * bh;
+      for (long long k = lane; k < area; k += 32)
+        depth_pixel(T, b.x0 + int(k / bh), b.y0 + int(k % bh), L.height, depth_key, (unsigned long long)ql);
+    }
+  }
+}
+
+// One block: the exclusive prefix of the large triangles' tile counts
+// (64-bit), in chunks of the block size.
+__global__ void __launch_bounds__(1024) k_raster_tile_prefix(RasterStream S, ImageLayout L) {
+  __shared__ unsigned long long part[32];
+  __shared__ unsigned long long carry;
+  const uint32_t n = S.count[1];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (uint32_t base = 0; base < n; base += blockDim.x) {
+    const uint32_t k = base + threadIdx.x;
+    unsigned long long tiles = 0;
+    if (k < n) {
+      const Box b = bbox(S.tris[S.large[k]], L);
+      tiles = (unsigned long long)((b.x1 - b.x0 + kRasterTileW) / kRasterTileW) *
+              ((b.y1 - b.y0 + kRasterTileH) / kRasterTileH);
+    }
+    unsigned long long v = tiles;  // inclusive warp scan
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned long long t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    if (lane == 31) part[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned long long w = lane < int(blockDim.x >> 5) ? part[lane] : 0;
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      part[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    const unsigned long long before = carry + (warp > 0 ? part[warp - 1] : 0) + v - tiles;
+    if (k < n) S.tile_prefix[k] = before;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = before + tiles;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) S.tile_prefix[n] = carry;
+}
+
+// Warp per 8 x 32 pixel tile of a large triangle, over the whole grid: the
+// tile's triangle by binary search of the prefix; lane = row, 8 columns.
+__global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, ImageLayout L,
+                                                            unsigned long long* __restrict__ depth_key) {
+  const uint32_t n = S.count[1];
+  if (n == 0) return;
+  const unsigned long long total = S.tile_prefix[n];
+  const int lane = threadIdx.x & 31;
+  const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+  for (unsigned long long w = blockIdx.x * (unsigned long long)(blockDim.x >> 5) + (threadIdx.x >> 5); w < total;
+       w += warps) {
+    uint32_t lo = 0, hi = n - 1;  // last k with prefix[k] <= w
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi + 1) >> 1;
+      if (S.tile_prefix[mid] <= w) lo = mid; else hi = mid - 1;
+    }
+    const uint32_t q = S.large[lo];
+    const RasterTri& T = S.tris[q];
+    const Box b = bbox(T, L);
+    const unsigned long long t = w - S.tile_prefix[lo];
+    const int rows = (b.y1 - b.y0 + kRasterTileH) / kRasterTileH;
+    const int tx = int(t / rows), ty = int(t % rows);
+    const int y = b.y0 + ty * kRasterTileH + lane;
+    if (y > b.y1) continue;
+    const int xs = b.x0 + tx * kRasterTileW, xe = min(xs + kRasterTileW - 1, b.x1);
+    for (int x = xs; x <= xe; ++x) depth_pixel(T, x, y, L.height, depth_key, (unsigned long long)q);
   }
 }
 
@@ -344,7 +452,7 @@ __global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLay
 
 __global__ void k_raster_clear(unsigned long long* __restrict__ depth_key, long long n, uint32_t* count) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i == 0) *count = 0u;
+  if (i < 3) count[i] = 0u;
   if (i < n) depth_key[i] = kSentinel;
 }
 
@@ -364,6 +472,12 @@ cudaError_t launch_raster(const RasterMeshDev& M, const RasterStream& S, const I
     if (e != cudaSuccess) return e;
   }
   k_raster_depth<<<unsigned(sm_count * 8), 256, 0, s>>>(S, L, depth_key);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_raster_tile_prefix<<<1, 1024, 0, s>>>(S, L);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_raster_depth_tiles<<<unsigned(sm_count * 8), 256, 0, s>>>(S, L, depth_key);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_raster_resolve<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(S, L, depth_key, O, mode, M.triangles_per_patch,
