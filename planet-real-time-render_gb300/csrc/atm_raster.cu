@@ -232,8 +232,8 @@ __device__ __forceinline__ Box bbox(const RasterTri& T, const ImageLayout& L) {
   return {max(int(floorf(fmn(fmn(ax, bx), cx))), 0), min(int(ceilf(fmx(fmx(ax, bx), cx))), L.width - 1),
           max(int(floorf(fmn(fmn(ay, by), cy))), 0), min(int(ceilf(fmx(fmx(ay, by), cy))), L.height - 1)};
 }
-constexpr long long kRasterThreadArea = 16;    // bounding boxes up to this many pixels: one thread
-constexpr long long kRasterWarpArea = 4096;    // up to this: one warp; larger: tiles over the whole grid
+constexpr long long kRasterThreadArea = 16;  // bounding boxes up to this many pixels: one thread
+constexpr long long kRasterWarpArea = 256;   // up to this: one warp; larger: tiles over the whole grid
 constexpr int kRasterTileW = 8, kRasterTileH = 32;  // a large triangle's work item: 8 columns x 32 rows
 
 // Thread per emitted triangle (grid-stride, warp-aligned): small boxes are
@@ -319,8 +319,25 @@ __global__ void __launch_bounds__(1024) k_raster_tile_prefix(RasterStream S, Ima
   if (threadIdx.x == 0) S.tile_prefix[n] = carry;
 }
 
-// Warp per 8 x 32 pixel tile of a large triangle, over the whole grid: the
-// tile's triangle by binary search of the prefix; lane = row, 8 columns.
+// Whether the edge equations reject a whole tile of pixel centres: an edge
+// whose value is negative at the tile's corner where it is largest.  The
+// float32 edge value is monotone in x (y) for a non-negative x (y)
+// coefficient, so that corner is the tile's largest value as the pixel test
+// evaluates it: a rejected tile holds no covered pixel.
+__device__ __forceinline__ bool tile_outside(const RasterTri& T, int xs, int xe, int ys, int ye) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float px = add(float(T.eq[k][0] >= 0.0f ? xe : xs), 0.5f);
+    const float py = add(float(T.eq[k][1] >= 0.0f ? ye : ys), 0.5f);
+    if (add(add(mul(T.eq[k][0], px), mul(T.eq[k][1], py)), T.eq[k][2]) < 0.0f) return true;
+  }
+  return false;
+}
+
+// The large triangles' 8 x 32 pixel tiles, split evenly over the grid's
+// warps in contiguous runs (a run mostly stays within one triangle, found
+// once by binary search of the prefix); lane = row, 8 columns; tiles the
+// edge equations reject are skipped.
 __global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, ImageLayout L,
                                                             unsigned long long* __restrict__ depth_key) {
   const uint32_t n = S.count[1];
@@ -328,22 +345,33 @@ __global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, Imag
   const unsigned long long total = S.tile_prefix[n];
   const int lane = threadIdx.x & 31;
   const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-  for (unsigned long long w = blockIdx.x * (unsigned long long)(blockDim.x >> 5) + (threadIdx.x >> 5); w < total;
-       w += warps) {
-    uint32_t lo = 0, hi = n - 1;  // last k with prefix[k] <= w
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi + 1) >> 1;
-      if (S.tile_prefix[mid] <= w) lo = mid; else hi = mid - 1;
+  const unsigned long long warp = blockIdx.x * (unsigned long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
+  const unsigned long long per = (total + warps - 1) / warps;
+  const unsigned long long w0 = warp * per, w1 = min(w0 + per, total);
+  if (w0 >= w1) return;
+  uint32_t k = 0, hi = n - 1;  // last k with prefix[k] <= w0
+  while (k < hi) {
+    const uint32_t mid = (k + hi + 1) >> 1;
+    if (S.tile_prefix[mid] <= w0) k = mid; else hi = mid - 1;
+  }
+  unsigned long long first = S.tile_prefix[k], next = S.tile_prefix[k + 1];
+  for (unsigned long long w = w0; w < w1; ++w) {
+    while (w >= next) {
+      ++k;
+      first = next;
+      next = S.tile_prefix[k + 1];
     }
-    const uint32_t q = S.large[lo];
+    const uint32_t q = S.large[k];
     const RasterTri& T = S.tris[q];
     const Box b = bbox(T, L);
-    const unsigned long long t = w - S.tile_prefix[lo];
     const int rows = (b.y1 - b.y0 + kRasterTileH) / kRasterTileH;
+    const unsigned long long t = w - first;
     const int tx = int(t / rows), ty = int(t % rows);
-    const int y = b.y0 + ty * kRasterTileH + lane;
-    if (y > b.y1) continue;
     const int xs = b.x0 + tx * kRasterTileW, xe = min(xs + kRasterTileW - 1, b.x1);
+    const int ys = b.y0 + ty * kRasterTileH, ye = min(ys + kRasterTileH - 1, b.y1);
+    if (tile_outside(T, xs, xe, ys, ye)) continue;
+    const int y = ys + lane;
+    if (y > ye) continue;
     for (int x = xs; x <= xe; ++x) depth_pixel(T, x, y, L.height, depth_key, (unsigned long long)q);
   }
 }

@@ -197,7 +197,9 @@ class OceanRenderer:
         self.width, self.height = int(width), int(height)
         self.config = config
         self.layout = layout
-        self.device = torch.device(device if device is not None else f"cuda:{torch.cuda.current_device()}")
+        self.device = torch.device(device if device is not None else "cuda")
+        if self.device.type == "cuda" and self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
         scale = config.wave_height_scale * config.wind_amplitude_scale()
         self.max_geometry_displacement_m = sum(_HEIGHTS_M[:config.geometry_cascades]) * scale
         self._lib = _native.library()

@@ -168,6 +168,8 @@ class TerrainRaster:
         self.max_patches, self.triangles_per_patch = int(max_patches), int(triangles_per_patch)
         self.layout = layout
         self.device = torch.device(device)
+        if self.device.type == "cuda" and self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
         self._lib = _native.library()
         h = ctypes.c_void_p()
         with torch.cuda.device(self.device):
