@@ -252,6 +252,9 @@ def raster(tris: Triangles, width, height, local_triangle_count, mode=0, slot_le
     """_raster_depth_direct then _resolve_raster; returns the G-buffer."""
 
     key = np.full((width, height), SENTINEL, dtype=object)
+    # every triangle covering a pixel, by depth bits: the exact-depth ties,
+    # where the winner is the atomic order's (the lowest stream index here)
+    cover = {}
     for q, t in enumerate(tris.rows):
         if t is None or not t["inv_area"] > 0.0:
             continue
@@ -269,10 +272,12 @@ def raster(tris: Triangles, width, height, local_triangle_count, mode=0, slot_le
                 z = F(1.0) / max(l[0] / a[2] + l[1] / b[2] + l[2] / c[2], F(1e-20))
                 k = (int(np.array(z, F).view(np.uint32)) << 32) | q
                 key[x, y] = min(key[x, y], k)
+                cover.setdefault((x, y), []).append(k)
     g = {"depth": np.zeros((width, height), F), "position": np.zeros((width, height, 3), F),
          "normal": np.zeros((width, height, 3), F), "albedo": np.zeros((width, height, 3), F),
          "material": np.zeros((width, height, 4), F), "height_m": np.zeros((width, height), F),
-         "surface_id": np.full((width, height), -1, np.int32), "cell_id": np.full((width, height), -1, np.int32)}
+         "surface_id": np.full((width, height), -1, np.int32), "cell_id": np.full((width, height), -1, np.int32),
+         "ties": {}}
     for x in range(width):
         for y in range(height):
             k = key[x, y]
@@ -280,6 +285,9 @@ def raster(tris: Triangles, width, height, local_triangle_count, mode=0, slot_le
                 continue
             q = k & 0xFFFFFFFF
             z = np.array(k >> 32, np.uint32).view(F)[()]
+            tied = [c & 0xFFFFFFFF for c in cover[(x, y)] if c >> 32 == k >> 32]
+            if len(tied) > 1:
+                g["ties"][(x, y)] = sorted({int(tris.rows[c]["src"]) for c in tied})
             t = tris.rows[q]
             a, b, c = t["screen"]
             l = _edges(t, x, y) * t["inv_area"]
