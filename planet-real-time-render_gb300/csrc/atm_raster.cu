@@ -236,11 +236,81 @@ constexpr long long kRasterThreadArea = 16;  // bounding boxes up to this many p
 constexpr long long kRasterWarpArea = 256;   // up to this: one warp; larger: tiles over the whole grid
 constexpr int kRasterTileW = 8, kRasterTileH = 32;  // a large triangle's work item: 8 columns x 32 rows
 
+// Whether the edge equations reject a whole tile of pixel centres: an edge
+// whose value is negative at the tile's corner where it is largest.  The
+// float32 edge value is monotone in x (y) for a non-negative x (y)
+// coefficient, so that corner is the tile's largest value as the pixel test
+// evaluates it: a rejected tile holds no covered pixel.
+__device__ __forceinline__ bool tile_outside(const RasterTri& T, int xs, int xe, int ys, int ye) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float px = add(float(T.eq[k][0] >= 0.0f ? xe : xs), 0.5f);
+    const float py = add(float(T.eq[k][1] >= 0.0f ? ye : ys), 0.5f);
+    if (add(add(mul(T.eq[k][0], px), mul(T.eq[k][1], py)), T.eq[k][2]) < 0.0f) return true;
+  }
+  return false;
+}
+
+// One warp over a tile of at most 8 columns x 32 rows (lane = row): the
+// lanes test their pixels' coverage, the covered pixels are compacted in the
+// warp's shared-memory list, then every lane takes list entries for the
+// depth and the atomic (the costly part runs with all lanes busy however
+// sparse the coverage).
+__device__ __forceinline__ void warp_tile(const RasterTri& T, unsigned long long q, int xs, int xe, int ys, int ye,
+                                          int H, unsigned long long* __restrict__ depth_key, uint8_t* list) {
+  const int lane = threadIdx.x & 31;
+  const int y = ys + lane;
+  unsigned mask = 0;
+  if (y <= ye) {
+    const float py = add(float(y), 0.5f);
+    for (int c = 0; c <= xe - xs; ++c)
+      if (inside_edges(T, edge_values(T, add(float(xs + c), 0.5f), py))) mask |= 1u << c;
+  }
+  const int n = __popc(mask);
+  int off = n;  // inclusive scan of the counts
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, off, o);
+    if (lane >= o) off += t;
+  }
+  const int total = __shfl_sync(0xffffffffu, off, 31);
+  off -= n;
+  while (mask) {
+    const int c = __ffs(mask) - 1;
+    mask &= mask - 1;
+    list[off++] = uint8_t((c << 5) | lane);
+  }
+  __syncwarp();
+  for (int i = lane; i < total; i += 32) {
+    const int c = list[i] >> 5, row = list[i] & 31;
+    const int px = xs + c, py = ys + row;
+    const r3 e = edge_values(T, add(float(px), 0.5f), add(float(py), 0.5f));
+    const r3 l = rscale(e, T.inv_area);
+    const float z = dv(1.0f, fmx(add(add(dv(l.x, T.screen[0][2]), dv(l.y, T.screen[1][2])), dv(l.z, T.screen[2][2])),
+                                 1e-20f));
+    atomicMin(depth_key + (size_t(px) * H + py), ((unsigned long long)__float_as_uint(z) << 32) | q);
+  }
+  __syncwarp();
+}
+
+// A whole box by one warp, in 8 x 32 tiles (each skipped when the edge
+// equations reject it).
+__device__ __forceinline__ void warp_box(const RasterTri& T, unsigned long long q, const Box& b, int H,
+                                         unsigned long long* __restrict__ depth_key, uint8_t* list) {
+  for (int xs = b.x0; xs <= b.x1; xs += kRasterTileW)
+    for (int ys = b.y0; ys <= b.y1; ys += kRasterTileH) {
+      const int xe = min(xs + kRasterTileW - 1, b.x1), ye = min(ys + kRasterTileH - 1, b.y1);
+      if (!tile_outside(T, xs, xe, ys, ye)) warp_tile(T, q, xs, xe, ys, ye, H, depth_key, list);
+    }
+}
+
 // Thread per emitted triangle (grid-stride, warp-aligned): small boxes are
 // walked by their own thread, medium ones by the whole warp in turn, large
 // ones are listed for k_raster_depth_tiles.
 __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayout L,
                                                       unsigned long long* __restrict__ depth_key) {
+  __shared__ uint8_t s_list[8][kRasterTileW * kRasterTileH];
+  uint8_t* list = s_list[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const long long n = min((long long)S.count[0], (long long)S.capacity);
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -268,11 +338,7 @@ __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayou
       m &= m - 1;
       const long long ql = base + leader;
       const RasterTri& T = S.tris[ql];
-      const Box b = bbox(T, L);
-      const int bh = b.y1 - b.y0 + 1;
-      const long long area = (long long)(b.x1 - b.x0 + 1) * bh;
-      for (long long k = lane; k < area; k += 32)
-        depth_pixel(T, b.x0 + int(k / bh), b.y0 + int(k % bh), L.height, depth_key, (unsigned long long)ql);
+      warp_box(T, (unsigned long long)ql, bbox(T, L), L.height, depth_key, list);
     }
   }
 }
@@ -319,31 +385,17 @@ __global__ void __launch_bounds__(1024) k_raster_tile_prefix(RasterStream S, Ima
   if (threadIdx.x == 0) S.tile_prefix[n] = carry;
 }
 
-// Whether the edge equations reject a whole tile of pixel centres: an edge
-// whose value is negative at the tile's corner where it is largest.  The
-// float32 edge value is monotone in x (y) for a non-negative x (y)
-// coefficient, so that corner is the tile's largest value as the pixel test
-// evaluates it: a rejected tile holds no covered pixel.
-__device__ __forceinline__ bool tile_outside(const RasterTri& T, int xs, int xe, int ys, int ye) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float px = add(float(T.eq[k][0] >= 0.0f ? xe : xs), 0.5f);
-    const float py = add(float(T.eq[k][1] >= 0.0f ? ye : ys), 0.5f);
-    if (add(add(mul(T.eq[k][0], px), mul(T.eq[k][1], py)), T.eq[k][2]) < 0.0f) return true;
-  }
-  return false;
-}
-
 // The large triangles' 8 x 32 pixel tiles, split evenly over the grid's
 // warps in contiguous runs (a run mostly stays within one triangle, found
 // once by binary search of the prefix); lane = row, 8 columns; tiles the
 // edge equations reject are skipped.
 __global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, ImageLayout L,
                                                             unsigned long long* __restrict__ depth_key) {
+  __shared__ uint8_t s_list[8][kRasterTileW * kRasterTileH];
+  uint8_t* list = s_list[threadIdx.x >> 5];
   const uint32_t n = S.count[1];
   if (n == 0) return;
   const unsigned long long total = S.tile_prefix[n];
-  const int lane = threadIdx.x & 31;
   const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
   const unsigned long long warp = blockIdx.x * (unsigned long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
   const unsigned long long per = (total + warps - 1) / warps;
@@ -370,9 +422,7 @@ __global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, Imag
     const int xs = b.x0 + tx * kRasterTileW, xe = min(xs + kRasterTileW - 1, b.x1);
     const int ys = b.y0 + ty * kRasterTileH, ye = min(ys + kRasterTileH - 1, b.y1);
     if (tile_outside(T, xs, xe, ys, ye)) continue;
-    const int y = ys + lane;
-    if (y > ye) continue;
-    for (int x = xs; x <= xe; ++x) depth_pixel(T, x, y, L.height, depth_key, (unsigned long long)q);
+    warp_tile(T, q, xs, xe, ys, ye, L.height, depth_key, list);
   }
 }
 
