@@ -1474,7 +1474,9 @@ struct AtmRaster {
   long long capacity = 0;
   uint32_t* count = nullptr;  // emitted, large, spare
   uint32_t* large = nullptr;
+  uint32_t* large_tiles = nullptr;
   unsigned long long* tile_prefix = nullptr;
+  unsigned long long* block_sums = nullptr;
   unsigned long long* depth_key = nullptr;
   int sm_count = 0;
 };
@@ -1499,7 +1501,9 @@ ATM_API int atm_raster_create(int32_t width, int32_t height, int32_t max_patches
   cudaError_t e = cudaMalloc(&r->tris, sizeof(atm::RasterTri) * size_t(capacity));
   if (e == cudaSuccess) e = cudaMalloc(&r->count, 4 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMalloc(&r->large, sizeof(uint32_t) * size_t(capacity));
+  if (e == cudaSuccess) e = cudaMalloc(&r->large_tiles, sizeof(uint32_t) * size_t(capacity));
   if (e == cudaSuccess) e = cudaMalloc(&r->tile_prefix, sizeof(unsigned long long) * (size_t(capacity) + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&r->block_sums, sizeof(unsigned long long) * (atm::kRasterScanBlocks + 1));
   if (e == cudaSuccess) e = cudaMalloc(&r->depth_key, sizeof(unsigned long long) * size_t(width) * height);
   int dev = 0;
   if (e == cudaSuccess) e = cudaGetDevice(&dev);
@@ -1518,6 +1522,8 @@ ATM_API int atm_raster_destroy(AtmRaster* r) {
   if (r->count) cudaFree(r->count);
   if (r->large) cudaFree(r->large);
   if (r->tile_prefix) cudaFree(r->tile_prefix);
+  if (r->large_tiles) cudaFree(r->large_tiles);
+  if (r->block_sums) cudaFree(r->block_sums);
   if (r->depth_key) cudaFree(r->depth_key);
   delete r;
   return ATM_OK;
@@ -1557,7 +1563,7 @@ ATM_API int atm_raster_terrain(AtmRaster* r, const AtmRasterMesh* m, double near
                        m->cell,       m->triangles,  m->active_slots, m->skirt_mask,
                        m->slot_level, m->patches,    m->vertices_per_patch, m->triangles_per_patch,
                        m->surface_triangles_per_patch, m->resolution, m->n_active};
-  atm::RasterStream S{r->tris, r->count, r->capacity, r->large, r->tile_prefix};
+  atm::RasterStream S{r->tris, r->count, r->capacity, r->large, r->large_tiles, r->tile_prefix, r->block_sums};
   if (o->terrain_surface_id && (!o->terrain_position || !o->terrain_normal || !o->terrain_albedo))
     return fail(ATM_E_INVALID, "the terrain snapshot needs position, normal and albedo images");
   atm::RasterOutDev O{o->depth,          o->position,        o->normal,           o->albedo,

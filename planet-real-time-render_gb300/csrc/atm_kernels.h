@@ -264,8 +264,11 @@ struct RasterStream {
                     // [1] large triangles listed, [2] spare
   long long capacity;
   uint32_t* large;                 // capacity: the emitted triangles too large for one warp
-  unsigned long long* tile_prefix; // capacity + 1: exclusive prefix of their pixel-tile counts
+  uint32_t* large_tiles;           // capacity: their pixel-tile counts
+  unsigned long long* tile_prefix; // capacity + 1: exclusive prefix of the tile counts
+  unsigned long long* block_sums;  // kRasterScanBlocks + 1: the prefix's per-block partial sums
 };
+constexpr int kRasterScanBlocks = 256;
 struct RasterMeshDev {
   const float* view;       // [patches][vertices][3]
   const float* normal;     // [patches][vertices][3]

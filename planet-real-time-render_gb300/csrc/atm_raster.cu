@@ -9,7 +9,7 @@
 //    plane and the four frustum sides, and the emission (an atomic append)
 //    of each resulting triangle with its screen setup: projection snapped to
 //    1/256 pixel, edge equations, top-left flags, inverse area;
-//  * k_raster_depth (+ k_raster_tile_prefix, k_raster_depth_tiles): coverage
+//  * k_raster_depth (+ k_raster_scan_*, k_raster_depth_tiles): coverage
 //    by the edge equations with the top-left rule and a 64-bit atomic
 //    minimum of (depth bits << 32 | triangle) per pixel; small triangles by
 //    one thread, medium ones by a warp, large ones cut into 8 x 32 pixel
@@ -293,24 +293,11 @@ __device__ __forceinline__ void warp_tile(const RasterTri& T, unsigned long long
   __syncwarp();
 }
 
-// A whole box by one warp, in 8 x 32 tiles (each skipped when the edge
-// equations reject it).
-__device__ __forceinline__ void warp_box(const RasterTri& T, unsigned long long q, const Box& b, int H,
-                                         unsigned long long* __restrict__ depth_key, uint8_t* list) {
-  for (int xs = b.x0; xs <= b.x1; xs += kRasterTileW)
-    for (int ys = b.y0; ys <= b.y1; ys += kRasterTileH) {
-      const int xe = min(xs + kRasterTileW - 1, b.x1), ye = min(ys + kRasterTileH - 1, b.y1);
-      if (!tile_outside(T, xs, xe, ys, ye)) warp_tile(T, q, xs, xe, ys, ye, H, depth_key, list);
-    }
-}
-
 // Thread per emitted triangle (grid-stride, warp-aligned): small boxes are
 // walked by their own thread, medium ones by the whole warp in turn, large
 // ones are listed for k_raster_depth_tiles.
 __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayout L,
                                                       unsigned long long* __restrict__ depth_key) {
-  __shared__ uint8_t s_list[8][kRasterTileW * kRasterTileH];
-  uint8_t* list = s_list[threadIdx.x >> 5];
   const int lane = threadIdx.x & 31;
   const long long n = min((long long)S.count[0], (long long)S.capacity);
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -328,7 +315,10 @@ __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayou
         } else if (area <= kRasterWarpArea) {
           medium = true;
         } else {
-          S.large[atomicAdd(S.count + 1, 1u)] = uint32_t(q);  // at most one entry per stored triangle
+          const uint32_t idx = atomicAdd(S.count + 1, 1u);  // at most one entry per stored triangle
+          S.large[idx] = uint32_t(q);
+          S.large_tiles[idx] = uint32_t((b.x1 - b.x0 + kRasterTileW) / kRasterTileW) *
+                               uint32_t((b.y1 - b.y0 + kRasterTileH) / kRasterTileH);
         }
       }
     }
@@ -338,51 +328,72 @@ __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayou
       m &= m - 1;
       const long long ql = base + leader;
       const RasterTri& T = S.tris[ql];
-      warp_box(T, (unsigned long long)ql, bbox(T, L), L.height, depth_key, list);
+      const Box b = bbox(T, L);
+      const int bh = b.y1 - b.y0 + 1;
+      const int area = (b.x1 - b.x0 + 1) * bh;  // at most kRasterWarpArea: 8 pixels per lane
+      for (int k = lane; k < area; k += 32)
+        depth_pixel(T, b.x0 + k / bh, b.y0 + k % bh, L.height, depth_key, (unsigned long long)ql);
     }
   }
 }
 
-// One block: the exclusive prefix of the large triangles' tile counts
-// (64-bit), in chunks of the block size.
-__global__ void __launch_bounds__(1024) k_raster_tile_prefix(RasterStream S, ImageLayout L) {
-  __shared__ unsigned long long part[32];
-  __shared__ unsigned long long carry;
-  const uint32_t n = S.count[1];
-  if (threadIdx.x == 0) carry = 0;
-  __syncthreads();
+// The exclusive prefix of the large triangles' tile counts (64-bit) in three
+// launches: per-block sums over kRasterScanBlocks equal ranges, a scan of
+// the sums, then each block's own scan offset by its sum's prefix.
+__device__ __forceinline__ void scan_range(uint32_t n, uint32_t& lo, uint32_t& hi) {
+  const uint32_t per = (n + kRasterScanBlocks - 1) / kRasterScanBlocks;
+  lo = min(n, blockIdx.x * per);
+  hi = min(n, lo + per);
+}
+// Exclusive block scan of one value per thread (256 threads); returns the
+// block total through `total`.
+__device__ __forceinline__ unsigned long long block_exclusive_scan(unsigned long long v, unsigned long long& total) {
+  __shared__ unsigned long long warp_sums[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (uint32_t base = 0; base < n; base += blockDim.x) {
-    const uint32_t k = base + threadIdx.x;
-    unsigned long long tiles = 0;
-    if (k < n) {
-      const Box b = bbox(S.tris[S.large[k]], L);
-      tiles = (unsigned long long)((b.x1 - b.x0 + kRasterTileW) / kRasterTileW) *
-              ((b.y1 - b.y0 + kRasterTileH) / kRasterTileH);
-    }
-    unsigned long long v = tiles;  // inclusive warp scan
-    for (int o = 1; o < 32; o <<= 1) {
-      const unsigned long long t = __shfl_up_sync(0xffffffffu, v, o);
-      if (lane >= o) v += t;
-    }
-    if (lane == 31) part[warp] = v;
-    __syncthreads();
-    if (warp == 0) {
-      unsigned long long w = lane < int(blockDim.x >> 5) ? part[lane] : 0;
-      for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
-        if (lane >= o) w += t;
-      }
-      part[lane] = w;  // inclusive over warps
-    }
-    __syncthreads();
-    const unsigned long long before = carry + (warp > 0 ? part[warp - 1] : 0) + v - tiles;
-    if (k < n) S.tile_prefix[k] = before;
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = before + tiles;
-    __syncthreads();
+  unsigned long long inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const unsigned long long t = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += t;
   }
-  if (threadIdx.x == 0) S.tile_prefix[n] = carry;
+  if (lane == 31) warp_sums[warp] = inc;
+  __syncthreads();
+  unsigned long long before = 0;
+  total = 0;
+  for (int w = 0; w < 8; ++w) {
+    if (w < warp) before += warp_sums[w];
+    total += warp_sums[w];
+  }
+  __syncthreads();  // warp_sums is reused by the next call
+  return before + inc - v;
+}
+__global__ void __launch_bounds__(256) k_raster_scan_sums(RasterStream S) {
+  uint32_t lo, hi;
+  scan_range(S.count[1], lo, hi);
+  unsigned long long sum = 0, total;
+  for (uint32_t k = lo + threadIdx.x; k < hi; k += blockDim.x) sum += S.large_tiles[k];
+  block_exclusive_scan(sum, total);
+  if (threadIdx.x == 0) S.block_sums[blockIdx.x] = total;
+}
+__global__ void __launch_bounds__(256) k_raster_scan_top(RasterStream S) {
+  unsigned long long total;
+  const unsigned long long v = threadIdx.x < kRasterScanBlocks ? S.block_sums[threadIdx.x] : 0;
+  const unsigned long long before = block_exclusive_scan(v, total);
+  if (threadIdx.x < kRasterScanBlocks) S.block_sums[threadIdx.x] = before;
+  if (threadIdx.x == 0) S.tile_prefix[S.count[1]] = total;
+}
+__global__ void __launch_bounds__(256) k_raster_scan_apply(RasterStream S) {
+  uint32_t lo, hi;
+  scan_range(S.count[1], lo, hi);
+  unsigned long long carry = S.block_sums[blockIdx.x];
+  for (uint32_t base = lo; base < hi; base += blockDim.x) {
+    const uint32_t k = base + threadIdx.x;
+    const unsigned long long v = k < hi ? S.large_tiles[k] : 0;
+    unsigned long long total;
+    const unsigned long long before = block_exclusive_scan(v, total);
+    if (k < hi) S.tile_prefix[k] = carry + before;
+    carry += total;
+  }
 }
 
 // The large triangles' 8 x 32 pixel tiles, split evenly over the grid's
@@ -552,7 +563,9 @@ cudaError_t launch_raster(const RasterMeshDev& M, const RasterStream& S, const I
   k_raster_depth<<<unsigned(sm_count * 8), 256, 0, s>>>(S, L, depth_key);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_raster_tile_prefix<<<1, 1024, 0, s>>>(S, L);
+  k_raster_scan_sums<<<kRasterScanBlocks, 256, 0, s>>>(S);
+  k_raster_scan_top<<<1, 256, 0, s>>>(S);
+  k_raster_scan_apply<<<kRasterScanBlocks, 256, 0, s>>>(S);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_raster_depth_tiles<<<unsigned(sm_count * 8), 256, 0, s>>>(S, L, depth_key);
