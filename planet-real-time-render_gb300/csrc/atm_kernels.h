@@ -261,7 +261,7 @@ struct RasterTri {
 struct RasterStream {
   RasterTri* tris;
   uint32_t* count;  // [0] triangles emitted (may exceed capacity: only capacity are stored),
-                    // [1] large triangles listed, [2] spare
+                    // [1] large triangles listed, [2..3] the 64-bit work ticket of their blocks
   long long capacity;
   uint32_t* large;                 // capacity: the emitted triangles too large for one warp
   uint32_t* large_tiles;           // capacity: their pixel-tile counts

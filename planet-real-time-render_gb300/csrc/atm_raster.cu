@@ -234,7 +234,8 @@ __device__ __forceinline__ Box bbox(const RasterTri& T, const ImageLayout& L) {
 }
 constexpr long long kRasterThreadArea = 16;  // bounding boxes up to this many pixels: one thread
 constexpr long long kRasterWarpArea = 256;   // up to this: one warp; larger: tiles over the whole grid
-constexpr int kRasterTileW = 8, kRasterTileH = 32;  // a large triangle's work item: 8 columns x 32 rows
+constexpr int kRasterTileW = 256, kRasterTileH = 32;  // a large triangle's work item: 256 columns x 32 rows
+constexpr int kRasterItemsPerTicket = 4;              // work items a warp takes per ticket
 
 // Whether the edge equations reject a whole tile of pixel centres: an edge
 // whose value is negative at the tile's corner where it is largest.  The
@@ -251,46 +252,69 @@ __device__ __forceinline__ bool tile_outside(const RasterTri& T, int xs, int xe,
   return false;
 }
 
-// One warp over a tile of at most 8 columns x 32 rows (lane = row): the
-// lanes test their pixels' coverage, the covered pixels are compacted in the
-// warp's shared-memory list, then every lane takes list entries for the
-// depth and the atomic (the costly part runs with all lanes busy however
-// sparse the coverage).
-__device__ __forceinline__ void warp_tile(const RasterTri& T, unsigned long long q, int xs, int xe, int ys, int ye,
-                                          int H, unsigned long long* __restrict__ depth_key, uint8_t* list) {
+// A row's conservative span of columns inside the triangle (within
+// [xs, xe]), from each edge's crossing: the exact per-pixel test decides,
+// the span only bounds the walk.  The crossing is widened by one pixel plus
+// a bound on the float32 rounding of the edge value, (|A x| + |B y| + |C|)
+// 2^-20 / |A| pixels: every pixel the exact test covers lies inside the
+// span.  n = 0: the row holds no covered pixel.
+__device__ __forceinline__ void row_span(const RasterTri& T, float py, int xs, int xe, int& l, int& n) {
+  float lo = float(xs), hi = float(xe);
+  const float xmag = fmaxf(fabsf(float(xs)), fabsf(float(xe))) + 1.0f;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float A = T.eq[k][0];
+    const float By = mul(T.eq[k][1], py);
+    const float rest = add(By, T.eq[k][2]);
+    if (A == 0.0f) {
+      if (rest < 0.0f) hi = -1.0f;  // e = (0 + B y) + C = rest exactly, for every pixel of the row
+    } else {
+      const float cross = sub(dv(-rest, A), 0.5f);  // pixel index where e crosses 0
+      const float margin =
+          1.0f + (fabsf(A) * xmag + fabsf(By) + fabsf(T.eq[k][2])) * 9.5367431640625e-07f / fabsf(A);
+      if (A > 0.0f)
+        lo = fmaxf(lo, floorf(cross - margin));
+      else
+        hi = fminf(hi, ceilf(cross + margin));
+    }
+  }
+  // NaN crossings compare false and leave the bounds as they were
+  lo = fmaxf(lo, float(xs));
+  hi = fminf(hi, float(xe));
+  l = int(lo);
+  n = hi >= lo ? int(hi) - int(lo) + 1 : 0;
+}
+
+// One work item of a large triangle, a block of up to 256 columns x 32 rows
+// walked by one warp: lane = row computes its span, the spans are prefix-
+// summed over the lanes, and the lanes then take the spans' pixels 32 at a
+// time (the exact coverage test, the depth and the atomic minimum), so the
+// lanes stay busy however thin the triangle.
+__device__ __forceinline__ void warp_block(const RasterTri& T, unsigned long long q, int xs, int xe, int ys, int ye,
+                                           int H, unsigned long long* __restrict__ depth_key) {
   const int lane = threadIdx.x & 31;
   const int y = ys + lane;
-  unsigned mask = 0;
-  if (y <= ye) {
-    const float py = add(float(y), 0.5f);
-    for (int c = 0; c <= xe - xs; ++c)
-      if (inside_edges(T, edge_values(T, add(float(xs + c), 0.5f), py))) mask |= 1u << c;
-  }
-  const int n = __popc(mask);
-  int off = n;  // inclusive scan of the counts
+  int l = 0, n = 0;
+  if (y <= ye) row_span(T, add(float(y), 0.5f), xs, xe, l, n);
+  int incl = n;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    const int t = __shfl_up_sync(0xffffffffu, off, o);
-    if (lane >= o) off += t;
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
   }
-  const int total = __shfl_sync(0xffffffffu, off, 31);
-  off -= n;
-  while (mask) {
-    const int c = __ffs(mask) - 1;
-    mask &= mask - 1;
-    list[off++] = uint8_t((c << 5) | lane);
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  for (int base = 0; base < total; base += 32) {
+    const int i = base + lane;
+    int row = 0;  // the first lane whose inclusive count exceeds i
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+      const int probe = __shfl_sync(0xffffffffu, incl, row + step - 1);
+      if (probe <= i) row += step;
+    }
+    const int rl = __shfl_sync(0xffffffffu, l, row), rn = __shfl_sync(0xffffffffu, n, row);
+    const int rincl = __shfl_sync(0xffffffffu, incl, row);
+    if (i < total) depth_pixel(T, rl + (i - (rincl - rn)), ys + row, H, depth_key, q);
   }
-  __syncwarp();
-  for (int i = lane; i < total; i += 32) {
-    const int c = list[i] >> 5, row = list[i] & 31;
-    const int px = xs + c, py = ys + row;
-    const r3 e = edge_values(T, add(float(px), 0.5f), add(float(py), 0.5f));
-    const r3 l = rscale(e, T.inv_area);
-    const float z = dv(1.0f, fmx(add(add(dv(l.x, T.screen[0][2]), dv(l.y, T.screen[1][2])), dv(l.z, T.screen[2][2])),
-                                 1e-20f));
-    atomicMin(depth_key + (size_t(px) * H + py), ((unsigned long long)__float_as_uint(z) << 32) | q);
-  }
-  __syncwarp();
 }
 
 // Thread per emitted triangle (grid-stride, warp-aligned): small boxes are
@@ -396,44 +420,46 @@ __global__ void __launch_bounds__(256) k_raster_scan_apply(RasterStream S) {
   }
 }
 
-// The large triangles' 8 x 32 pixel tiles, split evenly over the grid's
-// warps in contiguous runs (a run mostly stays within one triangle, found
-// once by binary search of the prefix); lane = row, 8 columns; tiles the
-// edge equations reject are skipped.
+// The large triangles' work items (blocks of 256 x 32 pixels of their
+// bounding boxes), taken by warps from a ticket kRasterItemsPerTicket at a
+// time (the first item's triangle by binary search of the prefix, the next
+// ones by walking on); blocks the edge equations reject are skipped.
 __global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, ImageLayout L,
                                                             unsigned long long* __restrict__ depth_key) {
-  __shared__ uint8_t s_list[8][kRasterTileW * kRasterTileH];
-  uint8_t* list = s_list[threadIdx.x >> 5];
   const uint32_t n = S.count[1];
   if (n == 0) return;
   const unsigned long long total = S.tile_prefix[n];
-  const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-  const unsigned long long warp = blockIdx.x * (unsigned long long)(blockDim.x >> 5) + (threadIdx.x >> 5);
-  const unsigned long long per = (total + warps - 1) / warps;
-  const unsigned long long w0 = warp * per, w1 = min(w0 + per, total);
-  if (w0 >= w1) return;
-  uint32_t k = 0, hi = n - 1;  // last k with prefix[k] <= w0
-  while (k < hi) {
-    const uint32_t mid = (k + hi + 1) >> 1;
-    if (S.tile_prefix[mid] <= w0) k = mid; else hi = mid - 1;
-  }
-  unsigned long long first = S.tile_prefix[k], next = S.tile_prefix[k + 1];
-  for (unsigned long long w = w0; w < w1; ++w) {
-    while (w >= next) {
-      ++k;
-      first = next;
-      next = S.tile_prefix[k + 1];
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long w0 = 0;
+    if (lane == 0)  // 64-bit ticket in count[2..3] (8-byte aligned): it cannot wrap below total
+      w0 = atomicAdd(reinterpret_cast<unsigned long long*>(S.count + 2), (unsigned long long)kRasterItemsPerTicket);
+    w0 = __shfl_sync(0xffffffffu, w0, 0);
+    if (w0 >= total) break;
+    const unsigned long long w1 = min(w0 + kRasterItemsPerTicket, total);
+    uint32_t k = 0, hi = n - 1;  // last k with prefix[k] <= w0
+    while (k < hi) {
+      const uint32_t mid = (k + hi + 1) >> 1;
+      if (S.tile_prefix[mid] <= w0) k = mid; else hi = mid - 1;
     }
-    const uint32_t q = S.large[k];
-    const RasterTri& T = S.tris[q];
-    const Box b = bbox(T, L);
-    const int rows = (b.y1 - b.y0 + kRasterTileH) / kRasterTileH;
-    const unsigned long long t = w - first;
-    const int tx = int(t / rows), ty = int(t % rows);
-    const int xs = b.x0 + tx * kRasterTileW, xe = min(xs + kRasterTileW - 1, b.x1);
-    const int ys = b.y0 + ty * kRasterTileH, ye = min(ys + kRasterTileH - 1, b.y1);
-    if (tile_outside(T, xs, xe, ys, ye)) continue;
-    warp_tile(T, q, xs, xe, ys, ye, L.height, depth_key, list);
+    unsigned long long first = S.tile_prefix[k], next = S.tile_prefix[k + 1];
+    for (unsigned long long w = w0; w < w1; ++w) {
+      while (w >= next) {
+        ++k;
+        first = next;
+        next = S.tile_prefix[k + 1];
+      }
+      const uint32_t q = S.large[k];
+      const RasterTri& T = S.tris[q];
+      const Box b = bbox(T, L);
+      const int rows = (b.y1 - b.y0 + kRasterTileH) / kRasterTileH;
+      const int t = int(w - first);
+      const int tx = t / rows, ty = t % rows;
+      const int xs = b.x0 + tx * kRasterTileW, xe = min(xs + kRasterTileW - 1, b.x1);
+      const int ys = b.y0 + ty * kRasterTileH, ye = min(ys + kRasterTileH - 1, b.y1);
+      if (tile_outside(T, xs, xe, ys, ye)) continue;
+      warp_block(T, q, xs, xe, ys, ye, L.height, depth_key);
+    }
   }
 }
 
@@ -541,7 +567,7 @@ __global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLay
 
 __global__ void k_raster_clear(unsigned long long* __restrict__ depth_key, long long n, uint32_t* count) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i < 3) count[i] = 0u;
+  if (i < 4) count[i] = 0u;
   if (i < n) depth_key[i] = kSentinel;
 }
 
