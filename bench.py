@@ -58,6 +58,10 @@ COMPOSITE_FLOP_PER_SAMPLE = 406.16
 # DRAM bytes a composite pixel must move: position 12 + surface_id 4 +
 # scene 12 + space 12 read, hdr 12 written (LUTs stay in L2).
 COMPOSITE_BYTES_PER_PIXEL = 52
+# DRAM bytes (read + write) of one k_composite launch of the 2 km camera at
+# 1920x1080, from `ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum`
+# on `bench.py --profile-case frame1080p` (58,468,352 + 3,072,256)
+COMPOSITE_DRAM_BYTES_1080P = 58_468_352 + 3_072_256
 MLP_CHECK_FRACTION = 0.01  # share of MLP pixels the plain path re-integrates
 # A step is this many passes of the three cameras' chains (48 frames of
 # 1080p, ~57 ms): with the usual 20 timed steps the timed region lasts over a
@@ -536,7 +540,8 @@ def main() -> None:
                             "uploads/read-backs on a copy stream overlapping the other cameras' kernels"},
             "gpu_launches": 12 * PASSES_PER_STEP * args.steps,
             "roofline": {"bound": "fp32", "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / peak_tflops, "traffic": None, "kernel": "k_composite",
+                         "frac": achieved_tflops / peak_tflops, "traffic": COMPOSITE_DRAM_BYTES_1080P, "traffic_unit": "bytes per launch (2 km camera, ncu)",
+                         "kernel": "k_composite",
                          "peak_source": f"derived: {SMS} SMs x {FP32_LANES} FP32 lanes x 2 x median SM clock "
                                         f"{sm_mhz:.0f} MHz sampled during the run",
                          "algorithmic": f"{COMPOSITE_FLOP_PER_SAMPLE} FLOP per radiance sample x "

@@ -249,15 +249,23 @@ cudaError_t launch_frame(const DevParams& P, const ImageLayout& L, const Composi
 // One emitted (clipped) triangle: vertex view positions, normals, material
 // weights, heights and cell ids, its screen setup (pixels snapped to 1/256,
 // view depth), edge equations, top-left flags (bit k: edge k) and source id.
-struct RasterTri {
-  float v[3][3], n[3][3], m[3][4], h[3];
-  int32_t c[3];
+// The setup the depth passes read comes first, 80 bytes; the attributes the
+// resolve reads for the winning triangle follow.  240 bytes, 16-byte
+// aligned: written and read as float4.
+struct alignas(16) RasterSetup {
   float screen[3][3];
   float eq[3][3];
   float inv_area;
   int32_t tl;
-  int32_t src;
 };
+struct alignas(16) RasterTri {
+  RasterSetup s;
+  float v[3][3], n[3][3], m[3][4], h[3];
+  int32_t c[3];
+  int32_t src;
+  int32_t pad[3];
+};
+static_assert(sizeof(RasterSetup) == 80 && sizeof(RasterTri) == 240, "raster record layout");
 struct RasterStream {
   RasterTri* tris;
   uint32_t* count;  // [0] triangles emitted (may exceed capacity: only capacity are stored),

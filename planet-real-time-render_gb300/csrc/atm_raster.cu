@@ -77,13 +77,31 @@ __device__ __forceinline__ int top_left(float ax, float ay, float bx, float by, 
   return (dy > 0.0f) || (dy == 0.0f && dx < 0.0f);
 }
 
-// _emit :628-686
+union TriBits {
+  RasterTri t;
+  float4 v[sizeof(RasterTri) / 16];
+};
+union SetupBits {
+  RasterSetup s;
+  float4 v[sizeof(RasterSetup) / 16];
+};
+__device__ __forceinline__ RasterSetup load_setup(const RasterTri* t) {
+  SetupBits u;
+  const float4* p = reinterpret_cast<const float4*>(t);
+#pragma unroll
+  for (int k = 0; k < int(sizeof(RasterSetup) / 16); ++k) u.v[k] = p[k];
+  return u.s;
+}
+
+// _emit :628-686: the record is assembled in registers and stored as float4s
 __device__ void emit(const RasterMeshDev& M, RasterStream S, int32_t src, const CVert (&v)[3], float tf,
                      float aspect, int width, int height) {
   const uint32_t s = atomicAdd(S.count, 1u);
   if (s >= uint32_t(S.capacity)) return;  // counted, not stored (the reference's s >= capacity)
-  RasterTri& T = S.tris[s];
+  TriBits u;
+  RasterTri& T = u.t;
   float sp[3][3];
+#pragma unroll
   for (int k = 0; k < 3; ++k) {
     const r3 p = v[k].p;
     T.v[k][0] = p.x;
@@ -92,6 +110,7 @@ __device__ void emit(const RasterMeshDev& M, RasterStream S, int32_t src, const 
     T.n[k][0] = v[k].n.x;
     T.n[k][1] = v[k].n.y;
     T.n[k][2] = v[k].n.z;
+#pragma unroll
     for (int i = 0; i < 4; ++i) T.m[k][i] = v[k].m.v[i];
     T.h[k] = v[k].h;
     T.c[k] = v[k].c;
@@ -102,23 +121,28 @@ __device__ void emit(const RasterMeshDev& M, RasterStream S, int32_t src, const 
     sp[k][0] = px;
     sp[k][1] = py;
     sp[k][2] = p.z;
-    T.screen[k][0] = px;
-    T.screen[k][1] = py;
-    T.screen[k][2] = p.z;
+    T.s.screen[k][0] = px;
+    T.s.screen[k][1] = py;
+    T.s.screen[k][2] = p.z;
   }
   const float ax = sp[0][0], ay = sp[0][1], bx = sp[1][0], by = sp[1][1], cx = sp[2][0], cy = sp[2][1];
   const float area = sub(mul(sub(bx, ax), sub(cy, ay)), mul(sub(by, ay), sub(cx, ax)));  // _edge(a, b, c)
   const float abs_area = fabsf(area);
   const float sg = area > 0.0f ? 1.0f : -1.0f;
-  T.inv_area = abs_area > 1e-8f ? dv(1.0f, abs_area) : 0.0f;
+  T.s.inv_area = abs_area > 1e-8f ? dv(1.0f, abs_area) : 0.0f;
   const r3 e0 = rscale(edge_coeff(bx, by, cx, cy), sg);
   const r3 e1 = rscale(edge_coeff(cx, cy, ax, ay), sg);
   const r3 e2 = rscale(edge_coeff(ax, ay, bx, by), sg);
-  T.eq[0][0] = e0.x, T.eq[0][1] = e0.y, T.eq[0][2] = e0.z;
-  T.eq[1][0] = e1.x, T.eq[1][1] = e1.y, T.eq[1][2] = e1.z;
-  T.eq[2][0] = e2.x, T.eq[2][1] = e2.y, T.eq[2][2] = e2.z;
-  T.tl = top_left(bx, by, cx, cy, sg) | (top_left(cx, cy, ax, ay, sg) << 1) | (top_left(ax, ay, bx, by, sg) << 2);
+  T.s.eq[0][0] = e0.x, T.s.eq[0][1] = e0.y, T.s.eq[0][2] = e0.z;
+  T.s.eq[1][0] = e1.x, T.s.eq[1][1] = e1.y, T.s.eq[1][2] = e1.z;
+  T.s.eq[2][0] = e2.x, T.s.eq[2][1] = e2.y, T.s.eq[2][2] = e2.z;
+  T.s.tl =
+      top_left(bx, by, cx, cy, sg) | (top_left(cx, cy, ax, ay, sg) << 1) | (top_left(ax, ay, bx, by, sg) << 2);
   T.src = src;
+  T.pad[0] = T.pad[1] = T.pad[2] = 0;
+  float4* dst = reinterpret_cast<float4*>(S.tris + s);
+#pragma unroll
+  for (int k = 0; k < int(sizeof(RasterTri) / 16); ++k) dst[k] = u.v[k];
 }
 
 // _clip :731-901
@@ -141,14 +165,13 @@ __global__ void __launch_bounds__(128) k_raster_clip(RasterMeshDev M, RasterStre
   const int32_t* ids = M.triangles + 3 * local_id;
   for (int k = 0; k < 3; ++k)
     if (ids[k] < 0 || ids[k] >= M.vertices_per_patch) return;  // a vertex outside the patch: dropped
+  // positions first: culled and rejected triangles read nothing else
   CVert v[3];
+  long long ev[3];
   for (int k = 0; k < 3; ++k) {
     const long long e = (long long)slot * M.vertices_per_patch + ids[k];
+    ev[k] = e;
     v[k].p = R3(M.view[3 * e], M.view[3 * e + 1], M.view[3 * e + 2]);
-    v[k].n = R3(M.normal[3 * e], M.normal[3 * e + 1], M.normal[3 * e + 2]);
-    for (int j = 0; j < 4; ++j) v[k].m.v[j] = M.material[4 * e + j];
-    v[k].h = M.height[e];
-    v[k].c = M.cell[e];
   }
   // ordinary terrain back faces are culled; skirts stay double-sided
   if (local_id < stc) {
@@ -158,6 +181,13 @@ __global__ void __launch_bounds__(128) k_raster_clip(RasterMeshDev M, RasterStre
   const int c0 = clip_code(v[0].p, near, tx, ty), c1 = clip_code(v[1].p, near, tx, ty),
             c2 = clip_code(v[2].p, near, tx, ty);
   if (c0 & c1 & c2) return;  // all three outside one plane
+  for (int k = 0; k < 3; ++k) {
+    const long long e = ev[k];
+    v[k].n = R3(M.normal[3 * e], M.normal[3 * e + 1], M.normal[3 * e + 2]);
+    for (int j = 0; j < 4; ++j) v[k].m.v[j] = M.material[4 * e + j];
+    v[k].h = M.height[e];
+    v[k].c = M.cell[e];
+  }
   if ((c0 | c1 | c2) == 0) {
     emit(M, S, source_id, v, tf, aspect, width, height);
     return;
@@ -200,12 +230,12 @@ __global__ void __launch_bounds__(128) k_raster_clip(RasterMeshDev M, RasterStre
   }
 }
 
-__device__ __forceinline__ r3 edge_values(const RasterTri& T, float px, float py) {
+__device__ __forceinline__ r3 edge_values(const RasterSetup& T, float px, float py) {
   return {add(add(mul(T.eq[0][0], px), mul(T.eq[0][1], py)), T.eq[0][2]),
           add(add(mul(T.eq[1][0], px), mul(T.eq[1][1], py)), T.eq[1][2]),
           add(add(mul(T.eq[2][0], px), mul(T.eq[2][1], py)), T.eq[2][2])};
 }
-__device__ __forceinline__ bool inside_edges(const RasterTri& T, r3 e) {
+__device__ __forceinline__ bool inside_edges(const RasterSetup& T, r3 e) {
   return (e.x > 0.0f || (e.x == 0.0f && (T.tl & 1))) && (e.y > 0.0f || (e.y == 0.0f && (T.tl & 2))) &&
          (e.z > 0.0f || (e.z == 0.0f && (T.tl & 4)));
 }
@@ -214,7 +244,7 @@ __device__ __forceinline__ bool inside_edges(const RasterTri& T, r3 e) {
 // pixel centre (edge equations with the top-left rule) takes the atomic
 // minimum of (depth bits << 32 | triangle); the order of the atomics changes
 // no result.  Pixels are walked along y, the depth keys' contiguous axis.
-__device__ __forceinline__ void depth_pixel(const RasterTri& T, int x, int y, int H,
+__device__ __forceinline__ void depth_pixel(const RasterSetup& T, int x, int y, int H,
                                             unsigned long long* __restrict__ depth_key, unsigned long long q) {
   const r3 e = edge_values(T, add(float(x), 0.5f), add(float(y), 0.5f));
   if (!inside_edges(T, e)) return;
@@ -226,7 +256,7 @@ __device__ __forceinline__ void depth_pixel(const RasterTri& T, int x, int y, in
 struct Box {
   int x0, x1, y0, y1;
 };
-__device__ __forceinline__ Box bbox(const RasterTri& T, const ImageLayout& L) {
+__device__ __forceinline__ Box bbox(const RasterSetup& T, const ImageLayout& L) {
   const float ax = T.screen[0][0], bx = T.screen[1][0], cx = T.screen[2][0];
   const float ay = T.screen[0][1], by = T.screen[1][1], cy = T.screen[2][1];
   return {max(int(floorf(fmn(fmn(ax, bx), cx))), 0), min(int(ceilf(fmx(fmx(ax, bx), cx))), L.width - 1),
@@ -242,7 +272,7 @@ constexpr int kRasterItemsPerTicket = 4;              // work items a warp takes
 // float32 edge value is monotone in x (y) for a non-negative x (y)
 // coefficient, so that corner is the tile's largest value as the pixel test
 // evaluates it: a rejected tile holds no covered pixel.
-__device__ __forceinline__ bool tile_outside(const RasterTri& T, int xs, int xe, int ys, int ye) {
+__device__ __forceinline__ bool tile_outside(const RasterSetup& T, int xs, int xe, int ys, int ye) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     const float px = add(float(T.eq[k][0] >= 0.0f ? xe : xs), 0.5f);
@@ -258,7 +288,7 @@ __device__ __forceinline__ bool tile_outside(const RasterTri& T, int xs, int xe,
 // a bound on the float32 rounding of the edge value, (|A x| + |B y| + |C|)
 // 2^-20 / |A| pixels: every pixel the exact test covers lies inside the
 // span.  n = 0: the row holds no covered pixel.
-__device__ __forceinline__ void row_span(const RasterTri& T, float py, int xs, int xe, int& l, int& n) {
+__device__ __forceinline__ void row_span(const RasterSetup& T, float py, int xs, int xe, int& l, int& n) {
   float lo = float(xs), hi = float(xe);
   const float xmag = fmaxf(fabsf(float(xs)), fabsf(float(xe))) + 1.0f;
 #pragma unroll
@@ -290,7 +320,7 @@ __device__ __forceinline__ void row_span(const RasterTri& T, float py, int xs, i
 // summed over the lanes, and the lanes then take the spans' pixels 32 at a
 // time (the exact coverage test, the depth and the atomic minimum), so the
 // lanes stay busy however thin the triangle.
-__device__ __forceinline__ void warp_block(const RasterTri& T, unsigned long long q, int xs, int xe, int ys, int ye,
+__device__ __forceinline__ void warp_block(const RasterSetup& T, unsigned long long q, int xs, int xe, int ys, int ye,
                                            int H, unsigned long long* __restrict__ depth_key) {
   const int lane = threadIdx.x & 31;
   const int y = ys + lane;
@@ -329,7 +359,7 @@ __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayou
     const long long q = base + lane;
     bool medium = false;
     if (q < n) {
-      const RasterTri& T = S.tris[q];
+      const RasterSetup T = load_setup(S.tris + q);
       const Box b = bbox(T, L);
       if (T.inv_area > 0.0f && b.x0 <= b.x1 && b.y0 <= b.y1) {
         const long long area = (long long)(b.x1 - b.x0 + 1) * (b.y1 - b.y0 + 1);
@@ -351,7 +381,7 @@ __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayou
       const int leader = __ffs(m) - 1;
       m &= m - 1;
       const long long ql = base + leader;
-      const RasterTri& T = S.tris[ql];
+      const RasterSetup T = load_setup(S.tris + ql);
       const Box b = bbox(T, L);
       const int bh = b.y1 - b.y0 + 1;
       const int area = (b.x1 - b.x0 + 1) * bh;  // at most kRasterWarpArea: 8 pixels per lane
@@ -450,7 +480,7 @@ __global__ void __launch_bounds__(256) k_raster_depth_tiles(RasterStream S, Imag
         next = S.tile_prefix[k + 1];
       }
       const uint32_t q = S.large[k];
-      const RasterTri& T = S.tris[q];
+      const RasterSetup T = load_setup(S.tris + q);
       const Box b = bbox(T, L);
       const int rows = (b.y1 - b.y0 + kRasterTileH) / kRasterTileH;
       const int t = int(w - first);
@@ -529,10 +559,14 @@ __global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLay
     return;
   }
   const float z = __uint_as_float(uint32_t(key >> 32));
-  const RasterTri& T = S.tris[key & 0xffffffffull];
-  const r3 l = rscale(edge_values(T, add(float(x), 0.5f), add(float(y), 0.5f)), T.inv_area);
-  const float w0 = dv(mul(l.x, z), T.screen[0][2]), w1 = dv(mul(l.y, z), T.screen[1][2]),
-              w2 = dv(mul(l.z, z), T.screen[2][2]);
+  TriBits u;
+  const float4* rec = reinterpret_cast<const float4*>(S.tris + (key & 0xffffffffull));
+#pragma unroll
+  for (int k = 0; k < int(sizeof(RasterTri) / 16); ++k) u.v[k] = rec[k];
+  const RasterTri& T = u.t;
+  const r3 l = rscale(edge_values(T.s, add(float(x), 0.5f), add(float(y), 0.5f)), T.s.inv_area);
+  const float w0 = dv(mul(l.x, z), T.s.screen[0][2]), w1 = dv(mul(l.y, z), T.s.screen[1][2]),
+              w2 = dv(mul(l.z, z), T.s.screen[2][2]);
   auto lerp3 = [&](const float (&a)[3][3]) {
     return radd(radd(rscale(R3(a[0][0], a[0][1], a[0][2]), w0), rscale(R3(a[1][0], a[1][1], a[1][2]), w1)),
                 rscale(R3(a[2][0], a[2][1], a[2][2]), w2));
@@ -551,7 +585,7 @@ __global__ void __launch_bounds__(256) k_raster_resolve(RasterStream S, ImageLay
   const int c = L.channels;
   O.depth[e] = z;
   O.surface_id[e] = src;
-  O.cell_id[e] = T.c[vi];
+  O.cell_id[e] = vi == 0 ? T.c[0] : (vi == 1 ? T.c[1] : T.c[2]);  // constant indices keep the record in registers
   O.position[e * c + 0] = bp.x, O.position[e * c + 1] = bp.y, O.position[e * c + 2] = bp.z;
   O.normal[e * c + 0] = bn.x, O.normal[e * c + 1] = bn.y, O.normal[e * c + 2] = bn.z;
   O.albedo[e * c + 0] = albedo.x, O.albedo[e * c + 1] = albedo.y, O.albedo[e * c + 2] = albedo.z;
