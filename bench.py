@@ -583,6 +583,7 @@ def _summary(frame_4k, luts, timed_s) -> dict:
         if sky:
             out.update({"sky_4k_net_speedup_vs_plain": sky["net_speedup_vs_plain"],
                         "sky_4k_net_err_mean": sky["error_vs_fp64"]["net"]["mean"],
+                        "sky_4k_net_uncalibrated_err_mean": sky["error_vs_fp64"]["net_uncalibrated"]["mean"],
                         "sky_4k_net_ms": sky["net_ms"], "sky_4k_plain_ms": sky["plain_ms"]})
         fused = frame_4k.get("fused_4k")
         if fused:
@@ -1228,7 +1229,8 @@ def _sky_4k(device, args, sg, n_pixels=1500) -> dict:
     ms = o.build_multi_scattering(cfg, EARTH_RADIUS_M, SOLAR_IRRADIANCE, ar, tl)
     rng = np.random.default_rng(SEED + 2)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    times = {"plain": 0.0, "net": 0.0, "lut": 0.0}
+    times = {"plain": 0.0, "net": 0.0, "net_uncalibrated": 0.0, "lut": 0.0}
+    tile = sg.calibration_tile
     errors = {k: [] for k in times}
     cams = []
     basis = camera.view_basis(0.0, 15.0)
@@ -1246,7 +1248,10 @@ def _sky_4k(device, args, sg, n_pixels=1500) -> dict:
         floor = 1e-4 * np.abs(ref).max()
         cam = {"altitude_m": alt, "sun_zenith_deg": v.sun_zenith_deg}
         for mode in times:
-            run = lambda: r.sky_pixels(out, *a, mode=mode, surrogate=sg if mode == "net" else None)
+            # the network with the calibration from 1% checked pixels, and without it
+            sg.calibration_tile = 0 if mode == "net_uncalibrated" else tile
+            kind = "net" if mode.startswith("net") else mode
+            run = lambda: r.sky_pixels(out, *a, mode=kind, surrogate=sg if kind == "net" else None, seed=SEED)
             for _ in range(3):
                 run()
             torch.cuda.synchronize(device)
@@ -1263,6 +1268,7 @@ def _sky_4k(device, args, sg, n_pixels=1500) -> dict:
             cam[f"{mode}_ms"] = ms_mode
             cam[f"{mode}_err_mean"] = float(e.mean())
         cams.append(cam)
+    sg.calibration_tile = tile
     r.check()
     r.close()
     del out
@@ -1272,8 +1278,11 @@ def _sky_4k(device, args, sg, n_pixels=1500) -> dict:
     n = len(SKY_ALTITUDES_M)
     return {"workload": "sky radiance of every pixel of 3840x2160 views (cameras 2 / 20 / 60 km, pitch +15 deg, "
                         "frame-chain sun positions): plain per-pixel sky-view march vs sky network (plain where "
-                        "|sun cosine| < 0.1 or within 0.5 deg of the limb) vs sky-view LUT lookup",
-            "plain_ms": times["plain"] / n, "net_ms": times["net"] / n, "lut_lookup_ms": times["lut"] / n,
+                        "|sun cosine| < 0.1 or within 0.5 deg of the limb; 1% of its pixels checked by the march "
+                        f"and {tile}-pixel tiles calibrated from them; also without the calibration) vs sky-view "
+                        "LUT lookup",
+            "plain_ms": times["plain"] / n, "net_ms": times["net"] / n,
+            "net_uncalibrated_ms": times["net_uncalibrated"] / n, "lut_lookup_ms": times["lut"] / n,
             "net_speedup_vs_plain": times["plain"] / times["net"], "error_vs_fp64": err,
             "pixels_per_camera": n_pixels, "cameras": cams}
 

@@ -1001,6 +1001,7 @@ ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t
 // Validation of an AtmSurrogate against the frame, and the device-side view
 // of its networks, gates and the handle's fallback queue (allocated on first
 // use).  Shared by the surrogate composite and the fused frame.
+int calibration_setup(AtmHandle* h, const AtmSurrogate* sg, atm::SurrogateQueue& Q);
 int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m, double camera_radius_m,
                     atm::SurrogateNets& nets, atm::SurrogateQueue& Q) {
   if (!valid_range(sg->scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
@@ -1062,30 +1063,36 @@ int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m
   Q.items = h->queue + 4;
   Q.stats = sg->stats;
   Q.check_fraction = float(sg->check_fraction);
-  if (sg->calibration_tile != 0) {
-    const int t = sg->calibration_tile;
-    if (t < 16 || t > 256 || (t & (t - 1)) != 0)
-      return fail(ATM_E_INVALID, "calibration_tile must be 0 or a power of two in 16..256");
-    if (!h->calib_lm) {
-      const size_t px = size_t(h->width) * size_t(h->height);
-      const size_t tiles = size_t((h->width + 15) / 16) * size_t((h->height + 15) / 16);
-      float *lm = nullptr, *sums = nullptr;
-      cudaError_t e = cudaMalloc(&lm, px * 3 * sizeof(float));
-      if (e == cudaSuccess) e = cudaMalloc(&sums, tiles * 4 * sizeof(float));
-      if (e != cudaSuccess) {
-        if (lm) cudaFree(lm);
-        return cuda_fail(e, "calibration scratch");
-      }
-      h->calib_lm = lm;
-      h->calib_tiles = sums;
-    }
-    Q.lm = h->calib_lm;
-    Q.tiles = h->calib_tiles;
-    Q.tile_shift = 0;
-    while ((1 << Q.tile_shift) < t) ++Q.tile_shift;
-    Q.tiles_x = (h->width + t - 1) / t;
-  }
+  if (int rc = calibration_setup(h, sg, Q)) return rc;
   Q.seed = sg->seed;
+  return ATM_OK;
+}
+
+// The checked pixels' calibration (AtmSurrogate.calibration_tile): the
+// handle's scratch image and tile sums (allocated on first use) into Q.
+int calibration_setup(AtmHandle* h, const AtmSurrogate* sg, atm::SurrogateQueue& Q) {
+  if (sg->calibration_tile == 0) return ATM_OK;
+  const int t = sg->calibration_tile;
+  if (t < 16 || t > 256 || (t & (t - 1)) != 0)
+    return fail(ATM_E_INVALID, "calibration_tile must be 0 or a power of two in 16..256");
+  if (!h->calib_lm) {
+    const size_t px = size_t(h->width) * size_t(h->height);
+    const size_t tiles = size_t((h->width + 15) / 16) * size_t((h->height + 15) / 16);
+    float *lm = nullptr, *sums = nullptr;
+    cudaError_t e = cudaMalloc(&lm, px * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&sums, tiles * 4 * sizeof(float));
+    if (e != cudaSuccess) {
+      if (lm) cudaFree(lm);
+      return cuda_fail(e, "calibration scratch");
+    }
+    h->calib_lm = lm;
+    h->calib_tiles = sums;
+  }
+  Q.lm = h->calib_lm;
+  Q.tiles = h->calib_tiles;
+  Q.tile_shift = 0;
+  while ((1 << Q.tile_shift) < t) ++Q.tile_shift;
+  Q.tiles_x = (h->width + t - 1) / t;
   return ATM_OK;
 }
 
@@ -1177,9 +1184,20 @@ ATM_API int atm_sky_pixels(AtmHandle* h, int32_t mode, float* radiance, const At
   const atm::CompositeScalars A =
       composite_scalars(h, planet_radius_m, camera_radius_m, sun_local, solar_irradiance, zero3,
                         sun_angular_radius_degrees, view_basis, tangent_half_fov, 0.0, 1.0);
+  atm::SurrogateQueue Q{};
+  if (mode == ATM_SKY_PIXELS_NET) {  // the checked pixels' calibration of the sky network
+    if (!(sg->check_fraction >= 0.0 && sg->check_fraction <= 1.0))
+      return fail(ATM_E_INVALID, "check_fraction must be in [0, 1]");
+    Q.count = h->queue;
+    Q.status = h->queue + 2;
+    Q.items = h->queue + 4;
+    Q.check_fraction = float(sg->check_fraction);
+    Q.seed = sg->seed;
+    if (int rc2 = calibration_setup(h, sg, Q)) return rc2;
+  }
   ATM_CUDA(atm::launch_sky_pixels(mode, h->dev, layout_of(image), A, h->lut[ATM_LUT_TRANSMITTANCE],
                                   h->lut[ATM_LUT_MULTI_SCATTERING], h->lut[ATM_LUT_SKY_VIEW], nets, h->queue + 2,
-                                  radiance, h->samples, static_cast<cudaStream_t>(stream)),
+                                  radiance, h->samples, h->sm_count, static_cast<cudaStream_t>(stream), &Q),
            "sky pixels");
   return ATM_OK;
 }

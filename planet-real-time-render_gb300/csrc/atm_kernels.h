@@ -167,7 +167,8 @@ size_t surrogate_smem_bytes(const SurrogateNets& nets);
 // timeout), 2 the sky-view LUT.
 cudaError_t launch_sky_pixels(int mode, const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                               const float4* tlut, const float4* mslut, const float4* svlut, const SurrogateNets& nets,
-                              uint32_t* status, float* out, unsigned long long* counter, cudaStream_t s);
+                              uint32_t* status, float* out, unsigned long long* counter, int sm_count, cudaStream_t s,
+                              const SurrogateQueue* calibration = nullptr);
 cudaError_t launch_composite_surrogate(const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                                        const float* scene, const float* space, const int32_t* sid, const float* pos,
                                        const float4* tlut, const float4* mslut, const float4* svlut,

@@ -554,7 +554,7 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
                                                        const float4* __restrict__ mslut,
                                                        const float4* __restrict__ svlut, SurrogateNets nets,
                                                        uint32_t* __restrict__ status, float* __restrict__ out,
-                                                       unsigned long long* counter) {
+                                                       unsigned long long* counter, SurrogateQueue Q) {
   extern __shared__ __align__(128) unsigned char smem[];  // the sky network (kSkyPixelsNet)
   __shared__ __align__(8) uint64_t s_mbar[3];
   __shared__ uint32_t s_tmem;
@@ -579,6 +579,7 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
   uint32_t samples = 0;
   f3 sky = splat(0.0f);
   bool plain = kMode == kSkyPixelsPlain;
+  bool checked = false;
   if (kMode == kSkyPixelsLut) sky = sample_sky_view(P, svlut, ray, F.sun, A.sky_alt, A.bottom);
   if (kMode == kSkyPixelsNet) {
     const bool near_limb =
@@ -617,6 +618,7 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
       if ((threadIdx.x & 127) == 0) atomicOr(status, 1u);
     } else if (net) {
       sky = net_radiance(yv, A.E, splat(nets.sky_floor));
+      checked = Q.lm != nullptr && check_pixel(x, y, Q.seed, Q.check_fraction);
     }
   }
   if (inside) {
@@ -628,6 +630,66 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
     out[o + 0] = sky.x;
     out[o + 1] = sky.y;
     out[o + 2] = sky.z;
+    if (kMode == kSkyPixelsNet && Q.lm != nullptr) {  // the calibration's scratch: the network radiance
+      float* lm = Q.lm + 3 * storage_index(L, x, y);
+      lm[0] = plain ? -1.0f : sky.x;
+      if (!plain) {
+        lm[1] = sky.y;
+        lm[2] = sky.z;
+      }
+    }
+  }
+  if (kMode == kSkyPixelsNet) {  // checked network pixels to the queue (warp-aggregated)
+    const int lane = threadIdx.x & 31;
+    const unsigned qm = __ballot_sync(kAll, checked);
+    if (qm) {
+      const int leader = __ffs(qm) - 1;
+      uint32_t base = 0;
+      if (lane == leader) base = atomicAdd(Q.count, uint32_t(__popc(qm)));
+      base = __shfl_sync(kAll, base, leader);
+      if (checked)
+        Q.items[base + __popc(qm & ((1u << lane) - 1u))] = (kQueueSkyCheck << 30) | uint32_t(cy * L.width + cx);
+    }
+  }
+  warp_count(samples, counter);
+}
+
+// The sky-pixel calibration's checks: each queued network pixel gets the
+// plain march, adds its tile's log ratio of plain to network radiance, and
+// keeps the plain result.  Warps take 32 entries per ticket.
+__global__ void __launch_bounds__(256) k_sky_pixels_check(DevParams P, ImageLayout L, CompositeScalars A,
+                                                          const float4* __restrict__ tlut,
+                                                          const float4* __restrict__ mslut, SurrogateQueue Q,
+                                                          float* __restrict__ out, unsigned long long* counter) {
+  const Frame F = make_frame(P, tlut, mslut, A.bottom, A.ar, arr3(A.sun), arr3(A.E));
+  const int lane = threadIdx.x & 31;
+  const uint32_t n = *Q.count;
+  uint32_t samples = 0;
+  for (;;) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(Q.count + 1, 32u);
+    base = __shfl_sync(kAll, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + uint32_t(lane);
+    if (i < n) {
+      const uint32_t p = Q.items[i] & 0x3fffffffu;
+      const int x = int(p % uint32_t(L.width)), y = int(p / uint32_t(L.width));
+      const f3 ray = pixel_ray(L, A, x, y).ray;
+      const f3 sky = sky_radiance(P, F, A.cam_alt, ray);
+      samples += uint32_t(P.sv_steps);
+      float* lm = Q.lm + 3 * storage_index(L, x, y);
+      const f3 Ln = ld3(lm);
+      float* t = Q.tiles + 4 * ((y >> Q.tile_shift) * Q.tiles_x + (x >> Q.tile_shift));
+      atomicAdd(t + 0, clampf(__logf(mx(sky.x, 1e-12f) / mx(Ln.x, 1e-12f)), -kCalibrationClamp, kCalibrationClamp));
+      atomicAdd(t + 1, clampf(__logf(mx(sky.y, 1e-12f) / mx(Ln.y, 1e-12f)), -kCalibrationClamp, kCalibrationClamp));
+      atomicAdd(t + 2, clampf(__logf(mx(sky.z, 1e-12f) / mx(Ln.z, 1e-12f)), -kCalibrationClamp, kCalibrationClamp));
+      atomicAdd(t + 3, 1.0f);
+      lm[0] = -1.0f;
+      const size_t o = pix_offset(L, x, y) * L.channels;
+      out[o + 0] = sky.x;
+      out[o + 1] = sky.y;
+      out[o + 2] = sky.z;
+    }
   }
   warp_count(samples, counter);
 }
@@ -636,18 +698,34 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
 
 cudaError_t launch_sky_pixels(int mode, const DevParams& P, const ImageLayout& L, const CompositeScalars& A,
                               const float4* tlut, const float4* mslut, const float4* svlut, const SurrogateNets& nets,
-                              uint32_t* status, float* out, unsigned long long* counter, cudaStream_t s) {
+                              uint32_t* status, float* out, unsigned long long* counter, int sm_count, cudaStream_t s,
+                              const SurrogateQueue* calibration) {
   const dim3 grid((L.width + 15) / 16, (L.height + 15) / 16);
+  SurrogateQueue Q{};
+  if (mode == kSkyPixelsNet && calibration != nullptr && calibration->lm != nullptr) Q = *calibration;
   if (mode == kSkyPixelsNet) {
     cudaError_t e = cudaFuncSetAttribute(k_sky_pixels<kSkyPixelsNet>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          nets.sky_bytes);
     if (e != cudaSuccess) return e;
+    if (Q.lm != nullptr) {
+      const int tiles_y = (L.height + (1 << Q.tile_shift) - 1) >> Q.tile_shift;
+      e = cudaMemsetAsync(Q.count, 0, 2 * sizeof(uint32_t), s);
+      if (e == cudaSuccess) e = cudaMemsetAsync(Q.tiles, 0, sizeof(float) * 4 * size_t(Q.tiles_x) * tiles_y, s);
+      if (e != cudaSuccess) return e;
+    }
     k_sky_pixels<kSkyPixelsNet><<<grid, 256, nets.sky_bytes, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out,
-                                                                  counter);
+                                                                  counter, Q);
+    e = cudaGetLastError();
+    if (e != cudaSuccess || Q.lm == nullptr) return e;
+    k_sky_pixels_check<<<2 * sm_count, 256, 0, s>>>(P, L, A, tlut, mslut, Q, out, counter);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    const size_t pixels = size_t(L.width) * L.height;
+    k_surrogate_calibrate<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(L, Q, out);
   } else if (mode == kSkyPixelsLut) {
-    k_sky_pixels<kSkyPixelsLut><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter);
+    k_sky_pixels<kSkyPixelsLut><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter, Q);
   } else {
-    k_sky_pixels<kSkyPixelsPlain><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter);
+    k_sky_pixels<kSkyPixelsPlain><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter, Q);
   }
   return cudaGetLastError();
 }

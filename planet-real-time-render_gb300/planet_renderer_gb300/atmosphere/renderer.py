@@ -344,17 +344,20 @@ class AtmosphereRenderer:
 
     def sky_pixels(self, radiance, planet_radius_m: float, camera_radius_m: float, sun_local, solar_irradiance,
                    sun_angular_radius_degrees: float, view_basis, tangent_half_fov: float, mode: str = "plain",
-                   surrogate=None) -> None:
+                   surrogate=None, check_fraction: float = 0.01, seed: int = 0) -> None:
         """Sky radiance along every pixel's view ray into ``radiance``
         (``(W, H, 3|4)`` float32, the renderer's layout): ``mode`` "plain" the
         sky-view march per pixel, "net" the sky network of ``surrogate`` with
         the plain march where a gate trips, "lut" the sky-view LUT of the last
-        ``update``."""
+        ``update``.  In "net" mode with the surrogate's ``calibration_tile``
+        set, a seeded ``check_fraction`` of the network pixels also take the
+        plain march (and keep it), and each tile's mean log ratio of plain to
+        network radiance rescales the tile's other network pixels."""
 
         code = {"plain": _native.ATM_SKY_PIXELS_PLAIN, "net": _native.ATM_SKY_PIXELS_NET,
                 "lut": _native.ATM_SKY_PIXELS_LUT}[mode]
         img = self._image([radiance], None)
-        sg = None if surrogate is None else surrogate.native(check_fraction=0.0)
+        sg = None if surrogate is None else surrogate.native(check_fraction=check_fraction, seed=seed)
         _native.check(self._lib.atm_sky_pixels(
             self._handle, code, ctypes.c_void_p(radiance.data_ptr()), ctypes.byref(img), float(planet_radius_m),
             float(camera_radius_m), _native.d3(sun_local), _native.d3(solar_irradiance),

@@ -522,12 +522,18 @@ def test_sky_pixels_network_against_the_plain_integrator(trained):
     sg = Surrogate(None, sg_full.sky, sg_full.planet_radius_m, sg_full.top_altitude_m, sg_full.scale_height_range)
     r, args = _sky_frame(320, 180, pitch_deg=15.0)
     plain = _sky(r, args, "plain")
-    net = _sky(r, args, "net", sg)
     floor = 1e-4 * np.abs(plain).max()
-    e = np.max(np.abs(net - plain) / np.maximum(np.abs(plain), floor), axis=-1)
+    rel = lambda img: np.max(np.abs(img - plain) / np.maximum(np.abs(plain), floor), axis=-1)
+    sg.calibration_tile = 0
+    e_raw = rel(_sky(r, args, "net", sg))
+    sg.calibration_tile = 32  # 32x32 tiles: about 10 checks each at 1%
+    e = rel(_sky(r, args, "net", sg))
+    print(f"sky network: raw {np.mean(e_raw):.4f} calibrated {np.mean(e):.4f}")
     # the reduced training budget (the sky network's held-out error bound of
-    # test_training_learns_both_networks is 0.15)
-    assert np.mean(e) < 0.25, (np.mean(e), np.quantile(e, 0.99))
+    # test_training_learns_both_networks is 0.15); the calibration from the
+    # 1% checked pixels must not make it worse
+    assert np.mean(e_raw) < 0.25, (np.mean(e_raw), np.quantile(e_raw, 0.99))
+    assert np.mean(e) <= np.mean(e_raw) * 1.02, (np.mean(e), np.mean(e_raw))
     sg.sky_twilight_cosine = 1.0  # gate every pixel
     np.testing.assert_allclose(_sky(r, args, "net", sg), plain, rtol=1e-6, atol=0)
     sg.sky_twilight_cosine = 0.1
