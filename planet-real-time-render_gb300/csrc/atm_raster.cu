@@ -382,9 +382,11 @@ __global__ void __launch_bounds__(256) k_raster_depth(RasterStream S, ImageLayou
       m &= m - 1;
       const long long ql = base + leader;
       const RasterSetup T = load_setup(S.tris + ql);
-      const Box b = bbox(T, L);  // at most kRasterWarpArea pixels: walked by row spans, 32 rows at a time
-      for (int ys = b.y0; ys <= b.y1; ys += kRasterTileH)
-        warp_block(T, (unsigned long long)ql, b.x0, b.x1, ys, min(ys + kRasterTileH - 1, b.y1), L.height, depth_key);
+      const Box b = bbox(T, L);
+      const int bh = b.y1 - b.y0 + 1;
+      const int area = (b.x1 - b.x0 + 1) * bh;  // at most kRasterWarpArea: 8 pixels per lane
+      for (int k = lane; k < area; k += 32)
+        depth_pixel(T, b.x0 + k / bh, b.y0 + k % bh, L.height, depth_key, (unsigned long long)ql);
     }
   }
 }
