@@ -1483,6 +1483,75 @@ def _profile_shade(args):
     print("profile case shade4k:", round(out["ms"], 3), "ms")
 
 
+def _profile_sky_tiles(args):
+    """The learned sky-view workload at 4K (cameras 2 / 20 / 60 km) with the
+    sky network trained as the bench trains it, for calibration tiles of 16,
+    32, 64 and 128 pixels and without the calibration: device ms and mean
+    error against the FP64 march at 1,500 pixels per camera."""
+
+    import numpy as np
+    import torch
+
+    from oracle.atm import Oracle
+    from planet_renderer_gb300 import camera
+    from planet_renderer_gb300.atmosphere import AtmosphereRenderer
+    from planet_renderer_gb300.atmosphere.config import earth_baseline
+    from planet_renderer_gb300.atmosphere.scene import pixel_rays
+    from planet_renderer_gb300.atmosphere.surrogate import (DEFAULT_SPECS, SKY, SampleSource, Surrogate,
+                                                            parameter_grid, train)
+    from planet_renderer_gb300.atmosphere.workloads import (EARTH_RADIUS_M, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG,
+                                                            frame_chain_cameras)
+
+    device = torch.device("cuda:0")
+    torch.cuda.set_device(device)
+    source = SampleSource(parameter_grid(), device=device)
+    net, _ = train(source, SKY, 2**22, 16384, args.mlp_epochs, lr=4e-3, seed=SEED + 1, spec=DEFAULT_SPECS[SKY],
+                   log_every=0)
+    sg = Surrogate(None, net, source.planet_radius_m, source.top_altitude_m, source.scale_height_range)
+    source.close()
+    width, height = 3840, 2160
+    cfg = earth_baseline()
+    r = AtmosphereRenderer(width, height, cfg, device=device)
+    out = torch.empty((width, height, 3), device=device)
+    o = Oracle("f64")
+    ar = math.radians(SUN_ANGULAR_RADIUS_DEG)
+    tl = o.build_transmittance(cfg, EARTH_RADIUS_M)
+    ms = o.build_multi_scattering(cfg, EARTH_RADIUS_M, SOLAR_IRRADIANCE, ar, tl)
+    rng = np.random.default_rng(SEED + 2)
+    basis = camera.view_basis(0.0, 15.0)
+    tanfov = camera.tangent_half_fov(60.0)
+    tiles = (0, 16, 32, 64, 128)
+    res = {t: {"ms": 0.0, "err": []} for t in tiles}
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for alt, v in zip(SKY_ALTITUDES_M, frame_chain_cameras(SEED)):
+        cr = EARTH_RADIUS_M + alt
+        r.update(EARTH_RADIUS_M, cr, v.sun_local.copy(), SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG)
+        a = (EARTH_RADIUS_M, cr, v.sun_local, SOLAR_IRRADIANCE, SUN_ANGULAR_RADIUS_DEG, basis, tanfov)
+        xs = torch.as_tensor(rng.integers(0, width, 1500))
+        ys = torch.as_tensor(rng.integers(0, height, 1500))
+        rays = pixel_rays(width, height, basis, tanfov, xs, ys).numpy()
+        ref = o.sky_rays(cfg, EARTH_RADIUS_M, np.full(1500, alt), rays, np.tile(v.sun_local, (1500, 1)),
+                         SOLAR_IRRADIANCE, ar, tl, ms)
+        floor = 1e-4 * np.abs(ref).max()
+        for t in tiles:
+            sg.calibration_tile = t
+            run = lambda: r.sky_pixels(out, *a, mode="net", surrogate=sg, seed=SEED)
+            for _ in range(3):
+                run()
+            torch.cuda.synchronize(device)
+            start.record()
+            for _ in range(10):
+                run()
+            end.record()
+            torch.cuda.synchronize(device)
+            res[t]["ms"] += start.elapsed_time(end) / 10 / len(SKY_ALTITUDES_M)
+            got = out[xs.to(device), ys.to(device)].cpu().numpy().astype(np.float64)
+            res[t]["err"].append(np.max(np.abs(got - ref) / np.maximum(np.abs(ref), floor), axis=1))
+    r.close()
+    print("profile case sky4k_tiles:", {t: {"ms": round(v["ms"], 4), "err_mean": round(float(np.concatenate(
+        v["err"]).mean()), 5)} for t, v in res.items()})
+
+
 def _profile_raster(args):
     """The terrain raster at 4K, both patch budgets, three frames each."""
 
@@ -1499,6 +1568,7 @@ def _profile_mesh_frame(args):
 
 PROFILE_CASES = {
     "raster4k": _profile_raster,
+    "sky4k_tiles": _profile_sky_tiles,
     "meshframe4k": _profile_mesh_frame,
     "frame1080p": _profile_frame_1080p,
     "frame4k_mlp": _profile_frame_4k_mlp,

@@ -171,6 +171,7 @@ struct AtmHandle {
   uint32_t* queue = nullptr;
   float* calib_lm = nullptr;     // the surrogate calibration's scratch image (width x height x 3)
   float* calib_tiles = nullptr;  // its tile sums, sized for the smallest tile (16 pixels)
+  uint8_t* calib_mask = nullptr; // the sky-pixel workload's network-pixel mask (width x height bytes)
   int sm_count = 0;
 };
 
@@ -300,6 +301,7 @@ ATM_API int atm_destroy(AtmHandle* h) {
   if (h->queue) cudaFree(h->queue);
   if (h->calib_lm) cudaFree(h->calib_lm);
   if (h->calib_tiles) cudaFree(h->calib_tiles);
+  if (h->calib_mask) cudaFree(h->calib_mask);
   delete h;
   return ATM_OK;
 }
@@ -1001,7 +1003,7 @@ ATM_API int atm_surrogate_samples(AtmBatch* b, int32_t kind, int64_t n, uint64_t
 // Validation of an AtmSurrogate against the frame, and the device-side view
 // of its networks, gates and the handle's fallback queue (allocated on first
 // use).  Shared by the surrogate composite and the fused frame.
-int calibration_setup(AtmHandle* h, const AtmSurrogate* sg, atm::SurrogateQueue& Q);
+int calibration_setup(AtmHandle* h, const AtmSurrogate* sg, atm::SurrogateQueue& Q, bool sky_pixels = false);
 int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m, double camera_radius_m,
                     atm::SurrogateNets& nets, atm::SurrogateQueue& Q) {
   if (!valid_range(sg->scale_height_range)) return fail(ATM_E_INVALID, "scale-height range must be 0 < min < max");
@@ -1070,29 +1072,30 @@ int surrogate_setup(AtmHandle* h, const AtmSurrogate* sg, double planet_radius_m
 
 // The checked pixels' calibration (AtmSurrogate.calibration_tile): the
 // handle's scratch image and tile sums (allocated on first use) into Q.
-int calibration_setup(AtmHandle* h, const AtmSurrogate* sg, atm::SurrogateQueue& Q) {
+int calibration_setup(AtmHandle* h, const AtmSurrogate* sg, atm::SurrogateQueue& Q, bool sky_pixels) {
   if (sg->calibration_tile == 0) return ATM_OK;
   const int t = sg->calibration_tile;
   if (t < 16 || t > 256 || (t & (t - 1)) != 0)
     return fail(ATM_E_INVALID, "calibration_tile must be 0 or a power of two in 16..256");
-  if (!h->calib_lm) {
-    const size_t px = size_t(h->width) * size_t(h->height);
+  if (!h->calib_tiles) {
     const size_t tiles = size_t((h->width + 15) / 16) * size_t((h->height + 15) / 16);
-    float *lm = nullptr, *sums = nullptr;
-    cudaError_t e = cudaMalloc(&lm, px * 3 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMalloc(&sums, tiles * 4 * sizeof(float));
-    if (e != cudaSuccess) {
-      if (lm) cudaFree(lm);
-      return cuda_fail(e, "calibration scratch");
-    }
-    h->calib_lm = lm;
-    h->calib_tiles = sums;
+    ATM_CUDA(cudaMalloc(&h->calib_tiles, tiles * 4 * sizeof(float)), "calibration tiles");
   }
-  Q.lm = h->calib_lm;
   Q.tiles = h->calib_tiles;
   Q.tile_shift = 0;
   while ((1 << Q.tile_shift) < t) ++Q.tile_shift;
   Q.tiles_x = (h->width + t - 1) / t;
+  if (sky_pixels) {  // the output holds the network radiance: a byte mask suffices
+    if (!h->calib_mask)
+      ATM_CUDA(cudaMalloc(&h->calib_mask, size_t(h->width) * size_t(h->height)), "calibration mask");
+    Q.net_mask = h->calib_mask;
+    return ATM_OK;
+  }
+  if (!h->calib_lm) {
+    const size_t px = size_t(h->width) * size_t(h->height);
+    ATM_CUDA(cudaMalloc(&h->calib_lm, px * 3 * sizeof(float)), "calibration scratch");
+  }
+  Q.lm = h->calib_lm;
   return ATM_OK;
 }
 
@@ -1193,7 +1196,7 @@ ATM_API int atm_sky_pixels(AtmHandle* h, int32_t mode, float* radiance, const At
     Q.items = h->queue + 4;
     Q.check_fraction = float(sg->check_fraction);
     Q.seed = sg->seed;
-    if (int rc2 = calibration_setup(h, sg, Q)) return rc2;
+    if (int rc2 = calibration_setup(h, sg, Q, true)) return rc2;
   }
   ATM_CUDA(atm::launch_sky_pixels(mode, h->dev, layout_of(image), A, h->lut[ATM_LUT_TRANSMITTANCE],
                                   h->lut[ATM_LUT_MULTI_SCATTERING], h->lut[ATM_LUT_SKY_VIEW], nets, h->queue + 2,

@@ -139,6 +139,10 @@ struct SurrogateQueue {
   float* lm;
   float* tiles;
   int tile_shift, tiles_x;
+  // The sky-pixel workload's calibration marks its network pixels here
+  // instead (one byte per pixel in storage order; the output image holds
+  // the network radiance itself).  Null: not that workload.
+  uint8_t* net_mask;
 };
 // a calibration tile applies when it holds this many checked pixels; each
 // checked pixel's log ratio is clamped to +-kCalibrationClamp

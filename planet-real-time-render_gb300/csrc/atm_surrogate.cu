@@ -618,7 +618,7 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
       if ((threadIdx.x & 127) == 0) atomicOr(status, 1u);
     } else if (net) {
       sky = net_radiance(yv, A.E, splat(nets.sky_floor));
-      checked = Q.lm != nullptr && check_pixel(x, y, Q.seed, Q.check_fraction);
+      checked = Q.net_mask != nullptr && check_pixel(x, y, Q.seed, Q.check_fraction);
     }
   }
   if (inside) {
@@ -630,14 +630,8 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
     out[o + 0] = sky.x;
     out[o + 1] = sky.y;
     out[o + 2] = sky.z;
-    if (kMode == kSkyPixelsNet && Q.lm != nullptr) {  // the calibration's scratch: the network radiance
-      float* lm = Q.lm + 3 * storage_index(L, x, y);
-      lm[0] = plain ? -1.0f : sky.x;
-      if (!plain) {
-        lm[1] = sky.y;
-        lm[2] = sky.z;
-      }
-    }
+    if (kMode == kSkyPixelsNet && Q.net_mask != nullptr)  // the calibration: which pixels are the network's
+      Q.net_mask[storage_index(L, x, y)] = plain ? 0 : 1;
   }
   if (kMode == kSkyPixelsNet) {  // checked network pixels to the queue (warp-aggregated)
     const int lane = threadIdx.x & 31;
@@ -652,6 +646,29 @@ __global__ void __launch_bounds__(256, 2) k_sky_pixels(DevParams P, ImageLayout 
     }
   }
   warp_count(samples, counter);
+}
+
+// The sky-pixel calibration pass: every network pixel of a tile holding
+// enough checked pixels is scaled by the tile's mean ratio.  Thread per
+// pixel in storage order.
+__global__ void __launch_bounds__(256) k_sky_pixels_calibrate(ImageLayout L, SurrogateQueue Q, float* __restrict__ out) {
+  const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i >= size_t(L.width) * size_t(L.height) || Q.net_mask[i] == 0) return;
+  int x, y;
+  if (L.sy <= L.sx) {
+    x = int(i / size_t(L.height));
+    y = int(i % size_t(L.height));
+  } else {
+    y = int(i / size_t(L.width));
+    x = int(i % size_t(L.width));
+  }
+  const float4 t = *reinterpret_cast<const float4*>(Q.tiles + 4 * ((y >> Q.tile_shift) * Q.tiles_x + (x >> Q.tile_shift)));
+  if (t.w < float(kCalibrationMinChecks)) return;
+  const float inv = 1.0f / t.w;
+  const size_t o = pix_offset(L, x, y) * L.channels;
+  out[o + 0] *= __expf(t.x * inv);
+  out[o + 1] *= __expf(t.y * inv);
+  out[o + 2] *= __expf(t.z * inv);
 }
 
 // The sky-pixel calibration's checks: each queued network pixel gets the
@@ -677,15 +694,14 @@ __global__ void __launch_bounds__(256) k_sky_pixels_check(DevParams P, ImageLayo
       const f3 ray = pixel_ray(L, A, x, y).ray;
       const f3 sky = sky_radiance(P, F, A.cam_alt, ray);
       samples += uint32_t(P.sv_steps);
-      float* lm = Q.lm + 3 * storage_index(L, x, y);
-      const f3 Ln = ld3(lm);
+      const size_t o = pix_offset(L, x, y) * L.channels;
+      const f3 Ln = ld3(out + o);  // the network's radiance
       float* t = Q.tiles + 4 * ((y >> Q.tile_shift) * Q.tiles_x + (x >> Q.tile_shift));
       atomicAdd(t + 0, clampf(__logf(mx(sky.x, 1e-12f) / mx(Ln.x, 1e-12f)), -kCalibrationClamp, kCalibrationClamp));
       atomicAdd(t + 1, clampf(__logf(mx(sky.y, 1e-12f) / mx(Ln.y, 1e-12f)), -kCalibrationClamp, kCalibrationClamp));
       atomicAdd(t + 2, clampf(__logf(mx(sky.z, 1e-12f) / mx(Ln.z, 1e-12f)), -kCalibrationClamp, kCalibrationClamp));
       atomicAdd(t + 3, 1.0f);
-      lm[0] = -1.0f;
-      const size_t o = pix_offset(L, x, y) * L.channels;
+      Q.net_mask[storage_index(L, x, y)] = 0;
       out[o + 0] = sky.x;
       out[o + 1] = sky.y;
       out[o + 2] = sky.z;
@@ -702,12 +718,12 @@ cudaError_t launch_sky_pixels(int mode, const DevParams& P, const ImageLayout& L
                               const SurrogateQueue* calibration) {
   const dim3 grid((L.width + 15) / 16, (L.height + 15) / 16);
   SurrogateQueue Q{};
-  if (mode == kSkyPixelsNet && calibration != nullptr && calibration->lm != nullptr) Q = *calibration;
+  if (mode == kSkyPixelsNet && calibration != nullptr && calibration->net_mask != nullptr) Q = *calibration;
   if (mode == kSkyPixelsNet) {
     cudaError_t e = cudaFuncSetAttribute(k_sky_pixels<kSkyPixelsNet>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          nets.sky_bytes);
     if (e != cudaSuccess) return e;
-    if (Q.lm != nullptr) {
+    if (Q.net_mask != nullptr) {
       const int tiles_y = (L.height + (1 << Q.tile_shift) - 1) >> Q.tile_shift;
       e = cudaMemsetAsync(Q.count, 0, 2 * sizeof(uint32_t), s);
       if (e == cudaSuccess) e = cudaMemsetAsync(Q.tiles, 0, sizeof(float) * 4 * size_t(Q.tiles_x) * tiles_y, s);
@@ -716,12 +732,12 @@ cudaError_t launch_sky_pixels(int mode, const DevParams& P, const ImageLayout& L
     k_sky_pixels<kSkyPixelsNet><<<grid, 256, nets.sky_bytes, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out,
                                                                   counter, Q);
     e = cudaGetLastError();
-    if (e != cudaSuccess || Q.lm == nullptr) return e;
+    if (e != cudaSuccess || Q.net_mask == nullptr) return e;
     k_sky_pixels_check<<<2 * sm_count, 256, 0, s>>>(P, L, A, tlut, mslut, Q, out, counter);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     const size_t pixels = size_t(L.width) * L.height;
-    k_surrogate_calibrate<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(L, Q, out);
+    k_sky_pixels_calibrate<<<unsigned((pixels + 255) / 256), 256, 0, s>>>(L, Q, out);
   } else if (mode == kSkyPixelsLut) {
     k_sky_pixels<kSkyPixelsLut><<<grid, 256, 0, s>>>(P, L, A, tlut, mslut, svlut, nets, status, out, counter, Q);
   } else {
