@@ -495,17 +495,25 @@ def main() -> None:
     e2e_steps = 100
     e2e_s, e2e_samples, h2d, d2h = _e2e(r, frames, e2e_steps, 2, device)
 
-    luts = None if args.no_luts else _lut_builds(device, args)
-    frame_4k = None
-    if not args.no_4k:
-        frame_4k = _frame_4k(device, args)
-    batch = None if args.no_batch else _batch(device, args)
-    post = None if args.no_post else _postprocess_4k(device, args)
-    shade = None if args.no_post else _shading_4k(device, args)
-    raster = None if args.no_raster else _raster_4k(device, args)
+    leg_s = {}  # wall seconds of each leg (host time, including its checks against the FP64 oracle)
+
+    def leg(name, skip, fn):
+        if skip:
+            return None
+        t0 = time.perf_counter()
+        out = fn()
+        leg_s[name] = round(time.perf_counter() - t0, 1)
+        return out
+
+    luts = leg("lut_build", args.no_luts, lambda: _lut_builds(device, args))
+    frame_4k = leg("frame_4k", args.no_4k, lambda: _frame_4k(device, args))
+    batch = leg("batch", args.no_batch, lambda: _batch(device, args))
+    post = leg("postprocess_4k", args.no_post, lambda: _postprocess_4k(device, args))
+    shade = leg("shading_4k", args.no_post, lambda: _shading_4k(device, args))
+    raster = leg("raster_4k", args.no_raster, lambda: _raster_4k(device, args))
     mesh_frame = (frame_4k or {}).pop("mesh_4k", None)
-    if mesh_frame is None and not args.no_raster:
-        mesh_frame = _frame_from_mesh_4k(device, args)
+    if mesh_frame is None:
+        mesh_frame = leg("frame_from_mesh_4k", args.no_raster, lambda: _frame_from_mesh_4k(device, args))
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -553,6 +561,7 @@ def main() -> None:
                                      f"{'fallback' if peaks.get('fallback') else 'measured'} copy bandwidth"},
             "cpu_baseline": cpu,
             "clocks": clocks,
+            "leg_seconds": leg_s,
         }
         line.update(_summary(frame_4k, luts, ms_total / 1e3))
         print(json.dumps(line), flush=True)

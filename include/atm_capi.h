@@ -683,7 +683,7 @@ typedef struct AtmOceanImages {
   float* albedo;
   float* material_weights;
   float* height_m;
-  float* water_depth_m;
+  float* water_depth;
   float* seabed_albedo;
   float* seabed_normal;
   float* slope_variance;

@@ -1716,7 +1716,7 @@ ATM_API int atm_ocean_rasterize(AtmOcean* o, const AtmOceanImages* im, const Atm
       image->stride_x <= 0 || image->stride_y <= 0)
     return fail(ATM_E_INVALID, "invalid AtmImage");
   if (!im->depth || !im->position || !im->normal || !im->albedo || !im->material_weights || !im->height_m ||
-      !im->water_depth_m || !im->seabed_albedo || !im->seabed_normal || !im->slope_variance || !im->surface_id ||
+      !im->water_depth || !im->seabed_albedo || !im->seabed_normal || !im->slope_variance || !im->surface_id ||
       !im->cell_id)
     return fail(ATM_E_INVALID, "null G-buffer image");
   if (!(planet_radius_m > 0.0) || !std::isfinite(planet_radius_m) || !std::isfinite(camera_altitude_m) ||
@@ -1777,7 +1777,7 @@ ATM_API int atm_ocean_rasterize(AtmOcean* o, const AtmOceanImages* im, const Atm
   F.enabled = c.enabled ? 1 : 0;
   F.debug_mode = debug_mode;
   atm::OceanImages G{im->depth,      im->position,      im->normal,        im->albedo,
-                     im->material_weights, im->height_m, im->water_depth_m, im->seabed_albedo,
+                     im->material_weights, im->height_m, im->water_depth, im->seabed_albedo,
                      im->seabed_normal, im->slope_variance, im->surface_id, im->cell_id};
   ATM_CUDA(atm::launch_ocean_coverage(o->spectrum, F, layout_of(image), G, s), "ocean coverage");
   return ATM_OK;
